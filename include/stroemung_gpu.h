@@ -1,0 +1,225 @@
+/*
+ * stroemung_gpu.h — C ABI of the GB300-native NaSt2D timestep.
+ *
+ * Drop-in for the timestep surface of the Rust crate wickedchicken/stroemung
+ * (Simulation / SimulationGrid).  All fields live on one GPU; every entry point
+ * takes plain pointers and sizes and returns an int status (STRM_OK = 0).
+ *
+ * Host arrays are [nx][ny] row-major with y the contiguous axis and the
+ * one-cell ring included, exactly like the reference's GridArray
+ * (src/types.rs:12-19); nx, ny are the reference's `size`.
+ *
+ * Threading: one simulation per handle, each with its own CUDA stream.  Calls
+ * on one handle must not overlap; distinct handles are independent.
+ */
+#ifndef STROEMUNG_GPU_H
+#define STROEMUNG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The first two mirror SimulationGridError
+ * (src/grid/mod.rs:51-59): BoundaryTooThinError -> STRM_ERR_THIN_WALL,
+ * BoundaryListIncorrectError -> STRM_ERR_BAD_BOUNDARY. */
+enum {
+    STRM_OK = 0,
+    STRM_ERR_THIN_WALL = 1,    /* a boundary cell has fluid on opposite sides */
+    STRM_ERR_BAD_BOUNDARY = 2, /* a cell code outside the five known kinds */
+    STRM_ERR_NONFINITE = 3,    /* the step completed but its residual is NaN/Inf */
+    STRM_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+    STRM_ERR_CUDA = 5,         /* a CUDA runtime call failed (see strm_last_error) */
+    STRM_ERR_INVALID = 6,      /* bad argument */
+    STRM_ERR_NO_DEVICE = 7     /* no usable sm_103 device */
+};
+
+/* Cell kinds (src/cell.rs:6-23).  STRM_MOVING_WALL is an extension (a wall
+ * whose tangential velocity is the wall's, for the lid-driven cavity). */
+enum {
+    STRM_FLUID = 0,
+    STRM_NO_SLIP = 1,
+    STRM_OUTFLOW = 2,
+    STRM_INFLOW = 3,
+    STRM_MOVING_WALL = 4
+};
+
+/* Fields for strm_download / strm_upload. */
+enum {
+    STRM_FIELD_U = 0,
+    STRM_FIELD_V = 1,
+    STRM_FIELD_P = 2,  /* grid.pressure */
+    STRM_FIELD_F = 3,
+    STRM_FIELD_G = 4,
+    STRM_FIELD_RHS = 5
+};
+
+/* Pressure-solve ordering. */
+enum {
+    STRM_SOR_RED_BLACK = 0,    /* (x+y) even cells, then odd: all SMs */
+    STRM_SOR_LEXICOGRAPHIC = 1 /* the reference's x-major Gauss-Seidel order,
+                                  run as anti-diagonal wavefronts in one CTA:
+                                  bit-identical to the reference, for small grids */
+};
+
+/* Arithmetic of the pressure solve.  Boundary conditions, F/G, RHS and the
+ * velocity update always follow the reference's operation order exactly. */
+enum {
+    STRM_ARITH_EXACT = 0, /* reference operation order, correctly rounded divisions */
+    STRM_ARITH_FAST = 1   /* fused multiply-adds and reciprocal multiplies */
+};
+
+/* Precision of the pressure solve. */
+enum {
+    STRM_PREC_FP64 = 0,  /* plain FP64 SOR */
+    STRM_PREC_MIXED = 1  /* FP32 red-black sweeps on the FP64 defect, FP64 refinement */
+};
+
+/* Mirrors Simulation's parameters (src/simulation.rs:30-69). */
+typedef struct {
+    double dx, dy;            /* cell_size */
+    double delt;              /* time step (the first step's, when tau > 0) */
+    double gamma;             /* donor-cell blend */
+    double reynolds;
+    double eps;               /* sor_absolute_epsilon */
+    double omega;
+    uint32_t max_iterations;
+    uint32_t iterations;
+    double time;
+    double initial_norm_squared; /* NaN: computed at creation, as the
+                                    reference does for `None` */
+    double tau;               /* > 0: adaptive time step, delt =
+                                 tau*min(Re/2/(1/dx^2+1/dy^2), dx/max|u|, dy/max|v|)
+                                 (extension; 0 keeps delt fixed as the reference) */
+} strm_params;
+
+typedef struct {
+    int sor_order;    /* STRM_SOR_* */
+    int arithmetic;   /* STRM_ARITH_* */
+    int precision;    /* STRM_PREC_* */
+    int strict_eps;   /* 1: stop only at ns < eps^2 (not at ns < initial norm) */
+    int inner_sweeps; /* mixed precision: FP32 sweeps per FP64 refinement (0 = 8) */
+} strm_mode;
+
+/* Scalar state readable after any call (pressure_range / speed_range are the
+ * reference's grid fields, src/grid/mod.rs:121-124). */
+typedef struct {
+    double time;
+    uint64_t iterations;
+    double delt;                  /* the time step of the last step */
+    double initial_norm_squared;
+    double fluid_cells;           /* reference's BoundaryList::fluid_cells */
+    double pressure_range[2];
+    double speed_range[2];
+    uint32_t last_sor_iterations;
+    double last_norm_squared;
+    uint32_t last_converged;
+} strm_state;
+
+typedef struct {
+    uint32_t sor_iterations;
+    uint32_t converged;
+    double norm_squared;
+    double delt;
+} strm_step_stats;
+
+typedef struct strm_sim strm_sim;
+
+/* Creates a simulation and runs the construction-time passes of
+ * Simulation::try_from (src/simulation.rs:71-99): classification
+ * (SimulationGrid::try_from, src/grid/mod.rs:127-153), F, G, RHS and the
+ * initial norm.  kinds[nx*ny] are STRM_* cell kinds; wall_uv[2*nx*ny] the
+ * velocity of inflow / moving-wall cells (NULL when there are none); u, v, p
+ * [nx*ny].  On STRM_ERR_THIN_WALL *bad_index (if given) is the first
+ * offending cell x*ny+y in x-major order and *out is NULL. */
+int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
+                const double *wall_uv, const double *u, const double *v, const double *p,
+                strm_sim **out, int64_t *bad_index);
+
+int strm_destroy(strm_sim *sim);
+
+/* Selects ordering / arithmetic / precision; rebuilds the step graph. */
+int strm_set_mode(strm_sim *sim, const strm_mode *mode);
+
+/* Simulation::run_simulation_tick (src/simulation.rs:324-333): boundary
+ * conditions, F/G, RHS, pressure solve, velocity update; time += delt;
+ * iterations += 1.  Returns (sor_iterations, norm_squared).  One CUDA graph
+ * launch and one 64-byte device-to-host read. */
+int strm_tick(strm_sim *sim, uint32_t *sor_iterations, double *norm_squared);
+
+/* n ticks back to back with a single host synchronisation; stats[n] (may be
+ * NULL) receives each tick's results. */
+int strm_step_n(strm_sim *sim, int n, strm_step_stats *stats);
+
+/* Reads / writes a whole field ([nx*ny] host array) — the reference's public
+ * fields grid.u, grid.v, grid.pressure, f, g, rhs (src/simulation.rs:50-69).
+ * Writing u or v refreshes the max|u|, max|v| used by the adaptive step. */
+int strm_download(strm_sim *sim, int field, double *host);
+int strm_upload(strm_sim *sim, int field, const double *host);
+
+/* Reads the cell kinds and the edge codes (0 none, 1 N, 2 NE, 3 E, 4 SE, 5 S,
+ * 6 SW, 7 W, 8 NW — EdgeType, src/grid/mod.rs:19-49) of every cell. */
+int strm_download_cells(strm_sim *sim, uint8_t *kinds, uint8_t *edges);
+
+/* The GUI's paint path (src/lib.rs:38-78) followed by rebuild_boundary_list
+ * (src/grid/mod.rs:202-235): for each of the n cells (xs[i], ys[i]) whose kind
+ * differs from kinds[i], zero its u, v and pressure and set the new kind (and
+ * wall velocity from wall_uv[2*i], may be NULL).  If the new layout has a thin
+ * wall, every change is rolled back and STRM_ERR_THIN_WALL is returned. */
+int strm_edit_cells(strm_sim *sim, int n, const int32_t *xs, const int32_t *ys,
+                    const uint8_t *kinds, const double *wall_uv, int64_t *bad_index);
+
+int strm_get_state(strm_sim *sim, strm_state *out);
+
+/* Individual phases, for callers that drive the pipeline step by step. */
+int strm_set_boundary_u_and_v(strm_sim *sim);      /* src/grid/mod.rs:414-651 */
+int strm_calculate_f_g_rhs(strm_sim *sim);         /* src/simulation.rs:122-214 */
+int strm_copy_pressure_to_boundaries(strm_sim *sim); /* src/grid/mod.rs:343-412 */
+int strm_calculate_norm_squared(strm_sim *sim, double *norm_squared); /* src/simulation.rs:216-227 */
+int strm_set_u_and_v(strm_sim *sim);               /* src/simulation.rs:287-322 */
+int strm_calculate_pressure_range(strm_sim *sim);  /* src/grid/mod.rs:237-251 */
+int strm_calculate_speed_range(strm_sim *sim);     /* src/grid/mod.rs:253-268 */
+
+/* n red-black pressure iterations of the loop body of solve_sor
+ * (src/simulation.rs:250-277: boundary pressure copy, sweep, residual norm)
+ * with no stop test, on the current pressure and RHS, in the selected
+ * arithmetic.  Asynchronous when norm_squared is NULL (see strm_synchronize);
+ * otherwise waits and returns the last iteration's norm. */
+int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
+
+/* Waits until all work queued on the simulation's stream has finished. */
+int strm_synchronize(strm_sim *sim);
+
+/* Device pointers of the fields (pitch in elements) for zero-copy interop. */
+typedef struct {
+    double *u, *v, *p, *f, *g, *rhs;
+    uint8_t *flags;
+    int nx, ny, pitch;
+    void *stream; /* cudaStream_t */
+} strm_device_view;
+int strm_device_view_get(strm_sim *sim, strm_device_view *out);
+
+/* Host-side utilities (no GPU needed).  The same classification and
+ * boundary-program compiler the device path uses, run on host arrays:
+ * strm_host_classify is SimulationGrid::rebuild_boundary_list's edge
+ * computation (src/grid/mod.rs:202-235, 270-332); strm_host_boundary_pass
+ * applies set_boundary_u_and_v (src/grid/mod.rs:414-651) to u, v in place and
+ * writes, for every boundary cell with an edge, the value set_u_and_v's
+ * restore replay (src/simulation.rs:313-320) leaves in u, v. */
+int strm_host_classify(int nx, int ny, const uint8_t *kinds, uint8_t *edges,
+                       double *fluid_cells, int64_t *bad_index);
+int strm_host_boundary_pass(int nx, int ny, const uint8_t *kinds, const double *wall_uv,
+                            double *u, double *v, double *restore_u, double *restore_v);
+
+/* Last error message of the calling thread. */
+int strm_last_error(char *buf, size_t len);
+
+/* Library version, for loaders that check the ABI. */
+int strm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

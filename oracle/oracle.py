@@ -95,6 +95,7 @@ def lib():
         L.orc_calculate_norm_squared.restype = ctypes.c_double
         L.orc_calculate_norm_squared.argtypes = [ctypes.c_void_p]
         L.orc_solve_sor.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), _dp]
+        L.orc_tick_timed.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _dp]
         _lib = L
     return _lib
 
@@ -249,6 +250,12 @@ class OracleSim:
 
     def set_u_and_v(self):
         lib().orc_set_u_and_v(self._h)
+
+    def tick_timed(self, max_iterations_cap: int = 0):
+        """(seconds before the solve, seconds in it, iterations, seconds after)."""
+        out = np.zeros(4)
+        lib().orc_tick_timed(self._h, int(max_iterations_cap), _d(out))
+        return float(out[0]), float(out[1]), int(out[2]), float(out[3])
 
     def adapt_dt(self):
         lib().orc_adapt_dt(self._h)

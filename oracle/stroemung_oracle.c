@@ -7,12 +7,14 @@
  * contract flag matters: the reference is Rust, which never fuses a*b+c, so
  * fusing here would change the last bit of F, G, RHS, p and u/v.
  */
+#define _POSIX_C_SOURCE 199309L
 #include "stroemung_oracle.h"
 
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 /* Rust's x.powi(2) lowers to x*x. */
 static inline double sq(double x) { return x * x; }
@@ -593,4 +595,37 @@ void orc_get_state(const orc_sim *s, double *out8) {
     out8[5] = s->pressure_range[1];
     out8[6] = s->speed_range[0];
     out8[7] = s->speed_range[1];
+}
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* One tick with its phases timed (CPU-baseline sampling): out4 = {seconds
+ * before the pressure solve (dt, boundary pass, F/G, RHS), seconds in the
+ * solve, iterations run, seconds after it (velocity update)}.  A
+ * max_iterations_cap > 0 bounds the solve for this tick only. */
+void orc_tick_timed(orc_sim *s, uint32_t max_iterations_cap, double *out4) {
+    uint32_t saved = s->prm.max_iterations, it = 0;
+    double ns = 0.0;
+    if (max_iterations_cap > 0 && max_iterations_cap < saved) s->prm.max_iterations = max_iterations_cap;
+    double t0 = now_s();
+    orc_adapt_dt(s);
+    orc_set_boundary_u_and_v(s);
+    orc_calculate_f_and_g(s);
+    orc_calculate_rhs(s);
+    double t1 = now_s();
+    orc_solve_sor(s, &it, &ns);
+    double t2 = now_s();
+    orc_set_u_and_v(s);
+    s->prm.time += s->prm.delt;
+    s->prm.iterations += 1;
+    double t3 = now_s();
+    s->prm.max_iterations = saved;
+    out4[0] = t1 - t0;
+    out4[1] = t2 - t1;
+    out4[2] = (double)it;
+    out4[3] = t3 - t2;
 }

@@ -1,0 +1,161 @@
+"""ctypes binding of the C ABI declared in include/stroemung_gpu.h.
+
+Loads the in-tree ``_build/libstroemung_gb300.so`` (building it when absent).
+There is no fallback: if the library cannot be built or loaded, or the
+device is not an sm_103 GPU, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+STRM_OK = 0
+STRM_ERR_THIN_WALL = 1
+STRM_ERR_BAD_BOUNDARY = 2
+STRM_ERR_NONFINITE = 3
+STRM_ERR_TIMEOUT = 4
+STRM_ERR_CUDA = 5
+STRM_ERR_INVALID = 6
+STRM_ERR_NO_DEVICE = 7
+
+FIELD_U, FIELD_V, FIELD_P, FIELD_F, FIELD_G, FIELD_RHS = range(6)
+SOR_RED_BLACK, SOR_LEXICOGRAPHIC = 0, 1
+ARITH_EXACT, ARITH_FAST = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("delt", ctypes.c_double),
+        ("gamma", ctypes.c_double), ("reynolds", ctypes.c_double), ("eps", ctypes.c_double),
+        ("omega", ctypes.c_double), ("max_iterations", ctypes.c_uint32),
+        ("iterations", ctypes.c_uint32), ("time", ctypes.c_double),
+        ("initial_norm_squared", ctypes.c_double), ("tau", ctypes.c_double),
+    ]
+
+
+class Mode(ctypes.Structure):
+    _fields_ = [("sor_order", ctypes.c_int), ("arithmetic", ctypes.c_int),
+                ("precision", ctypes.c_int), ("strict_eps", ctypes.c_int),
+                ("inner_sweeps", ctypes.c_int)]
+
+
+class State(ctypes.Structure):
+    _fields_ = [
+        ("time", ctypes.c_double), ("iterations", ctypes.c_uint64), ("delt", ctypes.c_double),
+        ("initial_norm_squared", ctypes.c_double), ("fluid_cells", ctypes.c_double),
+        ("pressure_range", ctypes.c_double * 2), ("speed_range", ctypes.c_double * 2),
+        ("last_sor_iterations", ctypes.c_uint32), ("last_norm_squared", ctypes.c_double),
+        ("last_converged", ctypes.c_uint32),
+    ]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("sor_iterations", ctypes.c_uint32), ("converged", ctypes.c_uint32),
+                ("norm_squared", ctypes.c_double), ("delt", ctypes.c_double)]
+
+
+class DeviceView(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("p", ctypes.c_void_p),
+                ("f", ctypes.c_void_p), ("g", ctypes.c_void_p), ("rhs", ctypes.c_void_p),
+                ("flags", ctypes.c_void_p), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("pitch", ctypes.c_int), ("stream", ctypes.c_void_p)]
+
+
+# Every function include/stroemung_gpu.h declares, with its ctypes signature.
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+SIGNATURES = {
+    "strm_create": [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp,
+                    ctypes.POINTER(_vp), _i64p],
+    "strm_destroy": [_vp],
+    "strm_set_mode": [_vp, ctypes.POINTER(Mode)],
+    "strm_tick": [_vp, ctypes.POINTER(ctypes.c_uint32), _dp],
+    "strm_step_n": [_vp, ctypes.c_int, ctypes.POINTER(StepStats)],
+    "strm_download": [_vp, ctypes.c_int, _dp],
+    "strm_upload": [_vp, ctypes.c_int, _dp],
+    "strm_download_cells": [_vp, _u8p, _u8p],
+    "strm_edit_cells": [_vp, ctypes.c_int, _i32p, _i32p, _u8p, _dp, _i64p],
+    "strm_get_state": [_vp, ctypes.POINTER(State)],
+    "strm_set_boundary_u_and_v": [_vp],
+    "strm_calculate_f_g_rhs": [_vp],
+    "strm_copy_pressure_to_boundaries": [_vp],
+    "strm_calculate_norm_squared": [_vp, _dp],
+    "strm_set_u_and_v": [_vp],
+    "strm_calculate_pressure_range": [_vp],
+    "strm_calculate_speed_range": [_vp],
+    "strm_device_view_get": [_vp, ctypes.POINTER(DeviceView)],
+    "strm_sor_sweeps": [_vp, ctypes.c_int, _dp],
+    "strm_synchronize": [_vp],
+    "strm_host_classify": [ctypes.c_int, ctypes.c_int, _u8p, _u8p, _dp, _i64p],
+    "strm_host_boundary_pass": [ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp, _dp],
+    "strm_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+    "strm_abi_version": [],
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    from . import build as _build
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads (building first when needed) the in-tree C-ABI library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+    path = _build.LIB
+    if build_if_missing:
+        _build.build()
+    if not path.exists():
+        raise RuntimeError(f"stroemung_gb300 native library missing at {path}")
+    L = ctypes.CDLL(str(path))
+    for name, args in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+class StroemungError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class BoundaryTooThinError(StroemungError):
+    """Mirror of SimulationGridError::BoundaryTooThinError (src/grid/mod.rs:57-58)."""
+
+
+class NonFiniteError(StroemungError):
+    pass
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().strm_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int) -> None:
+    if code == STRM_OK:
+        return
+    msg = last_error()
+    if code == STRM_ERR_THIN_WALL:
+        raise BoundaryTooThinError(code, msg)
+    if code == STRM_ERR_NONFINITE:
+        raise NonFiniteError(code, msg)
+    raise StroemungError(code, msg)
+
+
+NAN = math.nan

@@ -1,0 +1,682 @@
+// C ABI of the GB300 NaSt2D timestep (include/stroemung_gpu.h).
+//
+// Owns the device arena of one simulation, the compiled boundary program and
+// the step graph; every compute call is a kernel or graph launch on the
+// simulation's own stream.  There is no host fallback: without a usable
+// sm_103 device strm_create fails with STRM_ERR_NO_DEVICE.
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/stroemung_gpu.h"
+#include "strm_bcprog.h"
+#include "strm_kernels.cuh"
+
+using namespace strm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(STRM_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                \
+  } while (0)
+
+constexpr int kLogCap = 4096;
+constexpr int kAbiVersion = 1;
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct strm_sim {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  Geom g{};
+  RunCfg cfg{};
+  strm_params prm{};
+  strm_mode mode{};
+  DevFields d{};
+  void *arena = nullptr;
+  std::vector<uint8_t> kind;   // dense host copy of the cell kinds
+  std::vector<double> wall;    // dense [nx][ny][2]
+  std::vector<uint8_t> edge;   // dense edge codes (from the device classification)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  StepState *h_st = nullptr;   // pinned
+  StepLog *h_log = nullptr;    // pinned
+  int bc_cap = 0, pcopy_cap = 0;
+};
+
+namespace {
+
+double *field_ptr(strm_sim *s, int field) {
+  switch (field) {
+    case STRM_FIELD_U: return s->d.u;
+    case STRM_FIELD_V: return s->d.v;
+    case STRM_FIELD_P: return s->d.p;
+    case STRM_FIELD_F: return s->d.f;
+    case STRM_FIELD_G: return s->d.g;
+    case STRM_FIELD_RHS: return s->d.rhs;
+    default: return nullptr;
+  }
+}
+
+Consts make_consts(const strm_params &p) {
+  Consts c{};
+  c.dx = p.dx;
+  c.dy = p.dy;
+  c.gamma = p.gamma;
+  c.re = p.reynolds;
+  c.dx2 = p.dx * p.dx;
+  c.dy2 = p.dy * p.dy;
+  c.four_dx = 4.0 * p.dx;
+  c.four_dy = 4.0 * p.dy;
+  c.r_dx = 1.0 / c.dx;
+  c.r_dy = 1.0 / c.dy;
+  c.r_dx2 = 1.0 / c.dx2;
+  c.r_dy2 = 1.0 / c.dy2;
+  c.r_four_dx = 1.0 / c.four_dx;
+  c.r_four_dy = 1.0 / c.four_dy;
+  c.r_re = 1.0 / c.re;
+  // src/simulation.rs:240-246
+  c.one_minus_w = 1.0 - p.omega;
+  c.middle = p.omega / ((2.0 / c.dx2) + (2.0 / c.dy2));
+  c.eps2 = p.eps * p.eps;
+  return c;
+}
+
+void update_cfg(strm_sim *s) {
+  RunCfg &r = s->cfg;
+  r.g = s->g;
+  r.c = make_consts(s->prm);
+  r.tau = s->prm.tau;
+  r.delt = s->prm.delt;
+  r.itermax = s->prm.max_iterations;
+  r.strict_eps = s->mode.strict_eps;
+  r.sor_order = s->mode.sor_order == STRM_SOR_LEXICOGRAPHIC ? 1 : 0;
+  // grids without interior cells run the single-CTA solve, which handles them
+  if (s->g.nx < 3 || s->g.ny < 3) r.sor_order = 1;
+  r.arith = s->mode.arithmetic == STRM_ARITH_FAST ? 1 : 0;
+  r.precision = s->mode.precision;
+  r.inner_sweeps = s->mode.inner_sweeps > 0 ? s->mode.inner_sweeps : 8;
+}
+
+int rebuild_graph(strm_sim *s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+  update_cfg(s);
+  CK(build_step_graph(s->d, s->cfg, &s->graph));
+  CK(cudaGraphInstantiate(&s->exec, s->graph, 0));
+  return STRM_OK;
+}
+
+int sync_state(strm_sim *s) {
+  CK(cudaMemcpyAsync(s->h_st, s->d.st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+// Device classification + host compile of the boundary program.
+int classify_and_compile(strm_sim *s, long long *bad_out) {
+  const Geom &g = s->g;
+  const long long none = 0x7fffffffffffffffLL;
+  CK(cudaMemcpyAsync(s->d.first_bad, &none, sizeof none, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemsetAsync(s->d.fluid_count, 0, sizeof(unsigned long long), s->stream));
+  CK(launch_classify(s->d, g, s->stream));
+  long long bad = none;
+  unsigned long long fluid = 0;
+  CK(cudaMemcpyAsync(&bad, s->d.first_bad, sizeof bad, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(&fluid, s->d.fluid_count, sizeof fluid, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (bad != none) {
+    if (bad_out) *bad_out = bad;
+    return fail(STRM_ERR_THIN_WALL, "cell (%lld, %lld) has fluid on opposing sides",
+                bad / g.ny, bad % g.ny);
+  }
+  std::vector<uint8_t> flags((size_t)g.nx * g.ny);
+  CK(cudaMemcpy2DAsync(flags.data(), g.ny, s->d.flags, g.pitch, g.ny, g.nx,
+                       cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->edge.resize(flags.size());
+  for (size_t i = 0; i < flags.size(); ++i) s->edge[i] = edge_of(flags[i]);
+  std::vector<BcEntry> prog;
+  std::vector<PCopy> pc;
+  compile_boundary_program(g.nx, g.ny, g.pitch, s->kind.data(), s->edge.data(), s->wall.data(),
+                           prog, pc);
+  if ((int)prog.size() > s->bc_cap) {
+    if (s->d.bc) cudaFree(s->d.bc);
+    if (s->d.bc_val) cudaFree(s->d.bc_val);
+    s->d.bc = nullptr;
+    s->d.bc_val = nullptr;
+    s->bc_cap = (int)prog.size() + 1024;
+    CK(cudaMalloc(&s->d.bc, sizeof(BcEntry) * s->bc_cap));
+    CK(cudaMalloc(&s->d.bc_val, sizeof(double) * s->bc_cap));
+  }
+  if ((int)pc.size() > s->pcopy_cap) {
+    if (s->d.pcopy) cudaFree(s->d.pcopy);
+    s->d.pcopy = nullptr;
+    s->pcopy_cap = (int)pc.size() + 1024;
+    CK(cudaMalloc(&s->d.pcopy, sizeof(PCopy) * s->pcopy_cap));
+  }
+  s->d.n_bc = (int)prog.size();
+  s->d.n_pcopy = (int)pc.size();
+  if (!prog.empty())
+    CK(cudaMemcpyAsync(s->d.bc, prog.data(), sizeof(BcEntry) * prog.size(),
+                       cudaMemcpyHostToDevice, s->stream));
+  if (!pc.empty())
+    CK(cudaMemcpyAsync(s->d.pcopy, pc.data(), sizeof(PCopy) * pc.size(), cudaMemcpyHostToDevice,
+                       s->stream));
+  const double fc = (double)fluid;
+  CK(cudaMemcpyAsync(&s->d.st->fluid_cells, &fc, sizeof fc, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+void free_sim(strm_sim *s) {
+  if (!s) return;
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  if (s->arena) cudaFree(s->arena);
+  if (s->d.bc) cudaFree(s->d.bc);
+  if (s->d.bc_val) cudaFree(s->d.bc_val);
+  if (s->d.pcopy) cudaFree(s->d.pcopy);
+  if (s->h_st) cudaFreeHost(s->h_st);
+  if (s->h_log) cudaFreeHost(s->h_log);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+int check_device(int *dev_out) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(STRM_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  int major = 0, minor = 0;
+  CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (major != 10 || minor != 3)
+    return fail(STRM_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a",
+                dev, major, minor);
+  *dev_out = dev;
+  return STRM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int strm_abi_version(void) { return kAbiVersion; }
+
+int strm_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return STRM_ERR_INVALID;
+  snprintf(buf, len, "%s", g_last_error.c_str());
+  return STRM_OK;
+}
+
+int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
+                const double *wall_uv, const double *u, const double *v, const double *p,
+                strm_sim **out, int64_t *bad_index) {
+  if (!out) return fail(STRM_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!params || !kinds || !u || !v || !p || nx < 1 || ny < 1)
+    return fail(STRM_ERR_INVALID, "invalid arguments");
+  const size_t ncell = (size_t)nx * ny;
+  for (size_t i = 0; i < ncell; ++i)
+    if (kinds[i] > STRM_MOVING_WALL)
+      return fail(STRM_ERR_BAD_BOUNDARY, "cell %zu has unknown kind %u", i, (unsigned)kinds[i]);
+  if (!(params->dx > 0.0) || !(params->dy > 0.0) || !(params->reynolds != 0.0))
+    return fail(STRM_ERR_INVALID, "cell sizes must be positive and reynolds non-zero");
+  int dev = 0;
+  int rc = check_device(&dev);
+  if (rc) return rc;
+
+  strm_sim *s = new (std::nothrow) strm_sim();
+  if (!s) return fail(STRM_ERR_INVALID, "out of host memory");
+  s->dev = dev;
+  s->prm = *params;
+  s->mode = strm_mode{STRM_SOR_RED_BLACK, STRM_ARITH_EXACT, STRM_PREC_FP64, 0, 0};
+  s->g.nx = nx;
+  s->g.ny = ny;
+  s->g.pitch = (int)align_up((size_t)ny, 16);
+  s->kind.assign(kinds, kinds + ncell);
+  s->wall.assign(2 * ncell, 0.0);
+  if (wall_uv) s->wall.assign(wall_uv, wall_uv + 2 * ncell);
+
+#define CKS(call)              \
+  do {                         \
+    int rc_ = (call);          \
+    if (rc_) {                 \
+      free_sim(s);             \
+      return rc_;              \
+    }                          \
+  } while (0)
+#define CKC(call) CKS([&]() -> int { CK(call); return STRM_OK; }())
+
+  CKC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  const size_t nfield = (size_t)nx * s->g.pitch;
+  const int nb = residual_blocks(s->g);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  const size_t o_u = take(nfield * 8), o_v = take(nfield * 8), o_p = take(nfield * 8);
+  const size_t o_f = take(nfield * 8), o_g = take(nfield * 8), o_rhs = take(nfield * 8);
+  const size_t o_ru = take(nfield * 8), o_rv = take(nfield * 8), o_pw = take(nfield * 8);
+  const size_t o_e32 = take(nfield * 4), o_r32 = take(nfield * 4);
+  const size_t o_fl = take(nfield);
+  const size_t o_st = take(sizeof(StepState));
+  const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
+  const size_t o_log = take(sizeof(StepLog) * kLogCap);
+  const size_t o_bad = take(8), o_fc = take(8);
+  CKC(cudaMalloc(&s->arena, off));
+  char *base = (char *)s->arena;
+  DevFields &d = s->d;
+  d.u = (double *)(base + o_u);
+  d.v = (double *)(base + o_v);
+  d.p = (double *)(base + o_p);
+  d.f = (double *)(base + o_f);
+  d.g = (double *)(base + o_g);
+  d.rhs = (double *)(base + o_rhs);
+  d.ru = (double *)(base + o_ru);
+  d.rv = (double *)(base + o_rv);
+  d.pw = (double *)(base + o_pw);
+  d.e32 = (float *)(base + o_e32);
+  d.r32 = (float *)(base + o_r32);
+  d.flags = (uint8_t *)(base + o_fl);
+  d.st = (StepState *)(base + o_st);
+  d.partials = (double *)(base + o_part);
+  d.n_partials = 4 * nb;
+  d.log = (StepLog *)(base + o_log);
+  d.first_bad = (long long *)(base + o_bad);
+  d.fluid_count = (unsigned long long *)(base + o_fc);
+  CKC(cudaMemsetAsync(s->arena, 0, off, s->stream));
+  CKC(cudaMallocHost(&s->h_st, sizeof(StepState)));
+  CKC(cudaMallocHost(&s->h_log, sizeof(StepLog) * kLogCap));
+
+  const Geom &g = s->g;
+  const size_t pb = (size_t)g.pitch * 8;
+  CKC(cudaMemcpy2DAsync(d.u, pb, u, (size_t)ny * 8, (size_t)ny * 8, nx, cudaMemcpyHostToDevice,
+                        s->stream));
+  CKC(cudaMemcpy2DAsync(d.v, pb, v, (size_t)ny * 8, (size_t)ny * 8, nx, cudaMemcpyHostToDevice,
+                        s->stream));
+  CKC(cudaMemcpy2DAsync(d.p, pb, p, (size_t)ny * 8, (size_t)ny * 8, nx, cudaMemcpyHostToDevice,
+                        s->stream));
+  CKC(cudaMemcpy2DAsync(d.flags, g.pitch, kinds, ny, ny, nx, cudaMemcpyHostToDevice, s->stream));
+
+  StepState st{};
+  st.dt = params->delt;
+  st.time = params->time;
+  st.iterations = params->iterations;
+  st.ns0 = isnan(params->initial_norm_squared) ? 0.0 : params->initial_norm_squared;
+  st.umax = st.vmax = 1.0e-10;
+  st.p_min = st.s2_min = ord_enc(DBL_MAX);
+  st.p_max = st.s2_max = ord_enc(0.0);
+  st.log_cap = kLogCap;
+  CKC(cudaMemcpyAsync(d.st, &st, sizeof st, cudaMemcpyHostToDevice, s->stream));
+
+  long long bad = -1;
+  rc = classify_and_compile(s, &bad);
+  if (rc) {
+    if (bad_index) *bad_index = bad;
+    free_sim(s);
+    return rc;
+  }
+  update_cfg(s);
+  // construction passes of SimulationGrid::try_from and Simulation::try_from
+  CKC(launch_prange(d, s->cfg, s->stream, 1));
+  CKC(launch_velocity(d, s->cfg, s->stream, 0, 1, 0));
+  CKC(launch_fg_rhs(d, s->cfg, s->stream));
+  if (isnan(params->initial_norm_squared)) CKC(launch_norm(d, s->cfg, s->stream, 1));
+  CKS(rebuild_graph(s));
+  CKS(sync_state(s));
+#undef CKC
+#undef CKS
+  *out = s;
+  return STRM_OK;
+}
+
+int strm_destroy(strm_sim *sim) {
+  if (!sim) return STRM_ERR_INVALID;
+  cudaSetDevice(sim->dev);
+  cudaStreamSynchronize(sim->stream);
+  free_sim(sim);
+  return STRM_OK;
+}
+
+int strm_set_mode(strm_sim *s, const strm_mode *mode) {
+  if (!s || !mode) return fail(STRM_ERR_INVALID, "invalid arguments");
+  if (mode->sor_order < 0 || mode->sor_order > 1 || mode->arithmetic < 0 ||
+      mode->arithmetic > 1 || mode->precision < 0 || mode->precision > 1)
+    return fail(STRM_ERR_INVALID, "unknown mode value");
+  CK(cudaSetDevice(s->dev));
+  s->mode = *mode;
+  return rebuild_graph(s);
+}
+
+int strm_tick(strm_sim *s, uint32_t *sor_iterations, double *norm_squared) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(cudaGraphLaunch(s->exec, s->stream));
+  int rc = sync_state(s);
+  if (rc) return rc;
+  if (sor_iterations) *sor_iterations = s->h_st->sor_iters;
+  if (norm_squared) *norm_squared = s->h_st->ns;
+  if (s->h_st->overrun) return fail(STRM_ERR_TIMEOUT, "pressure loop passed its bound");
+  if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return STRM_OK;
+}
+
+int strm_step_n(strm_sim *s, int n, strm_step_stats *stats) {
+  if (!s || n < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  int done = 0;
+  while (done < n) {
+    const int chunk = (n - done) < kLogCap ? (n - done) : kLogCap;
+    const unsigned int zero = 0;
+    CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                       s->stream));
+    for (int i = 0; i < chunk; ++i) CK(cudaGraphLaunch(s->exec, s->stream));
+    if (stats)
+      CK(cudaMemcpyAsync(s->h_log, s->d.log, sizeof(StepLog) * chunk, cudaMemcpyDeviceToHost,
+                         s->stream));
+    int rc = sync_state(s);
+    if (rc) return rc;
+    if (stats)
+      for (int i = 0; i < chunk; ++i) {
+        stats[done + i].sor_iterations = s->h_log[i].sor_iters;
+        stats[done + i].converged = s->h_log[i].converged;
+        stats[done + i].norm_squared = s->h_log[i].ns;
+        stats[done + i].delt = s->h_log[i].dt;
+      }
+    done += chunk;
+    if (s->h_st->overrun) return fail(STRM_ERR_TIMEOUT, "pressure loop passed its bound");
+  }
+  if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return STRM_OK;
+}
+
+int strm_download(strm_sim *s, int field, double *host) {
+  if (!s || !host) return fail(STRM_ERR_INVALID, "invalid arguments");
+  double *src = field_ptr(s, field);
+  if (!src) return fail(STRM_ERR_INVALID, "unknown field %d", field);
+  CK(cudaSetDevice(s->dev));
+  const Geom &g = s->g;
+  CK(cudaMemcpy2DAsync(host, (size_t)g.ny * 8, src, (size_t)g.pitch * 8, (size_t)g.ny * 8, g.nx,
+                       cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_upload(strm_sim *s, int field, const double *host) {
+  if (!s || !host) return fail(STRM_ERR_INVALID, "invalid arguments");
+  double *dst = field_ptr(s, field);
+  if (!dst) return fail(STRM_ERR_INVALID, "unknown field %d", field);
+  CK(cudaSetDevice(s->dev));
+  const Geom &g = s->g;
+  CK(cudaMemcpy2DAsync(dst, (size_t)g.pitch * 8, host, (size_t)g.ny * 8, (size_t)g.ny * 8, g.nx,
+                       cudaMemcpyHostToDevice, s->stream));
+  if (field == STRM_FIELD_U || field == STRM_FIELD_V)
+    CK(launch_velocity(s->d, s->cfg, s->stream, 0, 0, 0));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_download_cells(strm_sim *s, uint8_t *kinds, uint8_t *edges) {
+  if (!s) return fail(STRM_ERR_INVALID, "invalid arguments");
+  const Geom &g = s->g;
+  std::vector<uint8_t> flags((size_t)g.nx * g.ny);
+  CK(cudaSetDevice(s->dev));
+  CK(cudaMemcpy2DAsync(flags.data(), g.ny, s->d.flags, g.pitch, g.ny, g.nx,
+                       cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (size_t i = 0; i < flags.size(); ++i) {
+    if (kinds) kinds[i] = kind_of(flags[i]);
+    if (edges) edges[i] = edge_of(flags[i]);
+  }
+  return STRM_OK;
+}
+
+int strm_edit_cells(strm_sim *s, int n, const int32_t *xs, const int32_t *ys,
+                    const uint8_t *kinds, const double *wall_uv, int64_t *bad_index) {
+  if (!s || n < 0 || (n > 0 && (!xs || !ys || !kinds)))
+    return fail(STRM_ERR_INVALID, "invalid arguments");
+  const Geom &g = s->g;
+  for (int i = 0; i < n; ++i) {
+    if (xs[i] < 0 || xs[i] >= g.nx || ys[i] < 0 || ys[i] >= g.ny)
+      return fail(STRM_ERR_INVALID, "cell (%d, %d) outside the grid", xs[i], ys[i]);
+    if (kinds[i] > STRM_MOVING_WALL)
+      return fail(STRM_ERR_BAD_BOUNDARY, "unknown kind %u", (unsigned)kinds[i]);
+  }
+  CK(cudaSetDevice(s->dev));
+  struct Backup {
+    size_t dense, off;
+    double u, v, p, wu, wv;
+    uint8_t kind;
+  };
+  std::vector<Backup> backup;
+  const double zero = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const size_t dense = (size_t)xs[i] * g.ny + ys[i];
+    const size_t off = (size_t)xs[i] * g.pitch + ys[i];
+    const double wu = wall_uv ? wall_uv[2 * i] : 0.0, wv = wall_uv ? wall_uv[2 * i + 1] : 0.0;
+    if (s->kind[dense] == kinds[i] && s->wall[2 * dense] == wu && s->wall[2 * dense + 1] == wv)
+      continue;
+    Backup b{dense, off, 0, 0, 0, s->wall[2 * dense], s->wall[2 * dense + 1], s->kind[dense]};
+    CK(cudaMemcpyAsync(&b.u, s->d.u + off, 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&b.v, s->d.v + off, 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&b.p, s->d.p + off, 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    backup.push_back(b);
+    if (s->kind[dense] != kinds[i]) {
+      CK(cudaMemcpyAsync(s->d.u + off, &zero, 8, cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d.v + off, &zero, 8, cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d.p + off, &zero, 8, cudaMemcpyHostToDevice, s->stream));
+    }
+    s->kind[dense] = kinds[i];
+    s->wall[2 * dense] = wu;
+    s->wall[2 * dense + 1] = wv;
+    CK(cudaMemcpyAsync(s->d.flags + off, &s->kind[dense], 1, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  if (backup.empty()) return STRM_OK;
+  long long bad = -1;
+  int rc = classify_and_compile(s, &bad);
+  if (rc == STRM_ERR_THIN_WALL) {
+    for (auto it = backup.rbegin(); it != backup.rend(); ++it) {
+      s->kind[it->dense] = it->kind;
+      s->wall[2 * it->dense] = it->wu;
+      s->wall[2 * it->dense + 1] = it->wv;
+      CK(cudaMemcpyAsync(s->d.u + it->off, &it->u, 8, cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d.v + it->off, &it->v, 8, cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d.p + it->off, &it->p, 8, cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d.flags + it->off, &s->kind[it->dense], 1, cudaMemcpyHostToDevice,
+                         s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+    }
+    int rc2 = classify_and_compile(s, nullptr);
+    if (rc2) return rc2;
+    if (bad_index) *bad_index = bad;
+    rebuild_graph(s);
+    return fail(STRM_ERR_THIN_WALL, "cell (%lld, %lld) has fluid on opposing sides; edit rolled back",
+                bad / g.ny, bad % g.ny);
+  }
+  if (rc) return rc;
+  CK(launch_velocity(s->d, s->cfg, s->stream, 0, 0, 0));
+  return rebuild_graph(s);
+}
+
+int strm_get_state(strm_sim *s, strm_state *out) {
+  if (!s || !out) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  int rc = sync_state(s);
+  if (rc) return rc;
+  const StepState &st = *s->h_st;
+  out->time = st.time;
+  out->iterations = st.iterations;
+  out->delt = st.dt;
+  out->initial_norm_squared = st.ns0;
+  out->fluid_cells = st.fluid_cells;
+  out->pressure_range[0] = ord_dec(st.p_min);
+  out->pressure_range[1] = ord_dec(st.p_max);
+  out->speed_range[0] = ord_dec(st.s2_min);
+  out->speed_range[1] = ord_dec(st.s2_max);
+  out->last_sor_iterations = st.sor_iters;
+  out->last_norm_squared = st.ns;
+  out->last_converged = st.converged;
+  return STRM_OK;
+}
+
+int strm_set_boundary_u_and_v(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_bc(s->d, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_calculate_f_g_rhs(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_fg_rhs(s->d, s->cfg, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_copy_pressure_to_boundaries(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_pcopy(s->d, s->g, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_calculate_norm_squared(strm_sim *s, double *norm_squared) {
+  if (!s || !norm_squared) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  const double zero = 0.0;
+  CK(cudaMemcpyAsync(&s->d.st->aux, &zero, 8, cudaMemcpyHostToDevice, s->stream));
+  CK(launch_norm(s->d, s->cfg, s->stream, 0));
+  int rc = sync_state(s);
+  if (rc) return rc;
+  *norm_squared = s->h_st->aux;
+  return STRM_OK;
+}
+
+int strm_sor_sweeps(strm_sim *s, int n, double *norm_squared) {
+  if (!s || n < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  for (int i = 0; i < n; ++i) CK(launch_sor_iteration(s->d, s->cfg, s->stream));
+  if (!norm_squared) return STRM_OK;
+  int rc = sync_state(s);
+  if (rc) return rc;
+  *norm_squared = s->h_st->aux;
+  return STRM_OK;
+}
+
+int strm_synchronize(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_set_u_and_v(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_velocity(s->d, s->cfg, s->stream, 1, 1, 0));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_calculate_pressure_range(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_prange(s->d, s->cfg, s->stream, 1));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_calculate_speed_range(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_velocity(s->d, s->cfg, s->stream, 0, 1, 0));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_device_view_get(strm_sim *s, strm_device_view *out) {
+  if (!s || !out) return fail(STRM_ERR_INVALID, "invalid arguments");
+  out->u = s->d.u;
+  out->v = s->d.v;
+  out->p = s->d.p;
+  out->f = s->d.f;
+  out->g = s->d.g;
+  out->rhs = s->d.rhs;
+  out->flags = s->d.flags;
+  out->nx = s->g.nx;
+  out->ny = s->g.ny;
+  out->pitch = s->g.pitch;
+  out->stream = (void *)s->stream;
+  return STRM_OK;
+}
+
+int strm_host_classify(int nx, int ny, const uint8_t *kinds, uint8_t *edges,
+                       double *fluid_cells, int64_t *bad_index) {
+  if (nx < 1 || ny < 1 || !kinds || !edges) return fail(STRM_ERR_INVALID, "invalid arguments");
+  for (size_t i = 0; i < (size_t)nx * ny; ++i)
+    if (kinds[i] > STRM_MOVING_WALL) return fail(STRM_ERR_BAD_BOUNDARY, "unknown kind");
+  long long bad = -1;
+  if (!classify_host(nx, ny, kinds, edges, fluid_cells, &bad)) {
+    if (bad_index) *bad_index = bad;
+    return fail(STRM_ERR_THIN_WALL, "cell (%lld, %lld) has fluid on opposing sides", bad / ny,
+                bad % ny);
+  }
+  return STRM_OK;
+}
+
+int strm_host_boundary_pass(int nx, int ny, const uint8_t *kinds, const double *wall_uv,
+                            double *u, double *v, double *restore_u, double *restore_v) {
+  if (nx < 1 || ny < 1 || !kinds || !u || !v || !restore_u || !restore_v)
+    return fail(STRM_ERR_INVALID, "invalid arguments");
+  std::vector<uint8_t> edge((size_t)nx * ny);
+  long long bad = -1;
+  int rc = strm_host_classify(nx, ny, kinds, edge.data(), nullptr, (int64_t *)&bad);
+  if (rc) return rc;
+  std::vector<double> wall(2 * (size_t)nx * ny, 0.0);
+  if (wall_uv) wall.assign(wall_uv, wall_uv + 2 * (size_t)nx * ny);
+  std::vector<BcEntry> prog;
+  std::vector<PCopy> pc;
+  compile_boundary_program(nx, ny, ny, kinds, edge.data(), wall.data(), prog, pc);
+  apply_boundary_program_host(prog, u, v, restore_u, restore_v);
+  return STRM_OK;
+}
+
+}  // extern "C"

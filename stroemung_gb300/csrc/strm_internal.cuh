@@ -1,0 +1,151 @@
+// Internal device-side definitions shared by the stroemung GB300 kernels.
+//
+// Data layout in HBM (one arena per simulation):
+//   every field is [nx][pitch] with y the contiguous axis, row x at x*pitch,
+//   pitch = ny rounded up to 16 elements (128 B for FP64), rows 128-B aligned.
+//   flags: one byte per cell, same [nx][pitch] indexing:
+//     bits 0-2  cell kind   (0 fluid, 1 no-slip, 2 outflow, 3 inflow, 4 moving wall)
+//     bits 3-6  edge code   (0 none, 1 N, 2 NE, 3 E, 4 SE, 5 S, 6 SW, 7 W, 8 NW)
+//   The edge code is the reference's EdgeType (src/grid/mod.rs:19-49), in its
+//   declaration order; "north" is y-1 (src/grid/mod.rs:168-170).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+namespace strm {
+
+enum : uint8_t { K_FLUID = 0, K_NO_SLIP = 1, K_OUTFLOW = 2, K_INFLOW = 3, K_MOVING = 4 };
+enum : uint8_t {
+  E_NONE = 0, E_N = 1, E_NE = 2, E_E = 3, E_SE = 4, E_S = 5, E_SW = 6, E_W = 7, E_NW = 8
+};
+
+__host__ __device__ __forceinline__ uint8_t kind_of(uint8_t f) { return f & 7u; }
+__host__ __device__ __forceinline__ uint8_t edge_of(uint8_t f) { return (f >> 3) & 15u; }
+__host__ __device__ __forceinline__ bool is_bnd(uint8_t f) { return (f & 7u) != 0; }
+
+// Geometry of one simulation's device fields.
+struct Geom {
+  int nx, ny;
+  int pitch;  // elements per row
+};
+
+// Constants of the stencils, with the exact reciprocals the correctly
+// rounded division needs (see xdiv).
+struct Consts {
+  double dx, dy, gamma, re;
+  double dx2, dy2;      // dx*dx, dy*dy   (reference: delx.powi(2))
+  double four_dx, four_dy;
+  double r_dx, r_dy, r_dx2, r_dy2, r_four_dx, r_four_dy, r_re;
+  // pressure solve
+  double one_minus_w, middle;  // 1-omega, omega/((2/dx2)+(2/dy2))
+  double eps2;
+};
+
+// Per-simulation device state.  Written by kernels, read by the host after
+// each step (one small D2H copy).
+struct StepState {
+  double dt;           // delt of the current step
+  double time;
+  double ns0;          // initial_norm_squared
+  double ns;           // norm_squared of the last pressure iteration
+  double fluid_cells;
+  double umax, vmax;   // max |u|, |v| over every cell (adaptive dt input)
+  double aux;          // result of a standalone norm
+  unsigned long long iterations;
+  unsigned int sor_iters;
+  unsigned int converged;   // pressure solve met its stop rule
+  unsigned int exhausted;   // pressure solve ran max_iterations
+  unsigned int nonfinite;   // last norm was NaN/Inf
+  unsigned int body_count;  // launches of the pressure-loop body this step
+  unsigned int overrun;     // the loop passed its bound without the normal stop
+  // ordered-bit encodings of the ranges (see ord_enc); speeds are squared
+  unsigned long long p_min, p_max, s2_min, s2_max;
+  unsigned long long umax_bits, vmax_bits;
+  unsigned int counter;     // last-block-done ticket for grid reductions
+  unsigned int log_pos;     // next slot of the per-step log
+  unsigned int log_cap;
+};
+
+// One record per completed step.
+struct StepLog {
+  double ns;
+  double dt;
+  unsigned int sor_iters;
+  unsigned int converged;
+};
+
+// Correctly rounded a / b for a divisor b known in advance, from its
+// correctly rounded reciprocal rb = RN(1/b) (computed with an IEEE division).
+// q0 = RN(a*rb) lies within 1.5 ulp of a/b; one remainder correction
+// (Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. R&D 34(1), 1990) makes it faithful; a second one, whose
+// remainder is then exact, gives RN(a/b).  A zero quotient takes the sign of
+// a^b.  Valid for finite a and b with a/b in the normal range; a non-finite
+// numerator yields NaN rather than Inf.  Five FP64 pipe operations instead of
+// a full division, which matters on a part with a narrow FP64 pipe.
+__host__ __device__ __forceinline__ double xdiv(double a, double b, double rb) {
+  double q0 = a * rb;
+  double r0 = fma(-b, q0, a);
+  double q1 = fma(r0, rb, q0);
+  double r1 = fma(-b, q1, a);
+  double q2 = fma(r1, rb, q1);
+#ifdef __CUDA_ARCH__
+  long long qb = __double_as_longlong(q2);
+  if ((qb << 1) == 0)
+    qb = (__double_as_longlong(a) ^ __double_as_longlong(b)) & (long long)0x8000000000000000ULL;
+  return __longlong_as_double(qb);
+#else
+  if (q2 == 0.0) return (signbit(a) != signbit(b)) ? -0.0 : 0.0;
+  return q2;
+#endif
+}
+
+// Order-preserving map of a double onto uint64 (for atomicMin/atomicMax).
+__host__ __device__ __forceinline__ unsigned long long ord_enc(double d) {
+#ifdef __CUDA_ARCH__
+  unsigned long long b = (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long b;
+  memcpy(&b, &d, 8);
+#endif
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__host__ __device__ __forceinline__ double ord_dec(unsigned long long e) {
+  unsigned long long b = (e >> 63) ? (e & 0x7fffffffffffffffULL) : ~e;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+
+// One entry of the compiled boundary-condition program: on a given step the
+// target (field, cell) receives   c            (op 0)
+//                                 +src         (op 1)
+//                                 -src         (op 2)
+//                                 c - src      (op 3)
+// where src is the value the same field held at `src` before the step's
+// boundary pass.  Fields: 0 u, 1 v, 2 restore-u, 3 restore-v (src reads u for
+// fields 0/2 and v for fields 1/3).
+struct BcEntry {
+  long long target;  // (field << 56) | offset
+  long long src;     // offset
+  double c;
+  int op;
+  int pad_;
+};
+
+// A boundary cell whose pressure is copied from its fluid neighbours before
+// each pressure iteration (src/grid/mod.rs:343-412).
+struct PCopy {
+  long long off;
+  int edge;
+  int pad_;
+};
+
+}  // namespace strm

@@ -1,0 +1,921 @@
+// sm_103a kernels of the NaSt2D timestep and the CUDA graph that chains them.
+//
+// Step graph (red-black solve):
+//   bc_kernel        cluster of 8 CTAs: step bookkeeping + compiled boundary program
+//   fg_rhs_kernel    tiled F, G (+ their boundary restore) and RHS, one pass
+//   WHILE(solve not done):
+//     pcopy_kernel     boundary pressure copy
+//     sor_color_kernel red cells, then black cells
+//     residual_kernel  residual norm, stop test, sets the WHILE condition
+//   prange_kernel    pressure range when the solve ran out of iterations
+//   velocity_kernel  velocity update + restore + max|u|,|v| + speed range + time
+//
+// Every kernel that follows a reference formula uses the reference's operation
+// order; the translation unit is compiled with --fmad=false so no multiply-add
+// is fused behind our back, and divisions by step constants use xdiv (correctly
+// rounded), so results are bit-identical to the reference's FP64 arithmetic.
+#include <cooperative_groups.h>
+#include <float.h>
+
+#include <initializer_list>
+
+#include "strm_kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace strm {
+
+#define OFF(x, y) ((size_t)(x) * (size_t)g.pitch + (size_t)(y))
+
+// Tiles of the grid-stride reduction kernels: 8 rows x 64 columns, 256
+// threads, two neighbouring columns per thread.
+constexpr int RT_X = 8;
+constexpr int RT_Y = 64;
+
+__device__ __forceinline__ double sqd(double x) { return x * x; }
+
+// ------------------------------------------------------------------------
+// reductions
+// ------------------------------------------------------------------------
+
+struct OpMax { __device__ double operator()(double a, double b) const { return fmax(a, b); } };
+struct OpMin { __device__ double operator()(double a, double b) const { return fmin(a, b); } };
+struct OpAdd { __device__ double operator()(double a, double b) const { return a + b; } };
+
+// Deterministic block reduction (fixed shuffle tree, then warp 0).
+template <typename Op>
+__device__ double block_reduce(double v, Op op, double identity) {
+  __shared__ double sm[32];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nthreads = blockDim.x * blockDim.y;
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = tid & 31, w = tid >> 5, nw = (nthreads + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) sm[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < nw ? sm[lane] : identity;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;  // valid in thread 0
+}
+
+// Returns true in the block that finished last; its reads of the other
+// blocks' partials are then ordered after their writes.
+__device__ __forceinline__ bool last_block_done(unsigned int *counter) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    unsigned int t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x * gridDim.y - 1);
+  }
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last;
+}
+
+// Sums a partials array in a fixed order (deterministic).
+template <typename Op>
+__device__ double reduce_partials(const double *part, int n, int stride, int idx, Op op,
+                                  double identity) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nthreads = blockDim.x * blockDim.y;
+  double v = identity;
+  for (int k = tid; k < n; k += nthreads) v = op(v, __ldcg(part + (size_t)k * stride + idx));
+  return block_reduce(v, op, identity);
+}
+
+// ------------------------------------------------------------------------
+// K0: classification (src/grid/mod.rs:202-235, 270-332)
+// ------------------------------------------------------------------------
+
+__global__ void classify_kernel(uint8_t *flags, Geom g, unsigned long long *fluid_count,
+                                long long *first_bad) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.y * blockDim.y + threadIdx.y;
+  double fluid = 0.0;
+  if (x < g.nx && y < g.ny) {
+    const size_t o = OFF(x, y);
+    const uint8_t k = kind_of(flags[o]);
+    if (k == K_FLUID) {
+      fluid = 1.0;
+      flags[o] = 0;
+    } else {
+      // Only kind bits of the neighbours are read; edge bits are written
+      // concurrently by their own threads.
+      const int left = x > 0 && kind_of(flags[OFF(x - 1, y)]) == K_FLUID;
+      const int right = x < g.nx - 1 && kind_of(flags[OFF(x + 1, y)]) == K_FLUID;
+      const int up = y > 0 && kind_of(flags[OFF(x, y - 1)]) == K_FLUID;
+      const int down = y < g.ny - 1 && kind_of(flags[OFF(x, y + 1)]) == K_FLUID;
+      const int code = (left << 3) | (right << 2) | (up << 1) | down;
+      int e = -1;
+      switch (code) {
+        case 0x0: e = E_NONE; break;
+        case 0x8: e = E_W; break;
+        case 0xA: e = E_NW; break;
+        case 0x2: e = E_N; break;
+        case 0x6: e = E_NE; break;
+        case 0x4: e = E_E; break;
+        case 0x5: e = E_SE; break;
+        case 0x1: e = E_S; break;
+        case 0x9: e = E_SW; break;
+        default: break;
+      }
+      if (e < 0) {
+        atomicMin(first_bad, (long long)x * g.ny + y);
+        e = E_NONE;
+      }
+      flags[o] = (uint8_t)(k | (e << 3));
+    }
+  }
+  double s = block_reduce(fluid, OpAdd(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0 && s > 0.0)
+    atomicAdd(fluid_count, (unsigned long long)s);
+}
+
+// ------------------------------------------------------------------------
+// K1: step bookkeeping + boundary program (src/grid/mod.rs:414-651)
+// ------------------------------------------------------------------------
+
+// The boundary pass is sequential in the reference, and later cells read
+// values earlier cells wrote.  The host compiles it into independent
+// (target <- expression of pre-pass values) entries; here every entry is
+// first evaluated against the pre-pass fields, then a cluster-wide barrier
+// orders all those reads before any write.
+constexpr int BC_CLUSTER = 8;
+constexpr int BC_THREADS = 1024;
+
+__device__ __forceinline__ void step_begin(StepState *st, const Consts &c, double tau,
+                                           double delt, unsigned int itermax) {
+  double dt = delt;
+  if (tau > 0.0) {
+    // tau * min(Re/2 / (1/dx^2 + 1/dy^2), dx/max|u|, dy/max|v|)
+    const double dt_re = (0.5 * c.re) / ((1.0 / (c.dx * c.dx)) + (1.0 / (c.dy * c.dy)));
+    const double dt_u = c.dx / st->umax;
+    const double dt_v = c.dy / st->vmax;
+    dt = tau * fmin(dt_re, fmin(dt_u, dt_v));
+  }
+  st->dt = dt;
+  st->sor_iters = 0;
+  st->converged = 0;
+  st->exhausted = (itermax == 0) ? 1u : 0u;
+  st->ns = 0.0;
+  st->body_count = 0;
+  st->overrun = 0;
+}
+
+__global__ void __cluster_dims__(BC_CLUSTER, 1, 1) __launch_bounds__(BC_THREADS)
+    bc_kernel(double *u, double *v, double *ru, double *rv, const BcEntry *e, double *val,
+              int n, StepState *st, Consts c, double tau, double delt, unsigned int itermax,
+              int begin_step) {
+  if (begin_step && blockIdx.x == 0 && threadIdx.x == 0) step_begin(st, c, tau, delt, itermax);
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  for (int k = tid; k < n; k += nt) {
+    const BcEntry en = e[k];
+    const int field = (int)(en.target >> 56);
+    const double *srcf = (field & 1) ? v : u;
+    const double s = (en.op == 0) ? 0.0 : srcf[en.src];
+    double r;
+    switch (en.op) {
+      case 0: r = en.c; break;
+      case 1: r = s; break;
+      case 2: r = -s; break;
+      default: r = en.c - s; break;
+    }
+    val[k] = r;
+  }
+  cg::this_cluster().sync();
+  for (int k = tid; k < n; k += nt) {
+    const long long t = e[k].target;
+    const int field = (int)(t >> 56);
+    const long long off = t & ((1LL << 56) - 1);
+    double *dst = field == 0 ? u : field == 1 ? v : field == 2 ? ru : rv;
+    dst[off] = val[k];
+  }
+}
+
+// ------------------------------------------------------------------------
+// K2: F, G, their restore, RHS (src/simulation.rs:122-214, src/math.rs)
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ double d_du2dx(double u_im1, double u_i, double u_ip1, const Consts &c) {
+  const double inner_left1 = sqd(u_i + u_ip1);
+  const double inner_right1 = sqd(u_im1 + u_i);
+  const double left_side = inner_left1 - inner_right1;
+  const double inner_left2 = fabs(u_i + u_ip1) * (u_i - u_ip1);
+  const double inner_right2 = fabs(u_im1 + u_i) * (u_im1 - u_i);
+  return xdiv(left_side + (c.gamma * (inner_left2 - inner_right2)), c.four_dx, c.r_four_dx);
+}
+
+__device__ __forceinline__ double d_duvdx(double u_i_j, double u_i_j_p1, double u_i_m1_j,
+                                          double u_i_m1_j_p1, double v_i_j, double v_i_p1_j,
+                                          double v_i_m1_j, const Consts &c) {
+  const double inner_left1 = (u_i_j + u_i_j_p1) * (v_i_j + v_i_p1_j);
+  const double inner_right1 = (u_i_m1_j + u_i_m1_j_p1) * (v_i_m1_j + v_i_j);
+  const double left_side = inner_left1 - inner_right1;
+  const double inner_left2 = fabs(u_i_j + u_i_j_p1) * (v_i_j - v_i_p1_j);
+  const double inner_right2 = fabs(u_i_m1_j + u_i_m1_j_p1) * (v_i_m1_j - v_i_j);
+  return xdiv(left_side + (c.gamma * (inner_left2 - inner_right2)), c.four_dx, c.r_four_dx);
+}
+
+__device__ __forceinline__ double d_duvdy(double u_i_j, double u_i_j_m1, double u_i_j_p1,
+                                          double v_i_j, double v_i_j_m1, double v_i_p1_j,
+                                          double v_i_p1_j_m1, const Consts &c) {
+  const double inner_left1 = (v_i_j + v_i_p1_j) * (u_i_j + u_i_j_p1);
+  const double inner_right1 = (v_i_j_m1 + v_i_p1_j_m1) * (u_i_j_m1 + u_i_j);
+  const double left_side = inner_left1 - inner_right1;
+  const double inner_left2 = fabs(v_i_j + v_i_p1_j) * (u_i_j - u_i_j_p1);
+  const double inner_right2 = fabs(v_i_j_m1 + v_i_p1_j_m1) * (u_i_j_m1 - u_i_j);
+  return xdiv(left_side + (c.gamma * (inner_left2 - inner_right2)), c.four_dy, c.r_four_dy);
+}
+
+__device__ __forceinline__ double d_dv2dy(double v_i_j_m1, double v_i_j, double v_i_j_p1,
+                                          const Consts &c) {
+  const double inner_left1 = sqd(v_i_j + v_i_j_p1);
+  const double inner_right1 = sqd(v_i_j_m1 + v_i_j);
+  const double left_side = inner_left1 - inner_right1;
+  const double inner_left2 = fabs(v_i_j + v_i_j_p1) * (v_i_j - v_i_j_p1);
+  const double inner_right2 = fabs(v_i_j_m1 + v_i_j) * (v_i_j_m1 - v_i_j);
+  return xdiv(left_side + (c.gamma * (inner_left2 - inner_right2)), c.four_dy, c.r_four_dy);
+}
+
+__device__ __forceinline__ double d_laplacian(double e_i_j, double e_i_j_m1, double e_i_j_p1,
+                                              double e_i_m1_j, double e_i_p1_j, const Consts &c) {
+  const double d2edx2 = xdiv(e_i_p1_j - (2. * e_i_j) + e_i_m1_j, c.dx2, c.r_dx2);
+  const double d2edy2 = xdiv(e_i_j_p1 - (2. * e_i_j) + e_i_j_m1, c.dy2, c.r_dy2);
+  return d2edx2 + d2edy2;
+}
+
+constexpr int FG_TX = 16;  // output rows per tile
+constexpr int FG_TY = 64;  // output columns per tile
+constexpr int FG_THREADS = 256;
+
+// One tile of F/G/RHS.  Shared tiles:
+//   su, sv  rows x0-2 .. x0+TX,   cols y0-2 .. y0+TY     (u, v)
+//   sfl     rows x0-1 .. x0+TX,   cols y0-1 .. y0+TY     (flags)
+//   sF, sG  rows x0-1 .. x0+TX-1, cols y0-1 .. y0+TY-1   (F, G)
+__global__ void __launch_bounds__(FG_THREADS)
+    fg_rhs_kernel(const double *__restrict__ u, const double *__restrict__ v, double *f,
+                  double *gg, double *__restrict__ rhs, const uint8_t *__restrict__ flags, Geom g,
+                  Consts c, const StepState *st) {
+  __shared__ double su[FG_TX + 3][FG_TY + 3];
+  __shared__ double sv[FG_TX + 3][FG_TY + 3];
+  __shared__ double sF[FG_TX + 1][FG_TY + 1];
+  __shared__ double sG[FG_TX + 1][FG_TY + 1];
+  __shared__ uint8_t sfl[FG_TX + 2][FG_TY + 2];
+  __shared__ double s_dt, s_rdt;
+
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * FG_TY;
+  const int x0 = blockIdx.y * FG_TX;
+  if (tid == 0) {
+    s_dt = st->dt;
+    s_rdt = 1.0 / s_dt;
+  }
+  for (int k = tid; k < (FG_TX + 3) * (FG_TY + 3); k += FG_THREADS) {
+    const int i = k / (FG_TY + 3), j = k % (FG_TY + 3);
+    const int x = x0 - 2 + i, y = y0 - 2 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    su[i][j] = in ? u[OFF(x, y)] : 0.0;
+    sv[i][j] = in ? v[OFF(x, y)] : 0.0;
+  }
+  for (int k = tid; k < (FG_TX + 2) * (FG_TY + 2); k += FG_THREADS) {
+    const int i = k / (FG_TY + 2), j = k % (FG_TY + 2);
+    const int x = x0 - 1 + i, y = y0 - 1 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    sfl[i][j] = in ? flags[OFF(x, y)] : (uint8_t)0;
+  }
+  __syncthreads();
+  const double dt = s_dt;
+
+  for (int k = tid; k < (FG_TX + 1) * (FG_TY + 1); k += FG_THREADS) {
+    const int i = k / (FG_TY + 1), j = k % (FG_TY + 1);
+    const int x = x0 - 1 + i, y = y0 - 1 + j;
+    double Fv = 0.0, Gv = 0.0;
+    if (x >= 0 && y >= 0 && x < g.nx && y < g.ny) {
+      const uint8_t fc = sfl[i][j];
+      const bool bc = is_bnd(fc);
+      const bool keepF = bc || (x + 1 < g.nx && is_bnd(sfl[i + 1][j]));
+      const bool keepG = bc || (y + 1 < g.ny && is_bnd(sfl[i][j + 1]));
+      const bool interior = x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+      // window: w(a, b) = field(x + a, y + b) = s[i + 1 + a][j + 1 + b]
+      const int si = i + 1, sj = j + 1;
+      if (keepF) {
+        Fv = su[si][sj];
+      } else if (interior) {
+        const double u01 = su[si - 1][sj], u10 = su[si][sj - 1], u11 = su[si][sj];
+        const double u12 = su[si][sj + 1], u21 = su[si + 1][sj];
+        const double v10 = sv[si][sj - 1], v11 = sv[si][sj], v20 = sv[si + 1][sj - 1];
+        const double v21 = sv[si + 1][sj];
+        const double lap = d_laplacian(u11, u10, u12, u01, u21, c);
+        const double a = d_du2dx(u01, u11, u21, c);
+        const double b = d_duvdy(u11, u10, u12, v11, v10, v21, v20, c);
+        Fv = u11 + (dt * (xdiv(lap, c.re, c.r_re) - a - b));
+      } else {
+        Fv = f[OFF(x, y)];
+      }
+      if (keepG) {
+        Gv = sv[si][sj];
+      } else if (interior) {
+        const double u01 = su[si - 1][sj], u02 = su[si - 1][sj + 1], u11 = su[si][sj];
+        const double u12 = su[si][sj + 1];
+        const double v01 = sv[si - 1][sj], v10 = sv[si][sj - 1], v11 = sv[si][sj];
+        const double v12 = sv[si][sj + 1], v21 = sv[si + 1][sj];
+        const double lap = d_laplacian(v11, v10, v12, v01, v21, c);
+        const double a = d_duvdx(u11, u12, u01, u02, v11, v21, v01, c);
+        const double b = d_dv2dy(v10, v11, v12, c);
+        Gv = v11 + (dt * (xdiv(lap, c.re, c.r_re) - a - b));
+      } else {
+        Gv = gg[OFF(x, y)];
+      }
+      if (i >= 1 && j >= 1) {
+        if (keepF || interior) f[OFF(x, y)] = Fv;
+        if (keepG || interior) gg[OFF(x, y)] = Gv;
+      }
+    }
+    sF[i][j] = Fv;
+    sG[i][j] = Gv;
+  }
+  __syncthreads();
+
+  for (int k = tid; k < FG_TX * FG_TY; k += FG_THREADS) {
+    const int i = k / FG_TY, j = k % FG_TY;
+    const int x = x0 + i, y = y0 + j;
+    if (x >= 1 && y >= 1 && x < g.nx && y < g.ny) {
+      const double a = xdiv(sF[i + 1][j + 1] - sF[i][j + 1], c.dx, c.r_dx);
+      const double b = xdiv(sG[i + 1][j + 1] - sG[i + 1][j], c.dy, c.r_dy);
+      rhs[OFF(x, y)] = xdiv(a + b, dt, s_rdt);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// K3: pressure solve (src/simulation.rs:239-285, src/grid/mod.rs:343-412)
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ void pcopy_one(double *p, const PCopy &pc, int pitch) {
+  const long long o = pc.off;
+  switch (pc.edge) {
+    case E_N: p[o] = p[o - 1]; break;
+    case E_NE: p[o] = (p[o - 1] + p[o + pitch]) * 0.5; break;
+    case E_E: p[o] = p[o + pitch]; break;
+    case E_SE: p[o] = (p[o + 1] + p[o + pitch]) * 0.5; break;
+    case E_S: p[o] = p[o + 1]; break;
+    case E_SW: p[o] = (p[o + 1] + p[o - pitch]) * 0.5; break;
+    case E_W: p[o] = p[o - pitch]; break;
+    case E_NW: p[o] = (p[o - 1] + p[o - pitch]) * 0.5; break;
+    default: break;
+  }
+}
+
+__global__ void pcopy_kernel(double *p, const PCopy *pc, int n, int pitch) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) pcopy_one(p, pc[k], pitch);
+}
+
+// SOR update of one fluid cell (src/simulation.rs:260-271).
+template <bool EXACT>
+__device__ __forceinline__ double sor_update(double p, double pw, double pe, double pn, double ps,
+                                             double r, const Consts &c) {
+  if (EXACT) {
+    return (c.one_minus_w * p) +
+           c.middle * (xdiv(pe + pw, c.dx2, c.r_dx2) + xdiv(ps + pn, c.dy2, c.r_dy2) - r);
+  } else {
+    const double t = fma(pe + pw, c.r_dx2, fma(ps + pn, c.r_dy2, -r));
+    return fma(c.one_minus_w, p, c.middle * t);
+  }
+}
+
+// Residual of one interior cell (src/math.rs:176-186).
+template <bool EXACT>
+__device__ __forceinline__ double residual_of(double p, double pw, double pe, double pn, double ps,
+                                              double r, const Consts &c) {
+  if (EXACT) {
+    const double part1 = xdiv((pe - p) - (p - pw), c.dx2, c.r_dx2);
+    const double part2 = xdiv((ps - p) - (p - pn), c.dy2, c.r_dy2);
+    return part1 + part2 - r;
+  } else {
+    const double a = fma(-2.0, p, pe + pw);
+    const double b = fma(-2.0, p, ps + pn);
+    return fma(a, c.r_dx2, fma(b, c.r_dy2, -r));
+  }
+}
+
+// One colour of a red-black sweep: cells with (x + y) % 2 == color.  Thread
+// (tx, ty) owns the cell pair y = 2*(y-pair), x = row; it updates the member
+// of the pair that has the colour.
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+    sor_color_kernel(double *__restrict__ p, const double *__restrict__ rhs,
+                     const uint8_t *__restrict__ flags, Geom g, Consts c, int color) {
+  const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int y = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((x + color) & 1);
+  if (x > g.nx - 2 || y < 1 || y > g.ny - 2) return;
+  const size_t o = OFF(x, y);
+  if (flags[o] != 0) return;
+  const double pc = p[o], pw = p[o - g.pitch], pe = p[o + g.pitch];
+  const double pn = p[o - 1], ps = p[o + 1];
+  p[o] = sor_update<EXACT>(pc, pw, pe, pn, ps, rhs[o], c);
+}
+
+// What a residual launch does once the norm is known.
+enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2 };
+
+// Residual norm over every interior cell (src/simulation.rs:216-227), in
+// grid-stride tiles; the last block to finish sums the per-block partials in
+// a fixed order, divides by fluid_cells and applies the stop rule of
+// src/simulation.rs:276-281 (mode RES_SOLVE), optionally ending the graph's
+// WHILE loop.
+template <bool EXACT, bool IN_GRAPH>
+__global__ void __launch_bounds__(256)
+    residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs, Geom g,
+                    Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
+                    cudaGraphConditionalHandle h, unsigned int itermax, int strict, int mode) {
+  double acc = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tx = t / tiles_y, ty = t % tiles_y;
+    const int x = 1 + tx * RT_X + threadIdx.y;
+    if (x > g.nx - 2) continue;
+    const int yb = 1 + ty * RT_Y + 2 * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = yb + q;
+      if (y <= g.ny - 2) {
+        const size_t o = OFF(x, y);
+        const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
+                                            p[o + 1], rhs[o], c);
+        acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
+      }
+    }
+  }
+  const double bsum = block_reduce(acc, OpAdd(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = bsum;
+  if (IN_GRAPH && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    // Independent bound on the WHILE loop: the normal stop below ends it at
+    // iteration itermax at the latest; should that bookkeeping ever fail,
+    // this ends it two launches later and flags the step.
+    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
+    if (launches >= itermax + 2) {
+      st->overrun = 1;
+      cudaGraphSetConditional(h, 0);
+    }
+  }
+  if (!last_block_done(&st->counter)) return;
+  const double total = reduce_partials(partials, gridDim.x, 1, 0, OpAdd(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    const double ns = total / st->fluid_cells;
+    if (mode == RES_NS0) {
+      st->ns0 = ns;
+    } else if (mode == RES_NORM) {
+      st->aux = ns;
+    } else {
+      const unsigned int it = st->sor_iters + 1;
+      st->sor_iters = it;
+      st->ns = ns;
+      st->nonfinite = !isfinite(ns);
+      const bool done = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      if (done) st->converged = 1;
+      else if (it >= itermax) st->exhausted = 1;
+      if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
+    }
+  }
+}
+
+// Lexicographic Gauss-Seidel SOR in one CTA, bit-identical to the reference
+// (src/simulation.rs:239-285): the sweep runs as anti-diagonal wavefronts
+// d = x + y (a cell reads its west/north neighbours from wavefront d-1, new,
+// and east/south from d+1, old — exactly the x-major order), and the residual
+// squares are summed by one thread in x-major order.
+__global__ void __launch_bounds__(1024)
+    sor_lex_kernel(double *p, const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
+                   const PCopy *pc, int npc, Geom g, Consts c, StepState *st, double *r2,
+                   unsigned int itermax, int strict) {
+  __shared__ int s_done;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int NI = g.nx - 2, NJ = g.ny - 2;
+  double ns = 0.0;
+  unsigned int iters = 0;
+  int conv = 0;
+  for (unsigned int it = 0; it < itermax; ++it) {
+    for (int k = tid; k < npc; k += nt) pcopy_one(p, pc[k], g.pitch);
+    __syncthreads();
+    for (int d = 2; d <= NI + NJ; ++d) {
+      const int xlo = max(1, d - NJ), xhi = min(NI, d - 1);
+      for (int x = xlo + tid; x <= xhi; x += nt) {
+        const int y = d - x;
+        const size_t o = OFF(x, y);
+        if (flags[o] == 0)
+          p[o] = sor_update<true>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
+                                  rhs[o], c);
+      }
+      __syncthreads();
+    }
+    for (int k = tid; k < NI * NJ; k += nt) {
+      const int x = 1 + k / NJ, y = 1 + k % NJ;
+      const size_t o = OFF(x, y);
+      r2[k] = sqd(residual_of<true>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
+                                    rhs[o], c));
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double acc = 0.0;
+      for (int k = 0; k < NI * NJ; ++k) acc = acc + r2[k];
+      ns = acc / st->fluid_cells;
+      iters = it + 1;
+      conv = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      s_done = conv;
+    }
+    __syncthreads();
+    if (s_done) break;
+  }
+  if (tid == 0) {
+    st->ns = ns;
+    st->sor_iters = conv ? iters : itermax;
+    st->converged = conv;
+    st->exhausted = conv ? 0u : 1u;
+    st->nonfinite = !isfinite(ns);
+  }
+}
+
+// Pressure range over fluid cells (src/grid/mod.rs:237-251), only when the
+// solve ran out of iterations (src/simulation.rs:283) or when forced.
+__global__ void __launch_bounds__(256)
+    prange_kernel(const double *__restrict__ p, const uint8_t *__restrict__ flags, Geom g,
+                  StepState *st, double *partials, int tiles_y, int ntiles, int force) {
+  if (!force && !st->exhausted) return;
+  double mn = DBL_MAX, mx = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int x = (t / tiles_y) * RT_X + threadIdx.y;
+    if (x >= g.nx) continue;
+    const int yb = (t % tiles_y) * RT_Y + 2 * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = yb + q;
+      if (y < g.ny) {
+        const size_t o = OFF(x, y);
+        if (flags[o] == 0) {
+          mn = fmin(mn, p[o]);
+          mx = fmax(mx, p[o]);
+        }
+      }
+    }
+  }
+  const double bmn = block_reduce(mn, OpMin(), DBL_MAX);
+  const double bmx = block_reduce(mx, OpMax(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    partials[2 * blockIdx.x] = bmn;
+    partials[2 * blockIdx.x + 1] = bmx;
+  }
+  if (!last_block_done(&st->counter)) return;
+  const double rmn = reduce_partials(partials, gridDim.x, 2, 0, OpMin(), DBL_MAX);
+  const double rmx = reduce_partials(partials, gridDim.x, 2, 1, OpMax(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    st->p_min = ord_enc(rmn);
+    st->p_max = ord_enc(rmx);
+  }
+}
+
+// ------------------------------------------------------------------------
+// K4: velocity update (src/simulation.rs:287-322) + statistics
+// ------------------------------------------------------------------------
+
+// Fluid cells in [0, nx-1) x [0, ny-1) get u = F - (dt/dx)(p[x+1]-p[x]),
+// v = G - (dt/dy)(p[y+1]-p[y]); boundary cells with an edge get the restore
+// values the boundary pass recorded (their final value in the reference's
+// u_v_restore replay); the rest keep their value.  Then max|u|, max|v| over
+// every cell, the fluid speed range and, for a step, time += delt.
+__global__ void __launch_bounds__(256)
+    velocity_kernel(double *u, double *v, const double *__restrict__ f,
+                    const double *__restrict__ gg, const double *__restrict__ p,
+                    const double *__restrict__ ru, const double *__restrict__ rv,
+                    const uint8_t *__restrict__ flags, Geom g, Consts c, StepState *st,
+                    double *partials, StepLog *log, int tiles_y, int ntiles, int update,
+                    int commit_speed, int advance) {
+  __shared__ double s_cu, s_cv;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    s_cu = st->dt / c.dx;
+    s_cv = st->dt / c.dy;
+  }
+  __syncthreads();
+  const double cu = s_cu, cv = s_cv;
+  double umax = 1.0e-10, vmax = 1.0e-10, smin = DBL_MAX, smax = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int x = (t / tiles_y) * RT_X + threadIdx.y;
+    if (x >= g.nx) continue;
+    const int yb = (t % tiles_y) * RT_Y + 2 * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = yb + q;
+      if (y < g.ny) {
+        const size_t o = OFF(x, y);
+        const uint8_t fl = flags[o];
+        double un, vn;
+        if (update && is_bnd(fl) && edge_of(fl) != E_NONE) {
+          un = ru[o];
+          vn = rv[o];
+          u[o] = un;
+          v[o] = vn;
+        } else if (update && !is_bnd(fl) && x < g.nx - 1 && y < g.ny - 1) {
+          const double pc = p[o];
+          un = f[o] - cu * (p[o + g.pitch] - pc);
+          vn = gg[o] - cv * (p[o + 1] - pc);
+          u[o] = un;
+          v[o] = vn;
+        } else {
+          un = u[o];
+          vn = v[o];
+        }
+        umax = fmax(umax, fabs(un));
+        vmax = fmax(vmax, fabs(vn));
+        if (!is_bnd(fl)) {
+          const double s2 = sqd(un) + sqd(vn);
+          smin = fmin(smin, s2);
+          smax = fmax(smax, s2);
+        }
+      }
+    }
+  }
+  const double b0 = block_reduce(umax, OpMax(), 1.0e-10);
+  const double b1 = block_reduce(vmax, OpMax(), 1.0e-10);
+  const double b2 = block_reduce(smin, OpMin(), DBL_MAX);
+  const double b3 = block_reduce(smax, OpMax(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    double *pp = partials + 4 * (size_t)blockIdx.x;
+    pp[0] = b0;
+    pp[1] = b1;
+    pp[2] = b2;
+    pp[3] = b3;
+  }
+  if (!last_block_done(&st->counter)) return;
+  const double r0 = reduce_partials(partials, gridDim.x, 4, 0, OpMax(), 1.0e-10);
+  const double r1 = reduce_partials(partials, gridDim.x, 4, 1, OpMax(), 1.0e-10);
+  const double r2 = reduce_partials(partials, gridDim.x, 4, 2, OpMin(), DBL_MAX);
+  const double r3 = reduce_partials(partials, gridDim.x, 4, 3, OpMax(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    st->umax = r0;
+    st->vmax = r1;
+    if (commit_speed) {
+      st->s2_min = ord_enc(sqrt(r2));
+      st->s2_max = ord_enc(sqrt(r3));
+    }
+    if (advance) {
+      st->time = st->time + st->dt;
+      st->iterations += 1;
+      if (log && st->log_pos < st->log_cap) {
+        StepLog &l = log[st->log_pos];
+        l.ns = st->ns;
+        l.dt = st->dt;
+        l.sor_iters = st->sor_iters;
+        l.converged = st->converged;
+        st->log_pos += 1;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------
+
+static int g_num_sms = 0;
+static int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 152;
+  }
+  return g_num_sms;
+}
+
+static void tiles_of(const Geom &g, int interior, int *tiles_y, int *ntiles) {
+  const int nx = interior ? g.nx - 2 : g.nx;
+  const int ny = interior ? g.ny - 2 : g.ny;
+  *tiles_y = (ny + RT_Y - 1) / RT_Y;
+  const int tiles_x = (nx + RT_X - 1) / RT_X;
+  *ntiles = (nx > 0 && ny > 0) ? (*tiles_y) * tiles_x : 0;
+}
+
+int residual_blocks(const Geom &g) {
+  int ty, nt;
+  tiles_of(g, 0, &ty, &nt);
+  int b = 4 * num_sms();
+  if (nt < b) b = nt;
+  return b < 1 ? 1 : b;
+}
+
+static const dim3 kRedBlock(RT_Y / 2, RT_X);
+
+cudaError_t launch_classify(const DevFields &d, const Geom &g, cudaStream_t s) {
+  dim3 blk(64, 4), grd((g.ny + 63) / 64, (g.nx + 3) / 4);
+  classify_kernel<<<grd, blk, 0, s>>>(d.flags, g, d.fluid_count, d.first_bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_begin(const DevFields &d, const RunCfg &r, cudaStream_t s) {
+  bc_kernel<<<BC_CLUSTER, BC_THREADS, 0, s>>>(d.u, d.v, d.ru, d.rv, d.bc, d.bc_val, 0, d.st,
+                                              r.c, r.tau, r.delt, r.itermax, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc(const DevFields &d, cudaStream_t s) {
+  Consts c{};
+  bc_kernel<<<BC_CLUSTER, BC_THREADS, 0, s>>>(d.u, d.v, d.ru, d.rv, d.bc, d.bc_val, d.n_bc, d.st,
+                                              c, 0.0, 0.0, 0u, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fg_rhs(const DevFields &d, const RunCfg &r, cudaStream_t s) {
+  dim3 grd((r.g.ny + FG_TY - 1) / FG_TY, (r.g.nx + FG_TX - 1) / FG_TX);
+  fg_rhs_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c, d.st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcopy(const DevFields &d, const Geom &g, cudaStream_t s) {
+  if (d.n_pcopy == 0) return cudaSuccess;
+  pcopy_kernel<<<(d.n_pcopy + 255) / 256, 256, 0, s>>>(d.p, d.pcopy, d.n_pcopy, g.pitch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm(const DevFields &d, const RunCfg &r, cudaStream_t s, int set_ns0) {
+  int ty, nt;
+  tiles_of(r.g, 1, &ty, &nt);
+  if (nt == 0) {
+    // no interior: the sum is 0.0
+    return cudaSuccess;
+  }
+  int nb = residual_blocks(r.g);
+  residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st, d.partials,
+                                                        ty, nt, 0, r.itermax, r.strict_eps,
+                                                        set_ns0 ? RES_NS0 : RES_NORM);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_velocity(const DevFields &d, const RunCfg &r, cudaStream_t s, int update,
+                            int commit_speed, int advance) {
+  int ty, nt;
+  tiles_of(r.g, 0, &ty, &nt);
+  int nb = residual_blocks(r.g);
+  velocity_kernel<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, r.g,
+                                           r.c, d.st, d.partials, d.log, ty, nt, update,
+                                           commit_speed, advance);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, int force) {
+  int ty, nt;
+  tiles_of(r.g, 0, &ty, &nt);
+  int nb = residual_blocks(r.g);
+  prange_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.flags, r.g, d.st, d.partials, ty, nt, force);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s) {
+  int ty, nt;
+  tiles_of(r.g, 1, &ty, &nt);
+  if (nt == 0) return cudaSuccess;
+  cudaError_t e = launch_pcopy(d, r.g, s);
+  if (e != cudaSuccess) return e;
+  dim3 sgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+             (r.g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+  const int nb = residual_blocks(r.g);
+  for (int color = 0; color < 2; ++color) {
+    if (r.arith)
+      sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
+    else
+      sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
+  }
+  if (r.arith)
+    residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st,
+                                                           d.partials, ty, nt, 0, r.itermax,
+                                                           r.strict_eps, RES_NORM);
+  else
+    residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st,
+                                                          d.partials, ty, nt, 0, r.itermax,
+                                                          r.strict_eps, RES_NORM);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s) {
+  sor_lex_kernel<<<1, 1024, 0, s>>>(d.p, d.rhs, d.flags, d.pcopy, d.n_pcopy, r.g, r.c, d.st,
+                                    d.pw, r.itermax, r.strict_eps);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// step graph
+// ------------------------------------------------------------------------
+
+namespace {
+
+struct GraphBuilder {
+  cudaGraph_t graph;
+  cudaError_t err = cudaSuccess;
+  // kernel parameter storage must outlive cudaGraphAddKernelNode
+  std::vector<std::vector<unsigned char>> store;
+
+  template <typename... Args>
+  cudaGraphNode_t kernel(cudaGraph_t gr, cudaGraphNode_t dep, const void *fn, dim3 grid,
+                         dim3 block, Args... args) {
+    if (err != cudaSuccess) return nullptr;
+    void *ptrs[sizeof...(Args) + 1];
+    size_t i = 0;
+    (void)std::initializer_list<int>{(ptrs[i++] = keep(args), 0)...};
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void *>(fn);
+    kp.gridDim = grid;
+    kp.blockDim = block;
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = ptrs;
+    kp.extra = nullptr;
+    cudaGraphNode_t node = nullptr;
+    err = cudaGraphAddKernelNode(&node, gr, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+    return node;
+  }
+
+  template <typename T>
+  void *keep(const T &v) {
+    store.emplace_back(sizeof(T));
+    memcpy(store.back().data(), &v, sizeof(T));
+    return store.back().data();
+  }
+};
+
+}  // namespace
+
+cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out) {
+  GraphBuilder b;
+  cudaError_t e = cudaGraphCreate(&b.graph, 0);
+  if (e != cudaSuccess) return e;
+  b.store.reserve(256);
+  const Geom g = r.g;
+  const Consts c = r.c;
+  int ty_all, nt_all, ty_int, nt_int;
+  tiles_of(g, 0, &ty_all, &nt_all);
+  tiles_of(g, 1, &ty_int, &nt_int);
+  const int nb = residual_blocks(g);
+
+  cudaGraphNode_t n = b.kernel(b.graph, nullptr, (const void *)bc_kernel, dim3(BC_CLUSTER),
+                               dim3(BC_THREADS), d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc,
+                               d.bc_val, d.n_bc, d.st, c, r.tau, r.delt, r.itermax, 1);
+  dim3 fg_grid((g.ny + FG_TY - 1) / FG_TY, (g.nx + FG_TX - 1) / FG_TX);
+  n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
+               (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
+               (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
+
+  if (r.sor_order == 1) {
+    n = b.kernel(b.graph, n, (const void *)sor_lex_kernel, dim3(1), dim3(1024), d.p,
+                 (const double *)d.rhs, (const uint8_t *)d.flags, (const PCopy *)d.pcopy,
+                 d.n_pcopy, g, c, d.st, d.pw, r.itermax, r.strict_eps);
+  } else if (nt_int > 0 && r.itermax > 0) {
+    cudaGraphConditionalHandle h;
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&wnode, b.graph, &n, nullptr, 1, &cp);
+    if (b.err == cudaSuccess) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      cudaGraphNode_t bn = nullptr;
+      if (d.n_pcopy > 0)
+        bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
+                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+      dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+                 (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+      const void *kc = r.arith ? (const void *)sor_color_kernel<false>
+                               : (const void *)sor_color_kernel<true>;
+      const void *kr = r.arith ? (const void *)residual_kernel<false, true>
+                               : (const void *)residual_kernel<true, true>;
+      for (int color = 0; color < 2; ++color)
+        bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
+                      (const uint8_t *)d.flags, g, c, color);
+      bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
+                    (const double *)d.rhs, g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax,
+                    r.strict_eps, (int)RES_SOLVE);
+    }
+    n = wnode;
+  }
+  n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock, (const double *)d.p,
+               (const uint8_t *)d.flags, g, d.st, d.partials, ty_all, nt_all, 0);
+  n = b.kernel(b.graph, n, (const void *)velocity_kernel, dim3(nb), kRedBlock, d.u, d.v,
+               (const double *)d.f, (const double *)d.g, (const double *)d.p,
+               (const double *)d.ru, (const double *)d.rv, (const uint8_t *)d.flags, g, c, d.st,
+               d.partials, d.log, ty_all, nt_all, 1, 1, 1);
+  if (b.err != cudaSuccess) {
+    cudaGraphDestroy(b.graph);
+    return b.err;
+  }
+  *out = b.graph;
+  return cudaSuccess;
+}
+
+}  // namespace strm

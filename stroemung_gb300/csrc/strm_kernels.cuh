@@ -1,0 +1,67 @@
+// Host-side interface between the C ABI (strm_capi.cu) and the kernels
+// (strm_kernels.cu).  Nothing here is part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "strm_internal.cuh"
+
+namespace strm {
+
+// Device buffers of one simulation.
+struct DevFields {
+  double *u, *v, *p, *f, *g, *rhs;
+  double *ru, *rv;        // restore values of boundary cells (per cell)
+  uint8_t *flags;
+  // mixed-precision pressure solve
+  float *e32, *r32;       // FP32 correction and defect
+  double *pw;             // FP64 work field
+  StepState *st;
+  double *partials;       // per-CTA residual partial sums
+  int n_partials;
+  StepLog *log;
+  BcEntry *bc;            // compiled boundary program
+  double *bc_val;         // its gathered values
+  int n_bc;
+  PCopy *pcopy;
+  int n_pcopy;
+  long long *first_bad;   // classification: first thin-wall cell (x*ny+y)
+  unsigned long long *fluid_count;
+};
+
+struct RunCfg {
+  Geom g;
+  Consts c;
+  double tau;             // > 0: adaptive time step
+  double delt;            // fixed time step when tau <= 0
+  unsigned int itermax;
+  int strict_eps;
+  int sor_order;          // 0 red-black, 1 lexicographic
+  int arith;              // 0 exact, 1 fast
+  int precision;          // 0 fp64, 1 mixed
+  int inner_sweeps;
+};
+
+// Standalone launches (phase entry points, creation).
+cudaError_t launch_classify(const DevFields &d, const Geom &g, cudaStream_t s);
+cudaError_t launch_step_begin(const DevFields &d, const RunCfg &r, cudaStream_t s);
+cudaError_t launch_bc(const DevFields &d, cudaStream_t s);
+cudaError_t launch_fg_rhs(const DevFields &d, const RunCfg &r, cudaStream_t s);
+cudaError_t launch_pcopy(const DevFields &d, const Geom &g, cudaStream_t s);
+cudaError_t launch_norm(const DevFields &d, const RunCfg &r, cudaStream_t s, int set_ns0);
+cudaError_t launch_velocity(const DevFields &d, const RunCfg &r, cudaStream_t s, int update,
+                            int commit_speed, int advance);
+cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, int force);
+cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s);
+// One red-black pressure iteration (copy, red, black, residual) without a stop test.
+cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s);
+
+// Builds the whole step as one CUDA graph (the pressure loop as a
+// conditional WHILE node for the red-black solve).
+cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out);
+
+int residual_blocks(const Geom &g);
+
+}  // namespace strm

@@ -1,0 +1,53 @@
+"""The C-ABI library builds, loads and exports every entry point the public
+header declares; without a GPU it refuses to create a simulation (no host
+fallback)."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from stroemung_gb300 import _lib, presets
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "stroemung_gpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(strm_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_expected_surface():
+    names = declared_functions()
+    for must in ("strm_create", "strm_tick", "strm_step_n", "strm_download", "strm_upload",
+                 "strm_edit_cells", "strm_destroy", "strm_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+    assert set(_lib.SIGNATURES) == set(declared_functions())
+    assert L.strm_abi_version() == 1
+
+
+def test_struct_sizes_match_header_layout():
+    # strm_params: 7 doubles, 2 uint32, 3 doubles
+    assert ctypes.sizeof(_lib.Params) == 7 * 8 + 2 * 4 + 3 * 8
+    assert ctypes.sizeof(_lib.Mode) == 5 * 4
+    assert ctypes.sizeof(_lib.StepStats) == 24
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from stroemung_gb300.simulation import Simulation, StroemungError
+    g = presets.simple_inflow((4, 3))
+    with pytest.raises(StroemungError) as ei:
+        Simulation(grid=g, cell_size=(0.1, 0.2), delt=0.005, gamma=0.9, reynolds=100.0)
+    assert ei.value.code in (_lib.STRM_ERR_NO_DEVICE, _lib.STRM_ERR_CUDA)

@@ -167,3 +167,25 @@ def test_serialize_empty(golden):
     s = orc.OracleSim(kind=g["kind"], u=g["u"], v=g["v"], p=g["p"], dx=1.0, dy=2.0,
                       delt=1.4, gamma=1.7, reynolds=100.0)
     assert s.state()["initial_norm_squared"] == snap["initial_norm_squared"]
+
+
+def test_red_black_matches_lexicographic_at_converged_residual():
+    """The property the GPU red-black solve is held to, shown on the oracle
+    itself: on a compatible problem (closed cavity) both orders converged to
+    the same residual give u, v and pressure (up to its constant) within
+    1e-6 relative L2."""
+    g = presets.cavity(30)
+    kw = dict(dx=1 / 30, dy=1 / 30, delt=0.002, gamma=0.9, reynolds=100.0, eps=1e-6,
+              omega=1.7, max_iterations=20000, tau=0.5, strict_eps=True)
+    a = orc.OracleSim(kind=g["kind"], wall_uv=g["wall_uv"], u=g["u"], v=g["v"], p=g["p"],
+                      sor_order=orc.LEXICOGRAPHIC, **kw)
+    b = orc.OracleSim(kind=g["kind"], wall_uv=g["wall_uv"], u=g["u"], v=g["v"], p=g["p"],
+                      sor_order=orc.RED_BLACK, **kw)
+    for _ in range(10):
+        assert a.tick()[1] < 1e-12 and b.tick()[1] < 1e-12
+    from tests.helpers import rel_l2
+    for n in ("u", "v"):
+        assert rel_l2(b.field(n), a.field(n)) < 1e-6
+    fl = g["kind"] == 0
+    pa, pb = a.field("p")[fl], b.field("p")[fl]
+    assert rel_l2(pb - pb.mean(), pa - pa.mean()) < 1e-6
