@@ -286,7 +286,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    e2e_iters = []
+    e2e_iters = [0] if args.e2e_steps == 0 else []
     for _ in range(args.e2e_steps):
         for n in ("u", "v", "p"):
             sim.upload(n, host[n])
@@ -301,7 +301,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     field_bytes = (IMAX + 2) * (JMAX + 2) * 8
-    e2e = {"value": CELLS * args.e2e_steps * world / e2e_s, "unit": "cell-updates/s",
+    e2e = {"value": CELLS * args.e2e_steps * world / e2e_s if args.e2e_steps else None, "unit": "cell-updates/s",
            "h2d_bytes_per_step": 3 * field_bytes, "d2h_bytes_per_step": 3 * field_bytes + 64,
            "steps": args.e2e_steps, "sor_iterations": e2e_iters,
            "path": "Simulation.upload(u,v,p) + run_simulation_tick() + download(u,v,p), "
@@ -330,7 +330,7 @@ def main():
         "clocks": clocks.summary(),
         "gpu_launches": launches,
     }
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_ticks > 0:
         t_step, t_it, wall = cpu_sample(grid, statistics.mean(iters), args.cpu_ticks,
                                         args.cpu_cap)
         out["cpu_baseline"] = {
