@@ -77,6 +77,15 @@ enum {
     STRM_PREC_MIXED = 1  /* FP32 red-black sweeps on the FP64 defect, FP64 refinement */
 };
 
+/* How a step is issued. */
+enum {
+    STRM_EXEC_GRAPH = 0, /* one CUDA graph launch per step (pressure loop as a
+                            conditional WHILE node) */
+    STRM_EXEC_EAGER = 1  /* the same kernels launched one by one, the loop driven
+                            from the host; identical results, for profilers and
+                            debugging */
+};
+
 /* Mirrors Simulation's parameters (src/simulation.rs:30-69). */
 typedef struct {
     double dx, dy;            /* cell_size */
@@ -100,7 +109,8 @@ typedef struct {
     int arithmetic;   /* STRM_ARITH_* */
     int precision;    /* STRM_PREC_* */
     int strict_eps;   /* 1: stop only at ns < eps^2 (not at ns < initial norm) */
-    int inner_sweeps; /* mixed precision: FP32 sweeps per FP64 refinement (0 = 8) */
+    int inner_sweeps; /* mixed precision: FP32 sweeps per FP64 refinement (0 = 16) */
+    int execution;    /* STRM_EXEC_* */
 } strm_mode;
 
 /* Scalar state readable after any call (pressure_range / speed_range are the
@@ -191,6 +201,12 @@ int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
 
 /* Waits until all work queued on the simulation's stream has finished. */
 int strm_synchronize(strm_sim *sim);
+
+/* Headless colour map of render_simulation (src/visualization.rs:79-105):
+ * color_type 0 pressure, 1 speed, rendered on the GPU from the current
+ * fields and ranges into rgba[ny][nx][4] (host), row y = image row, as the
+ * reference's macroquad Image of width nx.  No graphics API involved. */
+int strm_render_rgba(strm_sim *sim, int color_type, uint8_t *rgba);
 
 /* Device pointers of the fields (pitch in elements) for zero-copy interop. */
 typedef struct {

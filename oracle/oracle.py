@@ -96,6 +96,7 @@ def lib():
         L.orc_calculate_norm_squared.argtypes = [ctypes.c_void_p]
         L.orc_solve_sor.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), _dp]
         L.orc_tick_timed.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _dp]
+        L.orc_render.argtypes = [ctypes.c_void_p, ctypes.c_int, _u8p]
         _lib = L
     return _lib
 
@@ -250,6 +251,12 @@ class OracleSim:
 
     def set_u_and_v(self):
         lib().orc_set_u_and_v(self._h)
+
+    def render(self, color_type: int) -> np.ndarray:
+        """src/visualization.rs colour map: [ny, nx, 4] uint8 (0 pressure, 1 speed)."""
+        out = np.zeros((self.ny, self.nx, 4), dtype=np.uint8)
+        lib().orc_render(self._h, int(color_type), out.ctypes.data_as(_u8p))
+        return out
 
     def tick_timed(self, max_iterations_cap: int = 0):
         """(seconds before the solve, seconds in it, iterations, seconds after)."""

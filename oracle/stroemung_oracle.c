@@ -629,3 +629,66 @@ void orc_tick_timed(orc_sim *s, uint32_t max_iterations_cap, double *out4) {
     out4[2] = (double)it;
     out4[3] = t3 - t2;
 }
+
+/* ------------------------------------------------------------------ */
+/* Colour map, src/visualization.rs:7-105                              */
+/* ------------------------------------------------------------------ */
+
+/* src/visualization.rs:7-27, in f32 */
+static void hsl_to_rgb(float hue, float saturation, float lightness, float *r, float *g,
+                       float *b) {
+    float c = (1.0f - fabsf(2.0f * lightness - 1.0f)) * saturation;
+    float x = c * (1.0f - fabsf(fmodf(hue / 60.0f, 2.0f) - 1.0f));
+    float m = lightness - c / 2.0f;
+    float rr, gg, bb;
+    if (hue < 60.0f) { rr = c; gg = x; bb = 0.0f; }
+    else if (hue < 120.0f) { rr = x; gg = c; bb = 0.0f; }
+    else if (hue < 180.0f) { rr = 0.0f; gg = c; bb = x; }
+    else if (hue < 240.0f) { rr = 0.0f; gg = x; bb = c; }
+    else if (hue < 300.0f) { rr = x; gg = 0.0f; bb = c; }
+    else { rr = c; gg = 0.0f; bb = x; }
+    *r = rr + m;
+    *g = gg + m;
+    *b = bb + m;
+}
+
+/* Rust's `f as u8`: NaN -> 0, saturating, truncating; the colour channel is
+ * scaled by 255 first (macroquad's Color -> [u8; 4] conversion). */
+static uint8_t channel_u8(float c) {
+    float v = c * 255.0f;
+    if (!(v > 0.0f)) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint8_t)v;
+}
+
+/* render_simulation (src/visualization.rs:79-105) into rgba[ny][nx][4]:
+ * color_type 0 pressure (:49-70), 1 speed (:29-47). */
+void orc_render(const orc_sim *s, int color_type, uint8_t *rgba) {
+    const int nx = s->nx, ny = s->ny;
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) {
+            size_t i = (size_t)x * ny + y;
+            float r, g, b, a = 1.0f;
+            if (s->kind[i] != ORC_FLUID) {
+                if (color_type == 1) { r = 0.5f; g = 0.5f; b = 0.5f; }
+                else { r = 0.5f; g = 0.0f; b = 0.0f; }
+            } else {
+                double hue_d;
+                if (color_type == 1) {
+                    double speed = sqrt(sq(s->u[i]) + sq(s->v[i]));
+                    hue_d = 240.0 - (speed - s->speed_range[0]) * 240.0 /
+                                        (s->speed_range[1] - s->speed_range[0]);
+                } else {
+                    double offset = 240.0;
+                    hue_d = offset - (s->p[i] - s->pressure_range[0]) * offset /
+                                         (s->pressure_range[1] - s->pressure_range[0]);
+                }
+                hsl_to_rgb((float)hue_d, 1.0f, 0.5f, &r, &g, &b);
+            }
+            uint8_t *px = rgba + ((size_t)y * nx + x) * 4;
+            px[0] = channel_u8(r);
+            px[1] = channel_u8(g);
+            px[2] = channel_u8(b);
+            px[3] = channel_u8(a);
+        }
+}

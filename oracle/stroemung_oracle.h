@@ -121,6 +121,9 @@ void orc_set_u_and_v(orc_sim *s);
 void orc_adapt_dt(orc_sim *s);
 void orc_calculate_pressure_range(orc_sim *s);
 void orc_calculate_speed_range(orc_sim *s);
+/* Colour map of src/visualization.rs:79-105 into rgba[ny][nx][4]
+ * (0 pressure, 1 speed). */
+void orc_render(const orc_sim *s, int color_type, uint8_t *rgba);
 /* A tick with its phases timed, for the CPU baseline (see the .c file). */
 void orc_tick_timed(orc_sim *s, uint32_t max_iterations_cap, double *out4);
 

@@ -25,6 +25,7 @@ FIELD_U, FIELD_V, FIELD_P, FIELD_F, FIELD_G, FIELD_RHS = range(6)
 SOR_RED_BLACK, SOR_LEXICOGRAPHIC = 0, 1
 ARITH_EXACT, ARITH_FAST = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+EXEC_GRAPH, EXEC_EAGER = 0, 1
 
 
 class Params(ctypes.Structure):
@@ -40,7 +41,7 @@ class Params(ctypes.Structure):
 class Mode(ctypes.Structure):
     _fields_ = [("sor_order", ctypes.c_int), ("arithmetic", ctypes.c_int),
                 ("precision", ctypes.c_int), ("strict_eps", ctypes.c_int),
-                ("inner_sweeps", ctypes.c_int)]
+                ("inner_sweeps", ctypes.c_int), ("execution", ctypes.c_int)]
 
 
 class State(ctypes.Structure):
@@ -92,6 +93,7 @@ SIGNATURES = {
     "strm_calculate_speed_range": [_vp],
     "strm_device_view_get": [_vp, ctypes.POINTER(DeviceView)],
     "strm_sor_sweeps": [_vp, ctypes.c_int, _dp],
+    "strm_render_rgba": [_vp, ctypes.c_int, _u8p],
     "strm_synchronize": [_vp],
     "strm_host_classify": [ctypes.c_int, ctypes.c_int, _u8p, _u8p, _dp, _i64p],
     "strm_host_boundary_pass": [ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp, _dp],

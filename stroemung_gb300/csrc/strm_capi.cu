@@ -66,6 +66,7 @@ struct strm_sim {
   StepState *h_st = nullptr;   // pinned
   StepLog *h_log = nullptr;    // pinned
   int bc_cap = 0, pcopy_cap = 0;
+  void *rgba = nullptr;        // colour-map image, allocated on first use
 };
 
 namespace {
@@ -119,7 +120,8 @@ void update_cfg(strm_sim *s) {
   if (s->g.nx < 3 || s->g.ny < 3) r.sor_order = 1;
   r.arith = s->mode.arithmetic == STRM_ARITH_FAST ? 1 : 0;
   r.precision = s->mode.precision;
-  r.inner_sweeps = s->mode.inner_sweeps > 0 ? s->mode.inner_sweeps : 8;
+  r.inner_sweeps = s->mode.inner_sweeps > 0 ? s->mode.inner_sweeps : 16;
+  r.eager = s->mode.execution == STRM_EXEC_EAGER ? 1 : 0;
 }
 
 int rebuild_graph(strm_sim *s) {
@@ -204,6 +206,7 @@ void free_sim(strm_sim *s) {
   if (s->d.bc) cudaFree(s->d.bc);
   if (s->d.bc_val) cudaFree(s->d.bc_val);
   if (s->d.pcopy) cudaFree(s->d.pcopy);
+  if (s->rgba) cudaFree(s->rgba);
   if (s->h_st) cudaFreeHost(s->h_st);
   if (s->h_log) cudaFreeHost(s->h_log);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -260,7 +263,8 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   if (!s) return fail(STRM_ERR_INVALID, "out of host memory");
   s->dev = dev;
   s->prm = *params;
-  s->mode = strm_mode{STRM_SOR_RED_BLACK, STRM_ARITH_EXACT, STRM_PREC_FP64, 0, 0};
+  s->mode = strm_mode{STRM_SOR_RED_BLACK, STRM_ARITH_EXACT, STRM_PREC_FP64, 0, 0,
+                      STRM_EXEC_GRAPH};
   s->g.nx = nx;
   s->g.ny = ny;
   s->g.pitch = (int)align_up((size_t)ny, 16);
@@ -374,7 +378,8 @@ int strm_destroy(strm_sim *sim) {
 int strm_set_mode(strm_sim *s, const strm_mode *mode) {
   if (!s || !mode) return fail(STRM_ERR_INVALID, "invalid arguments");
   if (mode->sor_order < 0 || mode->sor_order > 1 || mode->arithmetic < 0 ||
-      mode->arithmetic > 1 || mode->precision < 0 || mode->precision > 1)
+      mode->arithmetic > 1 || mode->precision < 0 || mode->precision > 1 ||
+      mode->execution < 0 || mode->execution > 1 || mode->inner_sweeps < 0)
     return fail(STRM_ERR_INVALID, "unknown mode value");
   CK(cudaSetDevice(s->dev));
   s->mode = *mode;
@@ -384,7 +389,10 @@ int strm_set_mode(strm_sim *s, const strm_mode *mode) {
 int strm_tick(strm_sim *s, uint32_t *sor_iterations, double *norm_squared) {
   if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
   CK(cudaSetDevice(s->dev));
-  CK(cudaGraphLaunch(s->exec, s->stream));
+  if (s->cfg.eager)
+    CK(run_step_eager(s->d, s->cfg, s->stream, s->h_st));
+  else
+    CK(cudaGraphLaunch(s->exec, s->stream));
   int rc = sync_state(s);
   if (rc) return rc;
   if (sor_iterations) *sor_iterations = s->h_st->sor_iters;
@@ -403,7 +411,12 @@ int strm_step_n(strm_sim *s, int n, strm_step_stats *stats) {
     const unsigned int zero = 0;
     CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice,
                        s->stream));
-    for (int i = 0; i < chunk; ++i) CK(cudaGraphLaunch(s->exec, s->stream));
+    for (int i = 0; i < chunk; ++i) {
+      if (s->cfg.eager)
+        CK(run_step_eager(s->d, s->cfg, s->stream, s->h_st));
+      else
+        CK(cudaGraphLaunch(s->exec, s->stream));
+    }
     if (stats)
       CK(cudaMemcpyAsync(s->h_log, s->d.log, sizeof(StepLog) * chunk, cudaMemcpyDeviceToHost,
                          s->stream));
@@ -628,6 +641,18 @@ int strm_calculate_speed_range(strm_sim *s) {
   if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
   CK(cudaSetDevice(s->dev));
   CK(launch_velocity(s->d, s->cfg, s->stream, 0, 1, 0));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_render_rgba(strm_sim *s, int color_type, uint8_t *rgba) {
+  if (!s || !rgba || color_type < 0 || color_type > 1)
+    return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  const size_t bytes = (size_t)s->g.nx * s->g.ny * 4;
+  if (!s->rgba) CK(cudaMalloc(&s->rgba, bytes));
+  CK(launch_render(s->d, s->g, color_type, s->rgba, s->stream));
+  CK(cudaMemcpyAsync(rgba, s->rgba, bytes, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return STRM_OK;
 }

@@ -679,6 +679,199 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------------------
+// Mixed-precision pressure solve: FP32 red-black sweeps on the FP64 defect,
+// FP64 norm and FP64 accumulation of the correction (iterative refinement).
+//
+//   start:  e = 0; boundary copy of p; s = (float)(middle * residual(p))
+//   repeat: m x [red sweep + red boundary copy, black sweep + black boundary
+//           copy] on  Lap(e) = rhs - Lap(p)  in FP32;
+//           p += e on fluid cells, e = 0; boundary copy of p;
+//           FP64 norm of residual(p) -> stop rule; s = (float)(middle * r)
+//
+// The boundary copy of the correction is folded into the sweeps: a red
+// boundary cell takes its black fluid neighbours' values, which the red sweep
+// does not change; a black boundary cell takes red values, final once the red
+// sweep is done.  So one sweep kernel per colour and no copy launches.
+// ------------------------------------------------------------------------
+
+struct Consts32 {
+  float omw;      // 1 - omega
+  float a, b;     // middle / dx^2, middle / dy^2
+};
+
+__device__ __forceinline__ float copy32(const float *e, size_t o, int pitch, int edge) {
+  switch (edge) {
+    case E_N: return e[o - 1];
+    case E_NE: return (e[o - 1] + e[o + pitch]) * 0.5f;
+    case E_E: return e[o + pitch];
+    case E_SE: return (e[o + 1] + e[o + pitch]) * 0.5f;
+    case E_S: return e[o + 1];
+    case E_SW: return (e[o + 1] + e[o - pitch]) * 0.5f;
+    case E_W: return e[o - pitch];
+    default: return (e[o - 1] + e[o - pitch]) * 0.5f;  // E_NW
+  }
+}
+
+// One colour over the whole grid: fluid interior cells of the colour get the
+// SOR update, boundary cells of the colour with an edge get the copy.
+__global__ void __launch_bounds__(256)
+    sor32_color_kernel(float *__restrict__ e, const float *__restrict__ s,
+                       const uint8_t *__restrict__ flags, Geom g, Consts32 k, int color) {
+  const int x = blockIdx.y * blockDim.y + threadIdx.y;
+  const int y = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((x + color) & 1);
+  if (x >= g.nx || y >= g.ny) return;
+  const size_t o = OFF(x, y);
+  const uint8_t fl = flags[o];
+  if (fl == 0) {
+    if (x < 1 || y < 1 || x > g.nx - 2 || y > g.ny - 2) return;
+    const float sum_x = e[o - g.pitch] + e[o + g.pitch];
+    const float sum_y = e[o - 1] + e[o + 1];
+    e[o] = fmaf(k.omw, e[o], fmaf(k.a, sum_x, fmaf(k.b, sum_y, s[o])));
+  } else if (edge_of(fl) != E_NONE) {
+    e[o] = copy32(e, o, g.pitch, edge_of(fl));
+  }
+}
+
+// p += e on fluid interior cells (apply != 0), then e = 0 everywhere.
+__global__ void __launch_bounds__(256)
+    refine_kernel(double *__restrict__ p, float *__restrict__ e, const uint8_t *__restrict__ flags,
+                  Geom g, int apply) {
+  const int x = blockIdx.y * blockDim.y + threadIdx.y;
+  const int y0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (x >= g.nx) return;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int y = y0 + q;
+    if (y >= g.ny) break;
+    const size_t o = OFF(x, y);
+    if (apply && flags[o] == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2)
+      p[o] = p[o] + (double)e[o];
+    e[o] = 0.0f;
+  }
+}
+
+// FP64 norm of the residual on every interior cell (the reference's norm),
+// the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
+// and the stop rule every m sweeps.
+template <bool IN_GRAPH>
+__global__ void __launch_bounds__(256)
+    mixed_residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
+                          const uint8_t *__restrict__ flags, float *__restrict__ s, Geom g,
+                          Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
+                          cudaGraphConditionalHandle h, unsigned int itermax, int strict,
+                          int sweeps, int check) {
+  double acc = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
+    if (x > g.nx - 2) continue;
+    const int yb = 1 + (t % tiles_y) * RT_Y + 2 * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = yb + q;
+      if (y <= g.ny - 2) {
+        const size_t o = OFF(x, y);
+        const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
+                                            p[o + 1], rhs[o], c);
+        acc = fma(r, r, acc);
+        if (flags[o] == 0) s[o] = (float)(c.middle * r);
+      }
+    }
+  }
+  const double bsum = block_reduce(acc, OpAdd(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = bsum;
+  if (IN_GRAPH && check && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    // independent bound on the WHILE loop, as in residual_kernel
+    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
+    if ((unsigned long long)launches * (unsigned long long)sweeps >= itermax + 2ull * sweeps) {
+      st->overrun = 1;
+      cudaGraphSetConditional(h, 0);
+    }
+  }
+  if (!last_block_done(&st->counter)) return;
+  const double total = reduce_partials(partials, gridDim.x, 1, 0, OpAdd(), 0.0);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    const double ns = total / st->fluid_cells;
+    st->ns = ns;
+    if (check) {
+      const unsigned int it = st->sor_iters + sweeps;
+      st->sor_iters = it;
+      st->nonfinite = !isfinite(ns);
+      const bool done = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      const bool room = it + sweeps <= itermax;
+      if (done) st->converged = 1;
+      else if (!room) st->exhausted = 1;
+      if (IN_GRAPH && (done || !room)) cudaGraphSetConditional(h, 0);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// Headless colour map (src/visualization.rs:7-105): pressure or speed of
+// every cell to RGBA8, image rows = y, as the reference's macroquad Image
+// (width nx).  Same f32 arithmetic as the reference; channel bytes are
+// (c * 255) converted like Rust's `as u8` (NaN -> 0, saturating, truncating).
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned char channel_u8(float c) {
+  const float v = c * 255.0f;
+  if (!(v > 0.0f)) return 0;
+  if (v >= 255.0f) return 255;
+  return (unsigned char)v;
+}
+
+__global__ void render_kernel(const double *__restrict__ u, const double *__restrict__ v,
+                              const double *__restrict__ p, const uint8_t *__restrict__ flags,
+                              Geom g, const StepState *st, int color_type, uchar4 *rgba) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= g.nx || y >= g.ny) return;
+  const size_t o = OFF(x, y);
+  float r, gg, b;
+  if (is_bnd(flags[o])) {
+    r = 0.5f;
+    gg = color_type == 1 ? 0.5f : 0.0f;
+    b = color_type == 1 ? 0.5f : 0.0f;
+  } else {
+    double hue_d;
+    if (color_type == 1) {
+      const double r0 = ord_dec(st->s2_min), r1 = ord_dec(st->s2_max);
+      const double speed = sqrt(sqd(u[o]) + sqd(v[o]));
+      hue_d = 240.0 - (speed - r0) * 240.0 / (r1 - r0);
+    } else {
+      const double r0 = ord_dec(st->p_min), r1 = ord_dec(st->p_max);
+      const double offset = 240.0;
+      hue_d = offset - (p[o] - r0) * offset / (r1 - r0);
+    }
+    const float hue = (float)hue_d;
+    // hsl_to_rgb(hue, 1, 0.5), src/visualization.rs:7-27
+    const float sat = 1.0f, light = 0.5f;
+    const float c = (1.0f - fabsf(2.0f * light - 1.0f)) * sat;
+    const float xx = c * (1.0f - fabsf(fmodf(hue / 60.0f, 2.0f) - 1.0f));
+    const float m = light - c / 2.0f;
+    float rr, g2, bb;
+    if (hue < 60.0f) { rr = c; g2 = xx; bb = 0.0f; }
+    else if (hue < 120.0f) { rr = xx; g2 = c; bb = 0.0f; }
+    else if (hue < 180.0f) { rr = 0.0f; g2 = c; bb = xx; }
+    else if (hue < 240.0f) { rr = 0.0f; g2 = xx; bb = c; }
+    else if (hue < 300.0f) { rr = xx; g2 = 0.0f; bb = c; }
+    else { rr = c; g2 = 0.0f; bb = xx; }
+    r = rr + m;
+    gg = g2 + m;
+    b = bb + m;
+  }
+  rgba[(size_t)y * g.nx + x] = make_uchar4(channel_u8(r), channel_u8(gg), channel_u8(b),
+                                           channel_u8(1.0f));
+}
+
+cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, void *rgba,
+                          cudaStream_t s) {
+  dim3 blk(32, 8), grd((g.nx + 31) / 32, (g.ny + 7) / 8);
+  render_kernel<<<grd, blk, 0, s>>>(d.u, d.v, d.p, d.flags, g, d.st, color_type, (uchar4 *)rgba);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------
 
@@ -808,6 +1001,87 @@ cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s) 
 }
 
 // ------------------------------------------------------------------------
+// eager step: the graph's kernels launched one by one, the pressure loop
+// driven from the host (one 12-byte read per iteration).  Same kernels in the
+// same order, so results equal the graph's bit for bit; meant for profilers
+// that cannot see into conditional graph nodes, and for debugging.
+// ------------------------------------------------------------------------
+
+static cudaError_t poll_done(const DevFields &d, cudaStream_t s, StepState *h, bool *done) {
+  cudaError_t e = cudaMemcpyAsync(&h->sor_iters, &d.st->sor_iters, 4 * sizeof(unsigned int),
+                                  cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  *done = h->converged || h->exhausted;
+  return e;
+}
+
+cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, StepState *h) {
+  const Geom g = r.g;
+  const Consts c = r.c;
+  int ty_all, nt_all, ty_int, nt_int;
+  tiles_of(g, 0, &ty_all, &nt_all);
+  tiles_of(g, 1, &ty_int, &nt_int);
+  const int nb = residual_blocks(g);
+  cudaError_t e;
+  bc_kernel<<<BC_CLUSTER, BC_THREADS, 0, s>>>(d.u, d.v, d.ru, d.rv, d.bc, d.bc_val, d.n_bc, d.st,
+                                              c, r.tau, r.delt, r.itermax, 1);
+  if ((e = launch_fg_rhs(d, r, s)) != cudaSuccess) return e;
+  bool done = false;
+  if (r.sor_order == 1) {
+    if ((e = launch_sor_lex(d, r, s)) != cudaSuccess) return e;
+  } else if (r.precision == 1 && nt_int > 0 && r.itermax > 0) {
+    const int m = (int)((unsigned)r.inner_sweeps < r.itermax ? (unsigned)r.inner_sweeps : r.itermax);
+    Consts32 k32;
+    k32.omw = (float)c.one_minus_w;
+    k32.a = (float)(c.middle * c.r_dx2);
+    k32.b = (float)(c.middle * c.r_dy2);
+    dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (g.nx + kRedBlock.y - 1) / kRedBlock.y);
+    refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 0);
+    if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+    mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
+                                                          d.partials, ty_int, nt_int, 0,
+                                                          r.itermax, r.strict_eps, m, 0);
+    while (!done) {
+      for (int i = 0; i < m; ++i)
+        for (int color = 0; color < 2; ++color)
+          sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color);
+      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 1);
+      if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+      mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
+                                                            d.st, d.partials, ty_int, nt_int, 0,
+                                                            r.itermax, r.strict_eps, m, 1);
+      if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
+    }
+  } else if (nt_int > 0 && r.itermax > 0) {
+    dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+    while (!done) {
+      if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+      for (int color = 0; color < 2; ++color) {
+        if (r.arith)
+          sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
+        else
+          sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
+      }
+      if (r.arith)
+        residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, g, c, d.st, d.partials,
+                                                               ty_int, nt_int, 0, r.itermax,
+                                                               r.strict_eps, RES_SOLVE);
+      else
+        residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, g, c, d.st, d.partials,
+                                                              ty_int, nt_int, 0, r.itermax,
+                                                              r.strict_eps, RES_SOLVE);
+      if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
+    }
+  }
+  prange_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.flags, g, d.st, d.partials, ty_all, nt_all, 0);
+  velocity_kernel<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, g, c,
+                                           d.st, d.partials, d.log, ty_all, nt_all, 1, 1, 1);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
 // step graph
 // ------------------------------------------------------------------------
 
@@ -872,6 +1146,49 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     n = b.kernel(b.graph, n, (const void *)sor_lex_kernel, dim3(1), dim3(1024), d.p,
                  (const double *)d.rhs, (const uint8_t *)d.flags, (const PCopy *)d.pcopy,
                  d.n_pcopy, g, c, d.st, d.pw, r.itermax, r.strict_eps);
+  } else if (r.precision == 1 && nt_int > 0 && r.itermax > 0) {
+    const int m = (int)((unsigned)r.inner_sweeps < r.itermax ? (unsigned)r.inner_sweeps : r.itermax);
+    Consts32 k32;
+    k32.omw = (float)c.one_minus_w;
+    k32.a = (float)(c.middle * c.r_dx2);
+    k32.b = (float)(c.middle * c.r_dy2);
+    dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (g.nx + kRedBlock.y - 1) / kRedBlock.y);
+    cudaGraphConditionalHandle h;
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
+    n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
+                 (const uint8_t *)d.flags, g, 0);
+    if (d.n_pcopy > 0)
+      n = b.kernel(b.graph, n, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
+                   dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+    n = b.kernel(b.graph, n, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
+                 (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32, g,
+                 c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 0);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&wnode, b.graph, &n, nullptr, 1, &cp);
+    if (b.err == cudaSuccess) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      cudaGraphNode_t bn = nullptr;
+      for (int i = 0; i < m; ++i)
+        for (int color = 0; color < 2; ++color)
+          bn = b.kernel(body, bn, (const void *)sor32_color_kernel, pgrid, kRedBlock, d.e32,
+                        (const float *)d.r32, (const uint8_t *)d.flags, g, k32, color);
+      bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
+                    (const uint8_t *)d.flags, g, 1);
+      if (d.n_pcopy > 0)
+        bn = b.kernel(body, bn, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
+                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+      bn = b.kernel(body, bn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
+                    (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32,
+                    g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 1);
+    }
+    n = wnode;
   } else if (nt_int > 0 && r.itermax > 0) {
     cudaGraphConditionalHandle h;
     if (b.err == cudaSuccess)

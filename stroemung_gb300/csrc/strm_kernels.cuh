@@ -42,6 +42,7 @@ struct RunCfg {
   int arith;              // 0 exact, 1 fast
   int precision;          // 0 fp64, 1 mixed
   int inner_sweeps;
+  int eager;              // 1: launch kernels one by one instead of the graph
 };
 
 // Standalone launches (phase entry points, creation).
@@ -57,6 +58,14 @@ cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, i
 cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s);
 // One red-black pressure iteration (copy, red, black, residual) without a stop test.
 cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s);
+
+// Colour map into a device RGBA8 image [ny][nx] (0 pressure, 1 speed).
+cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, void *rgba,
+                          cudaStream_t s);
+
+// One step with every kernel launched eagerly and the pressure loop driven
+// from the host; h is pinned host memory for the polled flags.
+cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, StepState *h);
 
 // Builds the whole step as one CUDA graph (the pressure loop as a
 // conditional WHILE node for the red-black solve).

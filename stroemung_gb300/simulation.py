@@ -51,7 +51,7 @@ class Simulation:
                  omega: float = 1.7, iterations: int = 0, time: float = 0.0,
                  initial_norm_squared=None, tau: float = 0.0, sor_order: int = SOR_RED_BLACK,
                  arithmetic: int = ARITH_EXACT, precision: int = PREC_FP64,
-                 strict_eps: bool = False, inner_sweeps: int = 0):
+                 strict_eps: bool = False, inner_sweeps: int = 0, execution: int = 0):
         L = _lib.load()
         kind = np.ascontiguousarray(grid["kind"], dtype=np.uint8)
         self.size = tuple(int(s) for s in kind.shape)
@@ -84,8 +84,27 @@ class Simulation:
             raise BoundaryTooThinError(rc, f"{_lib.last_error()} at {divmod(bad.value, ny)}")
         _lib.check(rc)
         self._h = h
+        # host copies of what the device keeps only in compiled form
+        self._kind = kind.copy()
+        self._wall = np.zeros((nx, ny, 2)) if wall is None else wall.copy()
         self.set_mode(sor_order=sor_order, arithmetic=arithmetic, precision=precision,
-                      strict_eps=strict_eps, inner_sweeps=inner_sweeps)
+                      strict_eps=strict_eps, inner_sweeps=inner_sweeps, execution=execution)
+
+    @classmethod
+    def from_json(cls, path_or_text, float_parser: str = "serde", **mode):
+        """Simulation::from_reader (src/simulation.rs:117-120)."""
+        from . import jsonio
+        return jsonio.load_simulation(path_or_text, float_parser, **mode)
+
+    def to_json(self) -> str:
+        """Simulation's serde layout (src/simulation.rs:49-69)."""
+        from . import jsonio
+        return jsonio.dumps_simulation(self)
+
+    def grid_dict(self) -> dict:
+        """Host copy of the grid: kind, wall_uv, u, v, p."""
+        return {"kind": self._kind.copy(), "wall_uv": self._wall.copy(), "u": self.download("u"),
+                "v": self.download("v"), "p": self.download("p")}
 
     @classmethod
     def try_from(cls, unfinalized: dict, **mode):
@@ -120,12 +139,14 @@ class Simulation:
 
     # ---- configuration ---------------------------------------------------
     def set_mode(self, *, sor_order=SOR_RED_BLACK, arithmetic=ARITH_EXACT, precision=PREC_FP64,
-                 strict_eps=False, inner_sweeps=0):
+                 strict_eps=False, inner_sweeps=0, execution=0):
         m = _lib.Mode(sor_order=sor_order, arithmetic=arithmetic, precision=precision,
-                      strict_eps=1 if strict_eps else 0, inner_sweeps=inner_sweeps)
+                      strict_eps=1 if strict_eps else 0, inner_sweeps=inner_sweeps,
+                      execution=execution)
         _lib.check(_lib.load().strm_set_mode(self._h, ctypes.byref(m)))
         self.mode = {"sor_order": sor_order, "arithmetic": arithmetic, "precision": precision,
-                     "strict_eps": bool(strict_eps), "inner_sweeps": inner_sweeps}
+                     "strict_eps": bool(strict_eps), "inner_sweeps": inner_sweeps,
+                     "execution": execution}
 
     # ---- the timestep (src/simulation.rs:324-333) --------------------------
     def run_simulation_tick(self):
@@ -191,6 +212,8 @@ class Simulation:
             ys.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
             kinds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
             _dp(w) if w is not None else None, ctypes.byref(bad)))
+        self._kind[xs, ys] = kinds
+        self._wall[xs, ys] = 0.0 if w is None else w
 
     # ---- scalar state -------------------------------------------------------
     def state(self) -> dict:
@@ -248,6 +271,15 @@ class Simulation:
     def calculate_speed_range(self):
         _lib.check(_lib.load().strm_calculate_speed_range(self._h))
 
+    def render(self, color_type: str = "pressure") -> np.ndarray:
+        """render_simulation (src/visualization.rs:79-105) on the GPU:
+        [ny, nx, 4] uint8 RGBA, image row = y."""
+        ct = {"pressure": 0, "speed": 1}[color_type]
+        out = np.empty((self.size[1], self.size[0], 4), dtype=np.uint8)
+        _lib.check(_lib.load().strm_render_rgba(
+            self._h, ct, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out
+
     def device_view(self) -> dict:
         dv = _lib.DeviceView()
         _lib.check(_lib.load().strm_device_view_get(self._h, ctypes.byref(dv)))
@@ -284,3 +316,19 @@ def host_boundary_pass(kind, wall_uv, u, v):
         nx, ny, kind.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
         _dp(w) if w is not None else None, _dp(u), _dp(v), _dp(ru), _dp(rv)))
     return u, v, ru, rv
+
+
+def write_png(path, rgba: np.ndarray) -> None:
+    """Writes an [h, w, 4] uint8 image as a PNG (zlib, no imaging library)."""
+    import struct
+    import zlib
+    h, w, _ = rgba.shape
+    raw = b"".join(b"\x00" + np.ascontiguousarray(rgba[y]).tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return (struct.pack(">I", len(data)) + tag + data +
+                struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff))
+    png = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+           chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+    with open(path, "wb") as f:
+        f.write(png)

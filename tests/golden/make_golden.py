@@ -212,6 +212,25 @@ def main():
     tick["params"] = params
     gold["simulation_tick"] = tick
 
+    # python/test_generate_test_data.py: a 440-byte NaSt2D .out file and the
+    # grid JSON the reference's converter makes of it
+    import base64
+    td = REF / "python" / "test_data"
+    gold["nast2d"] = {
+        "out_b64": base64.b64encode((td / "small_data.out").read_bytes()).decode(),
+        "expected": json.loads((td / "small_data.out_expected.json").read_text()),
+        "rust_expected": json.loads((td / "small_data.out_rust_expected.json").read_text()),
+    }
+    # the grid/simulation JSON fixtures as text, so that loaders can be checked
+    # with the reference's own float parsing
+    gold["fixture_text"] = {
+        name: (REF / "src" / "test_data" / name).read_text()
+        for name in ("simple_grid.json", "small_grid_with_boundaries.json",
+                     "simple_simulation.json", "small_simulation_with_boundaries.json")
+    }
+    gold["fixture_text"]["small_data.out.json"] = (
+        REF / "tests" / "test_data" / "small_data.out.json").read_text()
+
     OUT.write_text(json.dumps(gold, indent=1, sort_keys=True) + "\n")
     print(f"wrote {OUT}")
 

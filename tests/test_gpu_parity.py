@@ -282,3 +282,56 @@ def test_cavity_moving_wall_matches_oracle():
     for _ in range(20):
         assert s.run_simulation_tick() == o.tick()
     assert_fields_equal(o, s, "cavity")
+
+
+def test_mixed_precision_matches_fp64_on_converged_cavity():
+    """FP32 sweeps on the FP64 defect with FP64 refinement reach the same
+    solution as the FP64 red-black solve at a converged residual."""
+    g = presets.cavity(64)
+    prm = dict(cell_size=(1 / 64, 1 / 64), delt=0.002, gamma=0.9, reynolds=1000.0, eps=1e-7,
+               max_iterations=20000, omega=1.8, tau=0.5)
+    kw = dict(grid=g, cell_size=prm["cell_size"], delt=prm["delt"], gamma=prm["gamma"],
+              reynolds=prm["reynolds"], sor_absolute_epsilon=prm["eps"],
+              max_iterations=prm["max_iterations"], omega=prm["omega"], tau=prm["tau"],
+              strict_eps=True)
+    ref = Simulation(**kw)
+    mix = Simulation(precision=1, inner_sweeps=16, **kw)
+    for _ in range(20):
+        i_r, n_r = ref.run_simulation_tick()
+        i_m, n_m = mix.run_simulation_tick()
+        assert n_r < 1e-14 and n_m < 1e-14, (i_r, n_r, i_m, n_m)
+        assert i_m % 16 == 0
+    for n in ("u", "v"):
+        assert rel_l2(mix.download(n), ref.download(n)) < 1e-6, n
+    assert rel_l2(p_fluid(mix.download("p"), g["kind"]), p_fluid(ref.download("p"), g["kind"])) < 1e-6
+
+
+def test_mixed_precision_channel_runs_and_tracks_fp64():
+    rects = presets.random_rectangles(256, 64, 6, 1, x_margin=16)
+    g = presets.channel(256, 64, rects)
+    prm = dict(grid=g, cell_size=(0.04, 0.04), delt=0.01, gamma=0.9, reynolds=400.0,
+               sor_absolute_epsilon=1e-3, max_iterations=512, omega=1.7, tau=0.5)
+    ref = Simulation(arithmetic=1, **prm)
+    mix = Simulation(precision=1, inner_sweeps=16, **prm)
+    for _ in range(10):
+        i_r, _ = ref.run_simulation_tick()
+        i_m, _ = mix.run_simulation_tick()
+        assert i_m <= 512 and i_m % 16 == 0
+    for n in ("u", "v"):
+        assert rel_l2(mix.download(n), ref.download(n)) < 1e-3, n
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_eager_execution_equals_graph(precision):
+    """The eager path launches the graph's kernels one by one: identical bits."""
+    rects = presets.random_rectangles(128, 48, 3, 2, x_margin=12)
+    g = presets.channel(128, 48, rects)
+    prm = dict(grid=g, cell_size=(0.05, 0.05), delt=0.01, gamma=0.9, reynolds=300.0,
+               sor_absolute_epsilon=1e-3, max_iterations=96, omega=1.7, tau=0.5,
+               precision=precision, inner_sweeps=8)
+    a = Simulation(**prm)
+    b = Simulation(execution=1, **prm)
+    for _ in range(8):
+        assert a.run_simulation_tick() == b.run_simulation_tick()
+    for n in ("u", "v", "p", "f", "g", "rhs"):
+        assert_bits_equal(b.download(n), a.download(n), n)
