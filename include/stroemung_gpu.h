@@ -199,6 +199,28 @@ int strm_calculate_speed_range(strm_sim *sim);     /* src/grid/mod.rs:253-268 */
  * otherwise waits and returns the last iteration's norm. */
 int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
 
+/* Residual norm that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they need the norm:
+ * code running inside a CUDA stream capture (cudaMalloc is not permitted
+ * there), host frameworks whose own memory pool owns the device budget, and
+ * fixed-footprint real-time loops.  Same quantity as
+ * strm_calculate_norm_squared (sum of squared residuals over the interior
+ * cells divided by fluid_cells, reference operation order) on caller-owned
+ * pitched fields p and rhs ([nx][pitch], y contiguous); the result is written
+ * to the device double *norm_squared, asynchronously on `stream` (a
+ * cudaStream_t, NULL for the default stream).
+ * Its reduction scratch is a fixed __device__ array inside this library
+ * (about 130 KB, held by every GPU that loads it until the process exits):
+ * grids with more than STRM_NORM_NOALLOC_MAX_TILES interior tiles of 8 x 64
+ * cells are rejected with STRM_ERR_INVALID.  The first call on a device looks
+ * up that array's device address; make that first call before any stream
+ * capture.  All calls share the one array: calls whose GPU work overlaps
+ * (different streams or threads) race and must be serialised by the caller. */
+#define STRM_NORM_NOALLOC_MAX_TILES 16384
+int strm_norm_squared_noalloc(const double *p, const double *rhs, int nx, int ny, int pitch,
+                              double dx, double dy, double fluid_cells, double *norm_squared,
+                              void *stream);
+
 /* Waits until all work queued on the simulation's stream has finished. */
 int strm_synchronize(strm_sim *sim);
 

@@ -95,6 +95,8 @@ SIGNATURES = {
     "strm_sor_sweeps": [_vp, ctypes.c_int, _dp],
     "strm_render_rgba": [_vp, ctypes.c_int, _u8p],
     "strm_synchronize": [_vp],
+    "strm_norm_squared_noalloc": [_dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _vp],
     "strm_host_classify": [ctypes.c_int, ctypes.c_int, _u8p, _u8p, _dp, _i64p],
     "strm_host_boundary_pass": [ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp, _dp],
     "strm_last_error": [ctypes.c_char_p, ctypes.c_size_t],

@@ -949,6 +949,23 @@ cudaError_t launch_norm(const DevFields &d, const RunCfg &r, cudaStream_t s, int
   return cudaGetLastError();
 }
 
+int interior_tiles(const Geom &g) {
+  int ty, nt;
+  tiles_of(g, 1, &ty, &nt);
+  return nt;
+}
+
+cudaError_t launch_norm_one_block_per_tile(const double *p, const double *rhs, const Geom &g,
+                                           const Consts &c, StepState *st, double *partials,
+                                           cudaStream_t s) {
+  int ty, nt;
+  tiles_of(g, 1, &ty, &nt);
+  if (nt == 0) return cudaSuccess;
+  residual_kernel<true, false><<<nt, kRedBlock, 0, s>>>(p, rhs, g, c, st, partials, ty, nt, 0,
+                                                        0u, 0, RES_NORM);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_velocity(const DevFields &d, const RunCfg &r, cudaStream_t s, int update,
                             int commit_speed, int advance) {
   int ty, nt;

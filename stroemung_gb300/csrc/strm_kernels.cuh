@@ -73,4 +73,12 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
 
 int residual_blocks(const Geom &g);
 
+// Residual norm of raw pitched fields with one block per 8x64 tile of the
+// interior: partials[] must hold interior_tiles(g) doubles; st->fluid_cells
+// must be set and st->counter zero; the norm lands in st->aux.
+int interior_tiles(const Geom &g);
+cudaError_t launch_norm_one_block_per_tile(const double *p, const double *rhs, const Geom &g,
+                                           const Consts &c, StepState *st, double *partials,
+                                           cudaStream_t s);
+
 }  // namespace strm
