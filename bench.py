@@ -189,6 +189,10 @@ def main():
     ap.add_argument("--ref-cap", type=int, default=10)
     ap.add_argument("--cpu-ticks", type=int, default=3)
     ap.add_argument("--cpu-cap", type=int, default=50)
+    ap.add_argument("--mixed", type=int, default=1)
+    ap.add_argument("--eager", type=int, default=0,
+                    help="1: launch kernels one by one (for per-kernel profiling)")
+    ap.add_argument("--inner-sweeps", type=int, default=16)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -215,7 +219,7 @@ def main():
 
     grid = workload(SEED + rank)
     arith = ARITH_FAST if args.arith == "fast" else ARITH_EXACT
-    sim = Simulation(grid=grid, arithmetic=arith, **PARAMS)
+    sim = Simulation(grid=grid, arithmetic=arith, execution=args.eager, **PARAMS)
     view = sim.device_view()
     stream = torch.cuda.ExternalStream(view["stream"])
 
@@ -241,6 +245,7 @@ def main():
     iters = [s[0] for s in stats]
     n_pcopy_launch = 1
     launches = sum(2 + 3 + n_pcopy_launch + (3 + n_pcopy_launch) * (k - 1) + 2 for k in iters)
+    fp64_fields = {n: sim.download(n) for n in ("u", "v", "p")}
 
     # ---- dominant kernel: one red-black iteration, timed live ----
     nsweep = 20
@@ -276,6 +281,57 @@ def main():
         del a
     except Exception:
         pass
+
+    # ---- mixed precision on the same workload: FP32 sweeps, FP64 norm and
+    # refinement; same warm-up and timed steps from the same initial state ----
+    mixed = None
+    if args.mixed:
+        from stroemung_gb300.simulation import PREC_MIXED
+        simm = Simulation(grid=grid, precision=PREC_MIXED, inner_sweeps=args.inner_sweeps,
+                          execution=args.eager, **PARAMS)
+        stream_m = torch.cuda.ExternalStream(simm.device_view()["stream"])
+        warm_m = simm.step_n(args.warmup)
+        torch.cuda.synchronize()
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        m0.record(stream_m)
+        stats_m = simm.step_n(args.steps)
+        m1.record(stream_m)
+        torch.cuda.synchronize()
+        ms_m = m0.elapsed_time(m1)
+        iters_m = [x[0] for x in stats_m]
+        err = {}
+        fl = grid["kind"] == 0
+        for n in ("u", "v", "p"):
+            a, b = simm.download(n), fp64_fields[n]
+            if n == "p":  # pressure is defined up to a constant: fluid cells, mean removed
+                a, b = a[fl] - a[fl].mean(), b[fl] - b[fl].mean()
+            err[n] = {"rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
+                      "max_abs": float(np.abs(a - b).max())}
+        sw0 = torch.cuda.Event(enable_timing=True)
+        sw1 = torch.cuda.Event(enable_timing=True)
+        simm.synchronize()
+        sw0.record(stream_m)
+        simm.sor_sweeps(nsweep, wait=False)
+        sw1.record(stream_m)
+        simm.synchronize()
+        t_sw = sw0.elapsed_time(sw1) / 1e3 / nsweep
+        sw_bytes = 13.0 * interior  # read e, s (8) + flags (1), write e (4)
+        m_inner = min(args.inner_sweeps, PARAMS["max_iterations"])
+        mixed = {
+            "value": CELLS * args.steps * world / (ms_m / 1e3), "unit": "cell-updates/s",
+            "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m,
+            "inner_sweeps": m_inner,
+            "sor_iterations": {"mean": statistics.mean(iters_m), "min": min(iters_m),
+                               "max": max(iters_m), "warmup": [w[0] for w in warm_m]},
+            "error_vs_fp64_after_steps": {"steps": args.warmup + args.steps, **err},
+            "roofline_fp32_sweep": {"achieved": sw_bytes / t_sw / 1e9, "peak": peak,
+                                    "unit": "GB/s", "frac": sw_bytes / t_sw / 1e9 / peak,
+                                    "ms_per_sweep": t_sw * 1e3,
+                                    "algorithmic_bytes": sw_bytes},
+            "dtype": "f32 sweeps, f64 norm/refinement/dt",
+        }
+        simm.close()
 
     # ---- e2e: public API with host buffers, copies inside the timed region ----
     pin = {n: torch.empty((IMAX + 2, JMAX + 2), dtype=torch.float64, pin_memory=True)
@@ -327,6 +383,7 @@ def main():
                  "dgemm_tflops_measured": fp64_peak,
                  "note": "FP64 pipe operations (add, mul, fma each 1) of the solve"},
         "e2e": e2e,
+        "mixed_precision": mixed,
         "clocks": clocks.summary(),
         "gpu_launches": launches,
     }

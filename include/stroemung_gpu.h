@@ -159,6 +159,22 @@ int strm_set_mode(strm_sim *sim, const strm_mode *mode);
  * launch and one 64-byte device-to-host read. */
 int strm_tick(strm_sim *sim, uint32_t *sor_iterations, double *norm_squared);
 
+/* run_simulation_tick in two halves, so that a predictor can replace the
+ * pressure the solve starts from: strm_tick_prepare does the time step,
+ * boundary pass, F/G and RHS; strm_tick_solve the pressure solve, the
+ * velocity update and the time bookkeeping, returning what strm_tick does. */
+int strm_tick_prepare(strm_sim *sim);
+int strm_tick_solve(strm_sim *sim, uint32_t *sor_iterations, double *norm_squared);
+
+/* Device-side plumbing for a pressure predictor: dense [nx][ny] FP32 copies
+ * of RHS and pressure and the flag bytes (kind | edge << 3) into device
+ * buffers (any may be NULL); p += scale * q on fluid interior cells (q a
+ * device FP32 [nx-2][ny-2] array); and device-to-device copies of a whole
+ * FP64 field to (to_sim = 0) or from (to_sim = 1) a dense [nx][ny] buffer. */
+int strm_export_planes(strm_sim *sim, float *rhs, float *p, uint8_t *flags);
+int strm_apply_correction(strm_sim *sim, const float *q, double scale);
+int strm_copy_field_device(strm_sim *sim, int field, double *dense, int to_sim);
+
 /* n ticks back to back with a single host synchronisation; stats[n] (may be
  * NULL) receives each tick's results. */
 int strm_step_n(strm_sim *sim, int n, strm_step_stats *stats);
@@ -195,8 +211,11 @@ int strm_calculate_speed_range(strm_sim *sim);     /* src/grid/mod.rs:253-268 */
 /* n red-black pressure iterations of the loop body of solve_sor
  * (src/simulation.rs:250-277: boundary pressure copy, sweep, residual norm)
  * with no stop test, on the current pressure and RHS, in the selected
- * arithmetic.  Asynchronous when norm_squared is NULL (see strm_synchronize);
- * otherwise waits and returns the last iteration's norm. */
+ * arithmetic.  In STRM_PREC_MIXED it runs n FP32 red-black sweeps of the
+ * correction equation on the current defect instead (the inner iteration of
+ * the mixed solve; norm_squared then returns the last stored norm).
+ * Asynchronous when norm_squared is NULL (see strm_synchronize); otherwise
+ * waits and returns the last iteration's norm. */
 int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
 
 /* Residual norm that allocates nothing.  No counterpart in the reference.

@@ -70,8 +70,11 @@ class DeviceView(ctypes.Structure):
 _vp = ctypes.c_void_p
 _dp = ctypes.POINTER(ctypes.c_double)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
+_u8d = ctypes.c_void_p
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
+_fp = ctypes.c_void_p  # device float pointers are passed as plain addresses
+_i = ctypes.c_int
 SIGNATURES = {
     "strm_create": [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp,
                     ctypes.POINTER(_vp), _i64p],
@@ -93,6 +96,11 @@ SIGNATURES = {
     "strm_calculate_speed_range": [_vp],
     "strm_device_view_get": [_vp, ctypes.POINTER(DeviceView)],
     "strm_sor_sweeps": [_vp, ctypes.c_int, _dp],
+    "strm_tick_prepare": [_vp],
+    "strm_tick_solve": [_vp, ctypes.POINTER(ctypes.c_uint32), _dp],
+    "strm_export_planes": [_vp, _vp, _vp, _vp],
+    "strm_apply_correction": [_vp, _vp, ctypes.c_double],
+    "strm_copy_field_device": [_vp, ctypes.c_int, _vp, ctypes.c_int],
     "strm_render_rgba": [_vp, ctypes.c_int, _u8p],
     "strm_synchronize": [_vp],
     "strm_norm_squared_noalloc": [_dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -100,6 +108,28 @@ SIGNATURES = {
     "strm_host_classify": [ctypes.c_int, ctypes.c_int, _u8p, _u8p, _dp, _i64p],
     "strm_host_boundary_pass": [ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp, _dp],
     "strm_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+    # include/stroemung_nn.h
+    "strm_nn_gemm_bf16": [_vp, _vp, _fp, _i, _i, _i, _vp],
+    "strm_nn_conv3x3": [_vp, _i, _i, _vp, _i, _fp, _vp, _fp, _i, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_conv3x3_wgrad": [_vp, _i, _i, _i, _vp, _i, _vp, _i, _fp, _i, _i, _i, _i, _vp],
+    "strm_nn_avgpool": [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_avgpool_bwd": [_vp, _i, _vp, _i, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_upsample": [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_upsample_bwd": [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_relu_mask": [_vp, _i, _vp, _i, _vp, _i, ctypes.c_longlong, _i, _vp],
+    "strm_nn_bias_grad": [_vp, _i, _vp, _i, _fp, ctypes.c_longlong, _i, _vp],
+    "strm_nn_flip_weights": [_vp, _i, _i, _i, _vp, _i, _i, _vp],
+    "strm_nn_head": [_vp, _i, _i, _fp, _fp, _fp, ctypes.c_longlong, _vp],
+    "strm_nn_zero": [_vp, ctypes.c_longlong, _vp],
+    "strm_nn_head_bwd": [_vp, _i, _i, _fp, _fp, _vp, _i, _fp, _fp, ctypes.c_longlong, _vp],
+    "strm_nn_prepare_input": [_fp, _u8d, _fp, _fp, _fp, _fp, ctypes.c_float, _vp, _i, _i, _i,
+                              _vp],
+    "strm_nn_residual_loss": [_fp, _fp, _u8d, _fp, _fp, ctypes.c_float, ctypes.c_float,
+                              ctypes.c_float, _fp, _fp, _fp, _fp, _i, _i, _i, _vp],
+    "strm_nn_residual_loss_grad": [_fp, _u8d, _fp, _fp, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_float, _fp, _fp, _i, _i, _i, _vp],
+    "strm_nn_adam": [_fp, _fp, _fp, _fp, ctypes.c_longlong, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, ctypes.c_float, _i, _vp, _vp],
     "strm_abi_version": [],
 }
 

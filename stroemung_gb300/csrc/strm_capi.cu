@@ -63,6 +63,8 @@ struct strm_sim {
   std::vector<uint8_t> edge;   // dense edge codes (from the device classification)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph_pre = nullptr, graph_post = nullptr;
+  cudaGraphExec_t exec_pre = nullptr, exec_post = nullptr;
   StepState *h_st = nullptr;   // pinned
   StepLog *h_log = nullptr;    // pinned
   int bc_cap = 0, pcopy_cap = 0;
@@ -124,14 +126,26 @@ void update_cfg(strm_sim *s) {
   r.eager = s->mode.execution == STRM_EXEC_EAGER ? 1 : 0;
 }
 
+void destroy_graphs(strm_sim *s) {
+  cudaGraphExec_t *ex[3] = {&s->exec, &s->exec_pre, &s->exec_post};
+  cudaGraph_t *gr[3] = {&s->graph, &s->graph_pre, &s->graph_post};
+  for (int i = 0; i < 3; ++i) {
+    if (*ex[i]) cudaGraphExecDestroy(*ex[i]);
+    if (*gr[i]) cudaGraphDestroy(*gr[i]);
+    *ex[i] = nullptr;
+    *gr[i] = nullptr;
+  }
+}
+
 int rebuild_graph(strm_sim *s) {
-  if (s->exec) cudaGraphExecDestroy(s->exec);
-  if (s->graph) cudaGraphDestroy(s->graph);
-  s->exec = nullptr;
-  s->graph = nullptr;
+  destroy_graphs(s);
   update_cfg(s);
-  CK(build_step_graph(s->d, s->cfg, &s->graph));
+  CK(build_step_graph(s->d, s->cfg, &s->graph, 0));
   CK(cudaGraphInstantiate(&s->exec, s->graph, 0));
+  CK(build_step_graph(s->d, s->cfg, &s->graph_pre, 1));
+  CK(cudaGraphInstantiate(&s->exec_pre, s->graph_pre, 0));
+  CK(build_step_graph(s->d, s->cfg, &s->graph_post, 2));
+  CK(cudaGraphInstantiate(&s->exec_post, s->graph_post, 0));
   return STRM_OK;
 }
 
@@ -200,8 +214,7 @@ int classify_and_compile(strm_sim *s, long long *bad_out) {
 
 void free_sim(strm_sim *s) {
   if (!s) return;
-  if (s->exec) cudaGraphExecDestroy(s->exec);
-  if (s->graph) cudaGraphDestroy(s->graph);
+  destroy_graphs(s);
   if (s->arena) cudaFree(s->arena);
   if (s->d.bc) cudaFree(s->d.bc);
   if (s->d.bc_val) cudaFree(s->d.bc_val);
@@ -600,6 +613,59 @@ int strm_calculate_norm_squared(strm_sim *s, double *norm_squared) {
   int rc = sync_state(s);
   if (rc) return rc;
   *norm_squared = s->h_st->aux;
+  return STRM_OK;
+}
+
+int strm_tick_prepare(strm_sim *s) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(cudaGraphLaunch(s->exec_pre, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_tick_solve(strm_sim *s, uint32_t *sor_iterations, double *norm_squared) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(cudaGraphLaunch(s->exec_post, s->stream));
+  int rc = sync_state(s);
+  if (rc) return rc;
+  if (sor_iterations) *sor_iterations = s->h_st->sor_iters;
+  if (norm_squared) *norm_squared = s->h_st->ns;
+  if (s->h_st->overrun) return fail(STRM_ERR_TIMEOUT, "pressure loop passed its bound");
+  if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return STRM_OK;
+}
+
+int strm_export_planes(strm_sim *s, float *rhs, float *p, uint8_t *flags) {
+  if (!s) return fail(STRM_ERR_INVALID, "sim is NULL");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_export(s->d, s->g, rhs, p, flags, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_apply_correction(strm_sim *s, const float *q, double scale) {
+  if (!s || !q) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  CK(launch_apply_correction(s->d, s->g, q, scale, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return STRM_OK;
+}
+
+int strm_copy_field_device(strm_sim *s, int field, double *dense, int to_sim) {
+  if (!s || !dense) return fail(STRM_ERR_INVALID, "invalid arguments");
+  double *f = field_ptr(s, field);
+  if (!f) return fail(STRM_ERR_INVALID, "unknown field %d", field);
+  CK(cudaSetDevice(s->dev));
+  const Geom &g = s->g;
+  if (to_sim)
+    CK(cudaMemcpy2DAsync(f, (size_t)g.pitch * 8, dense, (size_t)g.ny * 8, (size_t)g.ny * 8, g.nx,
+                         cudaMemcpyDeviceToDevice, s->stream));
+  else
+    CK(cudaMemcpy2DAsync(dense, (size_t)g.ny * 8, f, (size_t)g.pitch * 8, (size_t)g.ny * 8, g.nx,
+                         cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   return STRM_OK;
 }
 

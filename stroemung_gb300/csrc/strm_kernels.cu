@@ -682,16 +682,22 @@ __global__ void __launch_bounds__(256)
 // Mixed-precision pressure solve: FP32 red-black sweeps on the FP64 defect,
 // FP64 norm and FP64 accumulation of the correction (iterative refinement).
 //
-//   start:  e = 0; boundary copy of p; s = (float)(middle * residual(p))
-//   repeat: m x [red sweep + red boundary copy, black sweep + black boundary
-//           copy] on  Lap(e) = rhs - Lap(p)  in FP32;
-//           p += e on fluid cells, e = 0; boundary copy of p;
+//   start:  e = 0 on fluid cells; on boundary cells e = delta = copy(p) - p
+//   repeat: m x [red sweep, black sweep] on the correction e in FP32;
+//           p += e (fluid and boundary cells), e = 0; delta, e_b = delta;
 //           FP64 norm of residual(p) -> stop rule; s = (float)(middle * r)
 //
-// The boundary copy of the correction is folded into the sweeps: a red
-// boundary cell takes its black fluid neighbours' values, which the red sweep
+// Boundary values follow the reference exactly.  Before every sweep the
+// reference copies the fluid pressure to the boundary cells, so a boundary
+// value is one sweep stale when the norm is taken and when the solve ends
+// (quirk Q2).  Here p = p0 + e, and the copy rule for p becomes
+// e_b = delta_b + copy(e) with delta_b = copy(p0) - p0_b fixed for the outer
+// iteration (stored in s at boundary cells).  The copy is folded into the
+// sweeps: a red boundary cell takes black fluid values, which the red sweep
 // does not change; a black boundary cell takes red values, final once the red
-// sweep is done.  So one sweep kernel per colour and no copy launches.
+// sweep is done.  The last black sweep of an outer iteration skips its copy,
+// so after p += e every boundary value is the one copied before the last
+// sweep — the reference's stale value — and the norm is the reference's.
 // ------------------------------------------------------------------------
 
 struct Consts32 {
@@ -713,10 +719,12 @@ __device__ __forceinline__ float copy32(const float *e, size_t o, int pitch, int
 }
 
 // One colour over the whole grid: fluid interior cells of the colour get the
-// SOR update, boundary cells of the colour with an edge get the copy.
+// SOR update, boundary cells of the colour with an edge get the copy (when
+// copy_boundary is set).
 __global__ void __launch_bounds__(256)
     sor32_color_kernel(float *__restrict__ e, const float *__restrict__ s,
-                       const uint8_t *__restrict__ flags, Geom g, Consts32 k, int color) {
+                       const uint8_t *__restrict__ flags, Geom g, Consts32 k, int color,
+                       int copy_boundary) {
   const int x = blockIdx.y * blockDim.y + threadIdx.y;
   const int y = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((x + color) & 1);
   if (x >= g.nx || y >= g.ny) return;
@@ -727,12 +735,13 @@ __global__ void __launch_bounds__(256)
     const float sum_x = e[o - g.pitch] + e[o + g.pitch];
     const float sum_y = e[o - 1] + e[o + 1];
     e[o] = fmaf(k.omw, e[o], fmaf(k.a, sum_x, fmaf(k.b, sum_y, s[o])));
-  } else if (edge_of(fl) != E_NONE) {
-    e[o] = copy32(e, o, g.pitch, edge_of(fl));
+  } else if (copy_boundary && edge_of(fl) != E_NONE) {
+    e[o] = s[o] + copy32(e, o, g.pitch, edge_of(fl));
   }
 }
 
-// p += e on fluid interior cells (apply != 0), then e = 0 everywhere.
+// p += e on fluid interior cells and boundary cells with an edge (apply != 0),
+// then e = 0 everywhere.
 __global__ void __launch_bounds__(256)
     refine_kernel(double *__restrict__ p, float *__restrict__ e, const uint8_t *__restrict__ flags,
                   Geom g, int apply) {
@@ -744,10 +753,36 @@ __global__ void __launch_bounds__(256)
     const int y = y0 + q;
     if (y >= g.ny) break;
     const size_t o = OFF(x, y);
-    if (apply && flags[o] == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2)
+    const uint8_t fl = flags[o];
+    const bool fluid_in = fl == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+    if (apply && (fluid_in || (is_bnd(fl) && edge_of(fl) != E_NONE)))
       p[o] = p[o] + (double)e[o];
     e[o] = 0.0f;
   }
+}
+
+// delta_b = copy(p) - p_b on boundary cells with an edge (FP64, stored FP32
+// in s and as the starting correction e_b).
+__global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s,
+                             float *__restrict__ e, const PCopy *__restrict__ pc, int n,
+                             int pitch) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long long o = pc[k].off;
+  double c;
+  switch (pc[k].edge) {
+    case E_N: c = p[o - 1]; break;
+    case E_NE: c = (p[o - 1] + p[o + pitch]) * 0.5; break;
+    case E_E: c = p[o + pitch]; break;
+    case E_SE: c = (p[o + 1] + p[o + pitch]) * 0.5; break;
+    case E_S: c = p[o + 1]; break;
+    case E_SW: c = (p[o + 1] + p[o - pitch]) * 0.5; break;
+    case E_W: c = p[o - pitch]; break;
+    default: c = (p[o - 1] + p[o - pitch]) * 0.5; break;
+  }
+  const float d = (float)(c - p[o]);
+  s[o] = d;
+  e[o] = d;
 }
 
 // FP64 norm of the residual on every interior cell (the reference's norm),
@@ -872,6 +907,49 @@ cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, voi
 }
 
 // ------------------------------------------------------------------------
+// Warm-start plumbing: dense FP32 copies of RHS / pressure and the flags for
+// a predictor, and the application of a predicted FP32 correction to the
+// FP64 pressure on fluid interior cells.
+// ------------------------------------------------------------------------
+
+__global__ void export_kernel(const double *__restrict__ rhs, const double *__restrict__ p,
+                              const uint8_t *__restrict__ flags, Geom g, float *rhs32,
+                              float *p32, uint8_t *fl8) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.y;
+  if (y >= g.ny) return;
+  const size_t o = OFF(x, y), dn = (size_t)x * g.ny + y;
+  if (rhs32) rhs32[dn] = (float)rhs[o];
+  if (p32) p32[dn] = (float)p[o];
+  if (fl8) fl8[dn] = flags[o];
+}
+
+__global__ void apply_correction_kernel(double *__restrict__ p, const uint8_t *__restrict__ flags,
+                                        Geom g, const float *__restrict__ q, double scale) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.y + 1;
+  if (y < 1 || y > g.ny - 2 || x > g.nx - 2) return;
+  const size_t o = OFF(x, y);
+  if (flags[o] != 0) return;
+  p[o] = p[o] + scale * (double)q[(size_t)(x - 1) * (g.ny - 2) + (y - 1)];
+}
+
+cudaError_t launch_export(const DevFields &d, const Geom &g, float *rhs32, float *p32,
+                          uint8_t *fl8, cudaStream_t s) {
+  export_kernel<<<dim3((g.ny + 127) / 128, g.nx), 128, 0, s>>>(d.rhs, d.p, d.flags, g, rhs32,
+                                                               p32, fl8);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_correction(const DevFields &d, const Geom &g, const float *q,
+                                    double scale, cudaStream_t s) {
+  if (g.nx < 3 || g.ny < 3) return cudaSuccess;
+  apply_correction_kernel<<<dim3((g.ny + 127) / 128, g.nx - 2), 128, 0, s>>>(d.p, d.flags, g, q,
+                                                                             scale);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------
 
@@ -989,6 +1067,19 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
   int ty, nt;
   tiles_of(r.g, 1, &ty, &nt);
   if (nt == 0) return cudaSuccess;
+  if (r.precision == 1) {
+    // one FP32 red-black sweep of the correction equation on the current
+    // defect (the inner iteration of the mixed-precision solve)
+    Consts32 k32;
+    k32.omw = (float)r.c.one_minus_w;
+    k32.a = (float)(r.c.middle * r.c.r_dx2);
+    k32.b = (float)(r.c.middle * r.c.r_dy2);
+    dim3 pgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (r.g.nx + kRedBlock.y - 1) / kRedBlock.y);
+    for (int color = 0; color < 2; ++color)
+      sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, r.g, k32, color, 1);
+    return cudaGetLastError();
+  }
   cudaError_t e = launch_pcopy(d, r.g, s);
   if (e != cudaSuccess) return e;
   dim3 sgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
@@ -1009,6 +1100,12 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
                                                           d.partials, ty, nt, 0, r.itermax,
                                                           r.strict_eps, RES_NORM);
   return cudaGetLastError();
+}
+
+static void launch_delta(const DevFields &d, const Geom &g, cudaStream_t s) {
+  if (d.n_pcopy > 0)
+    delta_kernel<<<(d.n_pcopy + 255) / 256, 256, 0, s>>>(d.p, d.r32, d.e32, d.pcopy, d.n_pcopy,
+                                                        g.pitch);
 }
 
 cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s) {
@@ -1055,16 +1152,17 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx + kRedBlock.y - 1) / kRedBlock.y);
     refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 0);
-    if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+    launch_delta(d, g, s);
     mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
                                                           d.partials, ty_int, nt_int, 0,
                                                           r.itermax, r.strict_eps, m, 0);
     while (!done) {
       for (int i = 0; i < m; ++i)
         for (int color = 0; color < 2; ++color)
-          sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color);
+          sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color,
+                                                         (color == 0 || i < m - 1) ? 1 : 0);
       refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 1);
-      if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+      launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
                                                             r.itermax, r.strict_eps, m, 1);
@@ -1139,7 +1237,7 @@ struct GraphBuilder {
 
 }  // namespace
 
-cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out) {
+cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out, int part) {
   GraphBuilder b;
   cudaError_t e = cudaGraphCreate(&b.graph, 0);
   if (e != cudaSuccess) return e;
@@ -1151,15 +1249,19 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
   tiles_of(g, 1, &ty_int, &nt_int);
   const int nb = residual_blocks(g);
 
-  cudaGraphNode_t n = b.kernel(b.graph, nullptr, (const void *)bc_kernel, dim3(BC_CLUSTER),
-                               dim3(BC_THREADS), d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc,
-                               d.bc_val, d.n_bc, d.st, c, r.tau, r.delt, r.itermax, 1);
-  dim3 fg_grid((g.ny + FG_TY - 1) / FG_TY, (g.nx + FG_TX - 1) / FG_TX);
-  n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
-               (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
-               (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
-
-  if (r.sor_order == 1) {
+  cudaGraphNode_t n = nullptr;
+  if (part != 2) {
+    n = b.kernel(b.graph, nullptr, (const void *)bc_kernel, dim3(BC_CLUSTER), dim3(BC_THREADS),
+                 d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc, d.bc_val, d.n_bc, d.st, c, r.tau,
+                 r.delt, r.itermax, 1);
+    dim3 fg_grid((g.ny + FG_TY - 1) / FG_TY, (g.nx + FG_TX - 1) / FG_TX);
+    n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
+                 (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
+                 (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
+  }
+  if (part == 1) {
+    // the first half of a step ends after the RHS
+  } else if (r.sor_order == 1) {
     n = b.kernel(b.graph, n, (const void *)sor_lex_kernel, dim3(1), dim3(1024), d.p,
                  (const double *)d.rhs, (const uint8_t *)d.flags, (const PCopy *)d.pcopy,
                  d.n_pcopy, g, c, d.st, d.pw, r.itermax, r.strict_eps);
@@ -1177,8 +1279,9 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
                  (const uint8_t *)d.flags, g, 0);
     if (d.n_pcopy > 0)
-      n = b.kernel(b.graph, n, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
-                   dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+      n = b.kernel(b.graph, n, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
+                   dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
+                   d.n_pcopy, g.pitch);
     n = b.kernel(b.graph, n, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                  (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32, g,
                  c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 0);
@@ -1188,19 +1291,22 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t wnode = nullptr;
-    if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&wnode, b.graph, &n, nullptr, 1, &cp);
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphAddNode(&wnode, b.graph, n ? &n : nullptr, nullptr, n ? 1 : 0, &cp);
     if (b.err == cudaSuccess) {
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
       for (int i = 0; i < m; ++i)
         for (int color = 0; color < 2; ++color)
           bn = b.kernel(body, bn, (const void *)sor32_color_kernel, pgrid, kRedBlock, d.e32,
-                        (const float *)d.r32, (const uint8_t *)d.flags, g, k32, color);
+                        (const float *)d.r32, (const uint8_t *)d.flags, g, k32, color,
+                        (color == 0 || i < m - 1) ? 1 : 0);
       bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
                     (const uint8_t *)d.flags, g, 1);
       if (d.n_pcopy > 0)
-        bn = b.kernel(body, bn, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
-                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+        bn = b.kernel(body, bn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
+                      dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
+                      d.n_pcopy, g.pitch);
       bn = b.kernel(body, bn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                     (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32,
                     g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 1);
@@ -1216,7 +1322,8 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t wnode = nullptr;
-    if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&wnode, b.graph, &n, nullptr, 1, &cp);
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphAddNode(&wnode, b.graph, n ? &n : nullptr, nullptr, n ? 1 : 0, &cp);
     if (b.err == cudaSuccess) {
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
@@ -1238,12 +1345,15 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     }
     n = wnode;
   }
-  n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock, (const double *)d.p,
-               (const uint8_t *)d.flags, g, d.st, d.partials, ty_all, nt_all, 0);
-  n = b.kernel(b.graph, n, (const void *)velocity_kernel, dim3(nb), kRedBlock, d.u, d.v,
-               (const double *)d.f, (const double *)d.g, (const double *)d.p,
-               (const double *)d.ru, (const double *)d.rv, (const uint8_t *)d.flags, g, c, d.st,
-               d.partials, d.log, ty_all, nt_all, 1, 1, 1);
+  if (part != 1) {
+    n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock,
+                 (const double *)d.p, (const uint8_t *)d.flags, g, d.st, d.partials, ty_all,
+                 nt_all, 0);
+    n = b.kernel(b.graph, n, (const void *)velocity_kernel, dim3(nb), kRedBlock, d.u, d.v,
+                 (const double *)d.f, (const double *)d.g, (const double *)d.p,
+                 (const double *)d.ru, (const double *)d.rv, (const uint8_t *)d.flags, g, c,
+                 d.st, d.partials, d.log, ty_all, nt_all, 1, 1, 1);
+  }
   if (b.err != cudaSuccess) {
     cudaGraphDestroy(b.graph);
     return b.err;

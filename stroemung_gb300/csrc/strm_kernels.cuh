@@ -69,7 +69,15 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
 
 // Builds the whole step as one CUDA graph (the pressure loop as a
 // conditional WHILE node for the red-black solve).
-cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out);
+// part 0: the whole step; 1: up to the RHS; 2: from the pressure solve on.
+cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out, int part);
+
+// Dense FP32 copies ([nx][ny]) of RHS and pressure and the flag bytes (any
+// output may be NULL); p += scale*q on fluid interior cells, q [nx-2][ny-2].
+cudaError_t launch_export(const DevFields &d, const Geom &g, float *rhs32, float *p32,
+                          uint8_t *fl8, cudaStream_t s);
+cudaError_t launch_apply_correction(const DevFields &d, const Geom &g, const float *q,
+                                    double scale, cudaStream_t s);
 
 int residual_blocks(const Geom &g);
 

@@ -10,13 +10,15 @@ import pytest
 
 from stroemung_gb300 import _lib, presets
 
-HEADER = Path(__file__).resolve().parent.parent / "include" / "stroemung_gpu.h"
+HEADERS = sorted((Path(__file__).resolve().parent.parent / "include").glob("*.h"))
 
 
 def declared_functions():
-    text = HEADER.read_text()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\bint\s+(strm_\w+)\s*\(", text)))
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\bint\s+(strm_\w+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_the_expected_surface():

@@ -306,19 +306,25 @@ def test_mixed_precision_matches_fp64_on_converged_cavity():
     assert rel_l2(p_fluid(mix.download("p"), g["kind"]), p_fluid(ref.download("p"), g["kind"])) < 1e-6
 
 
-def test_mixed_precision_channel_runs_and_tracks_fp64():
+def test_mixed_precision_channel_tracks_fp64():
+    """Same sweep count in both (every step runs all 512 iterations: the
+    obstacle cells keep the norm above eps): in exact arithmetic the refined
+    solve equals plain SOR, so the difference is FP32 rounding of the
+    corrections plus the fresher boundary pressure at the end of each solve."""
     rects = presets.random_rectangles(256, 64, 6, 1, x_margin=16)
     g = presets.channel(256, 64, rects)
     prm = dict(grid=g, cell_size=(0.04, 0.04), delt=0.01, gamma=0.9, reynolds=400.0,
-               sor_absolute_epsilon=1e-3, max_iterations=512, omega=1.7, tau=0.5)
+               sor_absolute_epsilon=1e-3, max_iterations=512, omega=1.7, tau=0.5,
+               strict_eps=True)
     ref = Simulation(arithmetic=1, **prm)
     mix = Simulation(precision=1, inner_sweeps=16, **prm)
     for _ in range(10):
         i_r, _ = ref.run_simulation_tick()
         i_m, _ = mix.run_simulation_tick()
-        assert i_m <= 512 and i_m % 16 == 0
-    for n in ("u", "v"):
-        assert rel_l2(mix.download(n), ref.download(n)) < 1e-3, n
+        assert i_r == 512 and i_m == 512
+    errs = {n: rel_l2(mix.download(n), ref.download(n)) for n in ("u", "v")}
+    errs["p"] = rel_l2(p_fluid(mix.download("p"), g["kind"]), p_fluid(ref.download("p"), g["kind"]))
+    assert all(e < 1e-3 for e in errs.values()), errs
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
