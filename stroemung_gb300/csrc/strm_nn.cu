@@ -1,0 +1,480 @@
+// Dense contractions of the learned pressure warm start on the tcgen05 tensor
+// cores: BF16 operands staged in 128B-swizzled shared memory, FP32
+// accumulators in TMEM, one elected thread issuing tcgen05.mma.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "../../include/stroemung_nn.h"
+#include "strm_umma.cuh"
+
+namespace strm_nn {
+
+constexpr int GM = 128;  // rows per CTA tile (TMEM lanes)
+constexpr int GN = 128;  // columns per CTA tile (TMEM columns)
+constexpr int GK = 64;   // K per shared-memory stage (one 128-byte swizzle row)
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+// D[M x N] (FP32, row-major) = A[M x K] * B[N x K]^T, A and B BF16 row-major
+// (K contiguous).  M, N multiples of 128, K a multiple of 64.
+__global__ void __launch_bounds__(128)
+    gemm_bf16_kernel(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
+                     float *__restrict__ D, int M, int N, int K, unsigned int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *sA = smem_raw + pad;
+  uint8_t *sB = sA + GM * 128;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * GM, n0 = blockIdx.x * GN;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, GN);
+  if (tid == 0) mbar_init(&mbar, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_bf16_f32(GM, GN);
+
+  uint32_t phase = 0;
+  int ok = 1;
+  for (int k0 = 0; k0 < K && ok; k0 += GK) {
+    for (int c = tid; c < GM * 8; c += 128) {
+      const int r = c >> 3, j = c & 7;
+      const uint4 val = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * K + k0 + j * 8);
+      *reinterpret_cast<uint4 *>(sA + sw128_offset(r, j)) = val;
+    }
+    for (int c = tid; c < GN * 8; c += 128) {
+      const int r = c >> 3, j = c & 7;
+      const uint4 val = *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + r) * K + k0 + j * 8);
+      *reinterpret_cast<uint4 *>(sB + sw128_offset(r, j)) = val;
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint64_t da = desc_kmajor_sw128(smem_u32(sA));
+      const uint64_t db = desc_kmajor_sw128(smem_u32(sB));
+#pragma unroll
+      for (int kk = 0; kk < GK / 16; ++kk)
+        umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
+      umma_commit(&mbar);
+    }
+    ok = __syncthreads_and(mbar_wait_bounded(&mbar, phase, kWaitLimit) ? 1 : 0);
+    phase ^= 1u;
+  }
+  tc_fence_after();
+  if (ok) {
+    float *row = D + (size_t)(m0 + warp * 32 + lane) * N + n0;
+#pragma unroll 1
+    for (int c = 0; c < GN; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; i += 4)
+        *reinterpret_cast<float4 *>(row + c + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, GN);
+}
+
+// ------------------------------------------------------------------------
+// 3x3 "same" convolution as an implicit GEMM.
+//
+// Activations are BF16 NHWC: pixel q = (b*H + y)*W + x at x_ptr + q*cs,
+// channels contiguous (cs >= channels; a concatenation is two channel slices
+// of one buffer).  Input channels are padded to cin_p (a multiple of 8).  The
+// GEMM: M = pixels (128 per CTA), N = output channels (the whole Cout, <=
+// 256, a multiple of 16), K = 9*cin_p in tap-major order (tap t = (dy+1)*3 +
+// (dx+1), then channel), padded to a multiple of 64.  Weights w[co][k] use
+// the same K order, zero-padded.  Each 64-wide K chunk is 8 groups of 8
+// channels of one tap, i.e. eight 16-byte loads per pixel, zero outside the
+// image.  Epilogue: + bias, optional ReLU, BF16 NHWC store.
+// ------------------------------------------------------------------------
+
+struct ConvShape {
+  int batch, h, w;
+  int cin_p;      // padded input channels (multiple of 8)
+  int cs_in;      // input pixel stride (elements)
+  int cout;       // output channels (multiple of 16, <= 256)
+  int cs_out;     // output pixel stride (elements)
+  int kp;         // padded K = roundup(9*cin_p, 64)
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128)
+    conv3x3_fwd_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
+                       const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y,
+                       float *__restrict__ y32, ConvShape s, int relu, unsigned int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  constexpr int TM_COLS = BN < 32 ? 32 : BN;
+  const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *sA = smem_raw + pad;
+  uint8_t *sB = sA + GM * 128;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long npix = (long long)s.batch * s.h * s.w;
+  const long long q0 = (long long)blockIdx.x * GM;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, TM_COLS);
+  if (tid == 0) mbar_init(&mbar, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_bf16_f32(GM, BN);
+
+  uint32_t phase = 0;
+  int ok = 1;
+  const uint4 zero4 = make_uint4(0, 0, 0, 0);
+  for (int k0 = 0; k0 < s.kp && ok; k0 += GK) {
+    for (int c = tid; c < GM * 8; c += 128) {
+      const int r = c >> 3, j = c & 7;
+      const long long q = q0 + r;
+      const int k = k0 + 8 * j;
+      const int tap = k / s.cin_p, ch = k - tap * s.cin_p;
+      uint4 val = zero4;
+      if (q < npix && tap < 9) {
+        const int xx = (int)(q % s.w);
+        const long long t = q / s.w;
+        const int yy = (int)(t % s.h);
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const int sy = yy + dy, sx = xx + dx;
+        if (sy >= 0 && sy < s.h && sx >= 0 && sx < s.w)
+          val = *reinterpret_cast<const uint4 *>(x + (q + (long long)dy * s.w + dx) * s.cs_in + ch);
+      }
+      *reinterpret_cast<uint4 *>(sA + sw128_offset(r, j)) = val;
+    }
+    for (int c = tid; c < BN * 8; c += 128) {
+      const int r = c >> 3, j = c & 7;
+      *reinterpret_cast<uint4 *>(sB + sw128_offset(r, j)) =
+          *reinterpret_cast<const uint4 *>(w + (size_t)r * s.kp + k0 + j * 8);
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint64_t da = desc_kmajor_sw128(smem_u32(sA));
+      const uint64_t db = desc_kmajor_sw128(smem_u32(sB));
+#pragma unroll
+      for (int kk = 0; kk < GK / 16; ++kk)
+        umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
+      umma_commit(&mbar);
+    }
+    ok = __syncthreads_and(mbar_wait_bounded(&mbar, phase, kWaitLimit) ? 1 : 0);
+    phase ^= 1u;
+  }
+  tc_fence_after();
+  if (ok) {
+    const long long q = q0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (q < npix) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          v[i] += bias ? bias[c + i] : 0.0f;
+          if (relu) v[i] = fmaxf(v[i], 0.0f);
+        }
+        if (y32) {
+          float *dst = y32 + q * s.cs_out + c;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dst[i] = v[i];
+        } else {
+          __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
+          uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
+          dst[0] = reinterpret_cast<const uint4 *>(o)[0];
+          dst[1] = reinterpret_cast<const uint4 *>(o)[1];
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, TM_COLS);
+}
+
+// ------------------------------------------------------------------------
+// Weight gradient of the 3x3 convolution: dW[co][k] += sum over pixels q of
+// g[q][co] * im2col(x)[q][k], with g = dY masked by the ReLU (y > 0) when y
+// is given.  GEMM with M = K rows (128 per CTA), N = Cout, reduction over
+// pixels (64 per stage, `qchunk` pixels per CTA, partial sums added
+// atomically in FP32).  Both operands are gathered transposed into the
+// K-major swizzled tiles (the reduction index, pixels, along the 128-byte rows).
+// ------------------------------------------------------------------------
+
+template <int BN>
+__global__ void __launch_bounds__(128)
+    conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ dy,
+                         const __nv_bfloat16 *__restrict__ yact, float *__restrict__ dw,
+                         ConvShape s, int cs_dy, int qchunk, unsigned int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  constexpr int TM_COLS = BN < 32 ? 32 : BN;
+  const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *sA = smem_raw + pad;
+  uint8_t *sB = sA + GM * 128;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long npix = (long long)s.batch * s.h * s.w;
+  const int k_base = blockIdx.x * GM;               // rows of dW^T
+  const long long q_begin = (long long)blockIdx.y * qchunk;
+  const long long q_end = q_begin + qchunk < npix ? q_begin + qchunk : npix;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, TM_COLS);
+  if (tid == 0) mbar_init(&mbar, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_bf16_f32(GM, BN);
+  __nv_bfloat16 *tA = reinterpret_cast<__nv_bfloat16 *>(sA);
+  __nv_bfloat16 *tB = reinterpret_cast<__nv_bfloat16 *>(sB);
+  const __nv_bfloat16 bzero = __float2bfloat16_rn(0.0f);
+
+  uint32_t phase = 0;
+  int ok = 1;
+  bool first = true;
+  for (long long qs = q_begin; qs < q_end && ok; qs += GK) {
+    // A: 128 K-rows (tap, channel groups of 8) x 64 pixels
+    for (int c = tid; c < (GM / 8) * GK; c += 128) {
+      const int kg = c / GK, qi = c % GK;  // channel group within the tile, pixel
+      const int k = k_base + 8 * kg;
+      const long long q = qs + qi;
+      const int tap = k / s.cin_p, ch = k - tap * s.cin_p;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (q < q_end && tap < 9 && k < s.kp) {
+        const int xx = (int)(q % s.w);
+        const int yy = (int)((q / s.w) % s.h);
+        const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+        if (yy + ddy >= 0 && yy + ddy < s.h && xx + ddx >= 0 && xx + ddx < s.w)
+          val = *reinterpret_cast<const uint4 *>(x + (q + (long long)ddy * s.w + ddx) * s.cs_in + ch);
+      }
+      const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&val);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = 8 * kg + i;
+        tA[(sw128_offset(r, qi >> 3) >> 1) + (qi & 7)] = e[i];
+      }
+    }
+    // B: Cout rows x 64 pixels of the (masked) output gradient
+    for (int c = tid; c < (BN / 8) * GK; c += 128) {
+      const int cg = c / GK, qi = c % GK;
+      const long long q = qs + qi;
+      __align__(16) __nv_bfloat16 e[8];
+      if (q < q_end) {
+        *reinterpret_cast<uint4 *>(e) = *reinterpret_cast<const uint4 *>(dy + q * cs_dy + 8 * cg);
+        if (yact) {
+          __align__(16) __nv_bfloat16 a[8];
+          *reinterpret_cast<uint4 *>(a) =
+              *reinterpret_cast<const uint4 *>(yact + q * s.cs_out + 8 * cg);
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!(__bfloat162float(a[i]) > 0.0f)) e[i] = bzero;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) e[i] = bzero;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = 8 * cg + i;
+        tB[(sw128_offset(r, qi >> 3) >> 1) + (qi & 7)] = e[i];
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint64_t da = desc_kmajor_sw128(smem_u32(sA));
+      const uint64_t db = desc_kmajor_sw128(smem_u32(sB));
+#pragma unroll
+      for (int kk = 0; kk < GK / 16; ++kk)
+        umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (!first || kk > 0) ? 1u : 0u);
+      umma_commit(&mbar);
+    }
+    first = false;
+    ok = __syncthreads_and(mbar_wait_bounded(&mbar, phase, kWaitLimit) ? 1 : 0);
+    phase ^= 1u;
+  }
+  tc_fence_after();
+  if (ok && !first) {
+    const int k = k_base + warp * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (k < s.kp) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) atomicAdd(dw + (size_t)(c + i) * s.kp + k, v[i]);
+      }
+    }
+  } else if (!ok && tid == 0) {
+    atomicExch(err, 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, TM_COLS);
+}
+
+namespace {
+std::mutex g_mu;
+unsigned int *g_err[64] = {};
+
+cudaError_t error_flag(unsigned int **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_err[dev]) {
+    e = cudaMalloc(&g_err[dev], sizeof(unsigned int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(g_err[dev], 0, sizeof(unsigned int));
+    if (e != cudaSuccess) return e;
+  }
+  *out = g_err[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+}  // namespace strm_nn
+
+using namespace strm_nn;
+
+extern "C" int strm_nn_gemm_bf16(const void *a, const void *b, float *d, int m, int n, int k,
+                                 void *stream) {
+  if (!a || !b || !d || m <= 0 || n <= 0 || k <= 0 || m % GM || n % GN || k % GK)
+    return STRM_NN_ERR_INVALID;
+  unsigned int *err = nullptr;
+  if (error_flag(&err) != cudaSuccess) return STRM_NN_ERR_CUDA;
+  const int smem = 2 * GM * 128 + 1024;
+  cudaStream_t s = (cudaStream_t)stream;
+  gemm_bf16_kernel<<<dim3(n / GN, m / GM), 128, smem, s>>>(
+      (const __nv_bfloat16 *)a, (const __nv_bfloat16 *)b, d, m, n, k, err);
+  if (cudaGetLastError() != cudaSuccess) return STRM_NN_ERR_CUDA;
+  unsigned int h = 0;
+  if (cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return STRM_NN_ERR_CUDA;
+  return h ? STRM_NN_ERR_TIMEOUT : STRM_NN_OK;
+}
+
+namespace {
+
+template <int BN>
+int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, const float *bias,
+                void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
+                cudaStream_t s, unsigned int *err) {
+  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
+  const int smem = GM * 128 + BN * 128 + 1024;
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(conv3x3_fwd_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+      return STRM_NN_ERR_CUDA;
+    configured = true;
+  }
+  const long long npix = (long long)batch * h * width;
+  const unsigned int grid = (unsigned int)((npix + GM - 1) / GM);
+  conv3x3_fwd_kernel<BN><<<grid, 128, smem, s>>>((const __nv_bfloat16 *)x,
+                                                 (const __nv_bfloat16 *)w, bias,
+                                                 (__nv_bfloat16 *)y, y32, sh, relu, err);
+  return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
+}
+
+template <int BN>
+int launch_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy, int cs_dy,
+                 const void *yact, int cs_out, float *dw, int batch, int h, int width,
+                 cudaStream_t s, unsigned int *err) {
+  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
+  const int smem = GM * 128 + BN * 128 + 1024;
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(conv3x3_wgrad_kernel<BN>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return STRM_NN_ERR_CUDA;
+    configured = true;
+  }
+  const long long npix = (long long)batch * h * width;
+  // split the pixel reduction so that the grid fills the GPU
+  const int mtiles = (kp + GM - 1) / GM;
+  long long want = (152LL * 4 + mtiles - 1) / mtiles;
+  long long qchunk = (npix + want - 1) / want;
+  qchunk = (qchunk + GK - 1) / GK * GK;
+  if (qchunk < GK) qchunk = GK;
+  const unsigned int ysplit = (unsigned int)((npix + qchunk - 1) / qchunk);
+  conv3x3_wgrad_kernel<BN><<<dim3(mtiles, ysplit), 128, smem, s>>>(
+      (const __nv_bfloat16 *)x, (const __nv_bfloat16 *)dy, (const __nv_bfloat16 *)yact, dw, sh,
+      cs_dy, (int)qchunk, err);
+  return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
+}
+
+int finish(unsigned int *err, cudaStream_t s, int rc) {
+  if (rc != STRM_NN_OK) return rc;
+  unsigned int h = 0;
+  if (cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return STRM_NN_ERR_CUDA;
+  return h ? STRM_NN_ERR_TIMEOUT : STRM_NN_OK;
+}
+
+bool conv_args_ok(int cs_in, int cin_p, int kp, int cs_out, int cout) {
+  return cin_p > 0 && cin_p % 8 == 0 && cs_in % 8 == 0 && cs_in >= cin_p &&
+         kp % GK == 0 && kp >= 9 * cin_p && cs_out % 8 == 0 && cs_out >= cout &&
+         (cout == 16 || cout == 32 || cout == 64 || cout == 128 || cout == 256);
+}
+
+}  // namespace
+
+extern "C" int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *w, int kp,
+                               const float *bias, void *y, float *y32, int cs_out, int cout,
+                               int batch, int h, int width, int relu, void *stream) {
+  if (!x || !w || (!y && !y32) || batch < 1 || h < 1 || width < 1 ||
+      !conv_args_ok(cs_in, cin_p, kp, cs_out, cout))
+    return STRM_NN_ERR_INVALID;
+  unsigned int *err = nullptr;
+  if (error_flag(&err) != cudaSuccess) return STRM_NN_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  switch (cout) {
+    case 16: rc = launch_conv<16>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 32: rc = launch_conv<32>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 64: rc = launch_conv<64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 128: rc = launch_conv<128>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    default: rc = launch_conv<256>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+  }
+  return finish(err, s, rc);
+}
+
+extern "C" int strm_nn_conv3x3_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy,
+                                     int cs_dy, const void *yact, int cs_out, float *dw,
+                                     int cout, int batch, int h, int width, void *stream) {
+  if (!x || !dy || !dw || batch < 1 || h < 1 || width < 1 || cs_dy % 8 ||
+      !conv_args_ok(cs_in, cin_p, kp, cs_out, cout))
+    return STRM_NN_ERR_INVALID;
+  unsigned int *err = nullptr;
+  if (error_flag(&err) != cudaSuccess) return STRM_NN_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  switch (cout) {
+    case 16: rc = launch_wgrad<16>(x, cs_in, cin_p, kp, dy, cs_dy, yact, cs_out, dw, batch, h, width, s, err); break;
+    case 32: rc = launch_wgrad<32>(x, cs_in, cin_p, kp, dy, cs_dy, yact, cs_out, dw, batch, h, width, s, err); break;
+    case 64: rc = launch_wgrad<64>(x, cs_in, cin_p, kp, dy, cs_dy, yact, cs_out, dw, batch, h, width, s, err); break;
+    case 128: rc = launch_wgrad<128>(x, cs_in, cin_p, kp, dy, cs_dy, yact, cs_out, dw, batch, h, width, s, err); break;
+    default: rc = launch_wgrad<256>(x, cs_in, cin_p, kp, dy, cs_dy, yact, cs_out, dw, batch, h, width, s, err); break;
+  }
+  return finish(err, s, rc);
+}

@@ -1,0 +1,128 @@
+"""tcgen05 BF16 contractions of the learned warm start against torch (FP32
+reference of the same products)."""
+import ctypes
+
+import pytest
+
+from stroemung_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (256, 128, 256), (384, 256, 576)])
+def test_gemm_bf16_matches_torch(m, n, k):
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(m + n + k)
+    a = torch.randn(m, k, device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn(n, k, device="cuda", generator=g).to(torch.bfloat16)
+    d = torch.empty(m, n, device="cuda", dtype=torch.float32)
+    torch.cuda.synchronize()
+    rc = L.strm_nn_gemm_bf16(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                             ctypes.cast(d.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                             m, n, k, None)
+    assert rc == 0
+    ref = a.float() @ b.float().T
+    err = (d - ref).abs().max().item()
+    assert err <= 1e-3 * max(1.0, ref.abs().max().item()), err
+
+
+def _bf(t):
+    return t.to(__import__("torch").bfloat16)
+
+
+def _pack_weights(w, cin_p):
+    """torch [cout, cin, 3, 3] -> [cout, kp] with K = tap*cin_p + ci, tap = ky*3 + kx."""
+    import torch
+    cout, cin = w.shape[:2]
+    kp = -(-9 * cin_p // 64) * 64
+    out = torch.zeros(cout, kp, dtype=w.dtype, device=w.device)
+    for ky in range(3):
+        for kx in range(3):
+            t = ky * 3 + kx
+            out[:, t * cin_p:t * cin_p + cin] = w[:, :, ky, kx]
+    return out, kp
+
+
+def _nhwc(x, cin_p):
+    import torch
+    b, c, h, w = x.shape
+    out = torch.zeros(b, h, w, cin_p, dtype=x.dtype, device=x.device)
+    out[..., :c] = x.permute(0, 2, 3, 1)
+    return out.contiguous()
+
+
+@pytest.mark.parametrize("cin,cout,h,w,relu", [(3, 32, 16, 128, 1), (32, 64, 8, 64, 1),
+                                                (96, 32, 16, 32, 0), (128, 256, 4, 64, 1),
+                                                (64, 16, 8, 16, 1)])
+def test_conv3x3_forward_matches_torch(cin, cout, h, w, relu):
+    import torch
+    import torch.nn.functional as F
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(cin * 7 + cout)
+    b = 2
+    cin_p = -(-cin // 8) * 8
+    x = _bf(torch.randn(b, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.2)
+    bias = torch.randn(cout, device="cuda", generator=g)
+    wp, kp = _pack_weights(wt, cin_p)
+    xn = _nhwc(x, cin_p)
+    y = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+    torch.cuda.synchronize()
+    rc = L.strm_nn_conv3x3(xn.data_ptr(), cin_p, cin_p, wp.data_ptr(), kp, bias.data_ptr(),
+                           y.data_ptr(), None, cout, cout, b, h, w, relu, None)
+    assert rc == 0
+    ref = F.conv2d(x.float(), wt.float(), bias, padding=1)
+    if relu:
+        ref = ref.clamp_min(0)
+    ref = ref.permute(0, 2, 3, 1)
+    err = (y.float() - ref).abs().max().item()
+    assert err <= 1e-2 * max(1.0, ref.abs().max().item()), err
+
+
+@pytest.mark.parametrize("cin,cout,h,w", [(32, 32, 16, 64), (64, 128, 8, 32), (16, 16, 16, 16)])
+def test_conv3x3_weight_and_data_gradients_match_torch(cin, cout, h, w):
+    import torch
+    import torch.nn.functional as F
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(cin + 3 * cout)
+    b = 2
+    cin_p = cin
+    x = _bf(torch.randn(b, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.2)
+    gy = _bf(torch.randn(b, cout, h, w, device="cuda", generator=g))
+    # forward with ReLU to get the mask
+    wp, kp = _pack_weights(wt, cin_p)
+    xn = _nhwc(x, cin_p)
+    y = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_conv3x3(xn.data_ptr(), cin_p, cin_p, wp.data_ptr(), kp, None, y.data_ptr(),
+                             None, cout, cout, b, h, w, 1, None) == 0
+    gyn = gy.permute(0, 2, 3, 1).contiguous()
+    dw = torch.zeros(cout, kp, device="cuda", dtype=torch.float32)
+    assert L.strm_nn_conv3x3_wgrad(xn.data_ptr(), cin_p, cin_p, kp, gyn.data_ptr(), cout,
+                                   y.data_ptr(), cout, dw.data_ptr(), cout, b, h, w, None) == 0
+    # torch reference of the same masked gradient
+    mask = (y.float() > 0).permute(0, 3, 1, 2)
+    gm = gy.float() * mask
+    xr = x.float().requires_grad_(True)
+    wr = wt.float().requires_grad_(True)
+    out = F.conv2d(xr, wr, padding=1)
+    (out * gm).sum().backward()
+    ref_w, _ = _pack_weights(wr.grad, cin_p)
+    err = (dw - ref_w).abs().max().item()
+    assert err <= 2e-3 * max(1.0, ref_w.abs().max().item()), err
+    # data gradient: conv of the masked gradient with flipped weights
+    gmn = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_relu_mask(gyn.data_ptr(), cout, y.data_ptr(), cout, gmn.data_ptr(), cout,
+                               b * h * w, cout, None) == 0
+    kp_t = -(-9 * cout // 64) * 64
+    wflip = torch.zeros(cin_p, kp_t, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_flip_weights(wp.data_ptr(), cout, cin_p, kp, wflip.data_ptr(), cout, kp_t,
+                                  None) == 0
+    dx = torch.empty(b, h, w, cin_p, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_conv3x3(gmn.data_ptr(), cout, cout, wflip.data_ptr(), kp_t, None,
+                             dx.data_ptr(), None, cin_p, cin_p, b, h, w, 0, None) == 0
+    torch.cuda.synchronize()
+    ref_x = xr.grad.permute(0, 2, 3, 1)
+    err = (dx.float() - ref_x).abs().max().item()
+    assert err <= 1e-2 * max(1.0, ref_x.abs().max().item()), err
