@@ -86,6 +86,27 @@ enum {
                             debugging */
 };
 
+/* FP32 sweep schedules of the mixed solve (strm_mode.sweep_schedule). */
+enum {
+    STRM_SWEEPS_DEFAULT = 0,    /* 64 x 64 blocked tiles, 4 sweeps per launch */
+    STRM_SWEEPS_PER_COLOUR = 1, /* one launch per colour pass */
+    /* 2..7: tiles kept in shared memory for several sweeps (temporal
+       blocking): 64x64 by 2, 64x64 by 4, 64x64 by 8, 32x128 by 4,
+       96x96 by 4, 96x96 by 8 sweeps per launch */
+    STRM_SWEEPS_COUNT = 8
+};
+
+/* Which cells the residual norm sums (strm_mode.norm_cells). */
+enum {
+    STRM_NORM_ALL_INTERIOR = 0,   /* the reference's sum (src/simulation.rs:216-227) */
+    STRM_NORM_FLUID = 1,          /* fluid cells only */
+    STRM_NORM_FLUID_MEAN_FREE = 2 /* fluid cells, residual mean removed: the
+                                     pressure problem is pure Neumann, so the
+                                     residual's fluid sum equals -sum rhs
+                                     whatever p is; this part cannot be
+                                     solved away and is left out */
+};
+
 /* Mirrors Simulation's parameters (src/simulation.rs:30-69). */
 typedef struct {
     double dx, dy;            /* cell_size */
@@ -111,6 +132,15 @@ typedef struct {
     int strict_eps;   /* 1: stop only at ns < eps^2 (not at ns < initial norm) */
     int inner_sweeps; /* mixed precision: FP32 sweeps per FP64 refinement (0 = 16) */
     int execution;    /* STRM_EXEC_* */
+    int norm_cells;   /* STRM_NORM_ALL_INTERIOR: the residual norm sums every
+                         interior cell, obstacles included, as the reference
+                         does; STRM_NORM_FLUID(_MEAN_FREE): fluid cells only
+                         (extension, red-black orders) -- on grids with
+                         obstacles the reference sum has a floor that the
+                         solve cannot lower.  Divided by fluid_cells. */
+    int sweep_schedule; /* mixed precision: how the FP32 sweeps are issued
+                           (STRM_SWEEPS_*; results are identical, only the
+                           speed differs; strm_autotune_sweeps picks one) */
 } strm_mode;
 
 /* Scalar state readable after any call (pressure_range / speed_range are the
@@ -170,7 +200,10 @@ int strm_tick_solve(strm_sim *sim, uint32_t *sor_iterations, double *norm_square
  * of RHS and pressure and the flag bytes (kind | edge << 3) into device
  * buffers (any may be NULL); p += scale * q on fluid interior cells (q a
  * device FP32 [nx-2][ny-2] array); and device-to-device copies of a whole
- * FP64 field to (to_sim = 0) or from (to_sim = 1) a dense [nx][ny] buffer. */
+ * FP64 field to (to_sim = 0) or from (to_sim = 1) a dense [nx][ny] buffer
+ * (u or v written refresh max|u|, max|v| as strm_upload does).  Each call
+ * returns with its work finished; device inputs written on other streams
+ * must be complete before the call. */
 int strm_export_planes(strm_sim *sim, float *rhs, float *p, uint8_t *flags);
 int strm_apply_correction(strm_sim *sim, const float *q, double scale);
 int strm_copy_field_device(strm_sim *sim, int field, double *dense, int to_sim);
@@ -217,6 +250,22 @@ int strm_calculate_speed_range(strm_sim *sim);     /* src/grid/mod.rs:253-268 */
  * Asynchronous when norm_squared is NULL (see strm_synchronize); otherwise
  * waits and returns the last iteration's norm. */
 int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
+
+/* Residual history of the last pressure solve: (sweeps done, norm_squared)
+ * pairs into out[2*cap], one per norm the solve took (every iteration in
+ * FP64; the starting norm and one per inner_sweeps sweeps in mixed
+ * precision); *n receives how many the solve recorded (at most 65536 are
+ * kept).  Synchronises.  No reference counterpart. */
+int strm_residual_history(strm_sim *sim, double *out, int cap, int *n);
+
+/* Autotuner of the FP32 sweep schedule: times inner_sweeps sweeps `reps`
+ * times under every schedule on this simulation's grid and defect (the
+ * correction buffer is scratch between ticks), selects the fastest into the
+ * mode and rebuilds the step graph.  best (may be NULL) receives its number;
+ * ms_per_sweep (may be NULL, STRM_SWEEPS_COUNT entries) the measured
+ * milliseconds per sweep of schedule v at [v], the best at [0].  Results do
+ * not depend on the schedule.  No reference counterpart. */
+int strm_autotune_sweeps(strm_sim *sim, int reps, int *best, double *ms_per_sweep);
 
 /* Residual norm that allocates nothing.  No counterpart in the reference.
  * For callers that cannot allocate device memory when they need the norm:

@@ -26,6 +26,8 @@ SOR_RED_BLACK, SOR_LEXICOGRAPHIC = 0, 1
 ARITH_EXACT, ARITH_FAST = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 EXEC_GRAPH, EXEC_EAGER = 0, 1
+NORM_ALL_INTERIOR, NORM_FLUID, NORM_FLUID_MEAN_FREE = 0, 1, 2
+SWEEPS_DEFAULT, SWEEPS_PER_COLOUR, SWEEPS_COUNT = 0, 1, 8
 
 
 class Params(ctypes.Structure):
@@ -41,7 +43,8 @@ class Params(ctypes.Structure):
 class Mode(ctypes.Structure):
     _fields_ = [("sor_order", ctypes.c_int), ("arithmetic", ctypes.c_int),
                 ("precision", ctypes.c_int), ("strict_eps", ctypes.c_int),
-                ("inner_sweeps", ctypes.c_int), ("execution", ctypes.c_int)]
+                ("inner_sweeps", ctypes.c_int), ("execution", ctypes.c_int),
+                ("norm_cells", ctypes.c_int), ("sweep_schedule", ctypes.c_int)]
 
 
 class State(ctypes.Structure):
@@ -99,6 +102,8 @@ SIGNATURES = {
     "strm_tick_prepare": [_vp],
     "strm_tick_solve": [_vp, ctypes.POINTER(ctypes.c_uint32), _dp],
     "strm_export_planes": [_vp, _vp, _vp, _vp],
+    "strm_autotune_sweeps": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
+    "strm_residual_history": [_vp, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "strm_apply_correction": [_vp, _vp, ctypes.c_double],
     "strm_copy_field_device": [_vp, ctypes.c_int, _vp, ctypes.c_int],
     "strm_render_rgba": [_vp, ctypes.c_int, _u8p],

@@ -43,6 +43,7 @@ int fail(int code, const char *fmt, ...) {
   } while (0)
 
 constexpr int kLogCap = 4096;
+constexpr int kHistCap = 65536;  // residual history entries of one solve
 constexpr int kAbiVersion = 1;
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -116,13 +117,18 @@ void update_cfg(strm_sim *s) {
   r.tau = s->prm.tau;
   r.delt = s->prm.delt;
   r.itermax = s->prm.max_iterations;
-  r.strict_eps = s->mode.strict_eps;
+  r.strict_eps = (s->mode.strict_eps ? 1 : 0) |
+                 (s->mode.norm_cells != STRM_NORM_ALL_INTERIOR ? 2 : 0) |
+                 (s->mode.norm_cells == STRM_NORM_FLUID_MEAN_FREE ? 4 : 0);
   r.sor_order = s->mode.sor_order == STRM_SOR_LEXICOGRAPHIC ? 1 : 0;
   // grids without interior cells run the single-CTA solve, which handles them
   if (s->g.nx < 3 || s->g.ny < 3) r.sor_order = 1;
   r.arith = s->mode.arithmetic == STRM_ARITH_FAST ? 1 : 0;
   r.precision = s->mode.precision;
   r.inner_sweeps = s->mode.inner_sweeps > 0 ? s->mode.inner_sweeps : 16;
+  // public schedule numbers: 0 default (64 x 64 tiles, 4 sweeps per launch),
+  // 1 one launch per colour pass, 2.. the blocked tile shapes
+  r.sweep_schedule = s->mode.sweep_schedule == 0 ? 2 : s->mode.sweep_schedule - 1;
   r.eager = s->mode.execution == STRM_EXEC_EAGER ? 1 : 0;
 }
 
@@ -307,12 +313,13 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   const size_t o_u = take(nfield * 8), o_v = take(nfield * 8), o_p = take(nfield * 8);
   const size_t o_f = take(nfield * 8), o_g = take(nfield * 8), o_rhs = take(nfield * 8);
   const size_t o_ru = take(nfield * 8), o_rv = take(nfield * 8), o_pw = take(nfield * 8);
-  const size_t o_e32 = take(nfield * 4), o_r32 = take(nfield * 4);
+  const size_t o_e32 = take(nfield * 4), o_r32 = take(nfield * 4), o_e32b = take(nfield * 4);
   const size_t o_fl = take(nfield);
   const size_t o_st = take(sizeof(StepState));
   const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
   const size_t o_log = take(sizeof(StepLog) * kLogCap);
   const size_t o_bad = take(8), o_fc = take(8);
+  const size_t o_hist = take(sizeof(double) * 2 * kHistCap);
   CKC(cudaMalloc(&s->arena, off));
   char *base = (char *)s->arena;
   DevFields &d = s->d;
@@ -327,6 +334,7 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   d.pw = (double *)(base + o_pw);
   d.e32 = (float *)(base + o_e32);
   d.r32 = (float *)(base + o_r32);
+  d.e32b = (float *)(base + o_e32b);
   d.flags = (uint8_t *)(base + o_fl);
   d.st = (StepState *)(base + o_st);
   d.partials = (double *)(base + o_part);
@@ -357,6 +365,8 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   st.p_min = st.s2_min = ord_enc(DBL_MAX);
   st.p_max = st.s2_max = ord_enc(0.0);
   st.log_cap = kLogCap;
+  st.hist = (double *)(base + o_hist);
+  st.hist_cap = kHistCap;
   CKC(cudaMemcpyAsync(d.st, &st, sizeof st, cudaMemcpyHostToDevice, s->stream));
 
   long long bad = -1;
@@ -392,8 +402,12 @@ int strm_set_mode(strm_sim *s, const strm_mode *mode) {
   if (!s || !mode) return fail(STRM_ERR_INVALID, "invalid arguments");
   if (mode->sor_order < 0 || mode->sor_order > 1 || mode->arithmetic < 0 ||
       mode->arithmetic > 1 || mode->precision < 0 || mode->precision > 1 ||
-      mode->execution < 0 || mode->execution > 1 || mode->inner_sweeps < 0)
+      mode->execution < 0 || mode->execution > 1 || mode->inner_sweeps < 0 ||
+      mode->norm_cells < 0 || mode->norm_cells > 2 || mode->sweep_schedule < 0 ||
+      mode->sweep_schedule > num_sweep_schedules())
     return fail(STRM_ERR_INVALID, "unknown mode value");
+  if (mode->norm_cells != STRM_NORM_ALL_INTERIOR && mode->sor_order == STRM_SOR_LEXICOGRAPHIC)
+    return fail(STRM_ERR_INVALID, "the fluid-cell norms are available with red-black orders");
   CK(cudaSetDevice(s->dev));
   s->mode = *mode;
   return rebuild_graph(s);
@@ -659,20 +673,82 @@ int strm_copy_field_device(strm_sim *s, int field, double *dense, int to_sim) {
   if (!f) return fail(STRM_ERR_INVALID, "unknown field %d", field);
   CK(cudaSetDevice(s->dev));
   const Geom &g = s->g;
-  if (to_sim)
+  if (to_sim) {
     CK(cudaMemcpy2DAsync(f, (size_t)g.pitch * 8, dense, (size_t)g.ny * 8, (size_t)g.ny * 8, g.nx,
                          cudaMemcpyDeviceToDevice, s->stream));
-  else
+    // as strm_upload: new velocities refresh max|u|, max|v| for the adaptive step
+    if (field == STRM_FIELD_U || field == STRM_FIELD_V)
+      CK(launch_velocity(s->d, s->cfg, s->stream, 0, 0, 0));
+  } else
     CK(cudaMemcpy2DAsync(dense, (size_t)g.ny * 8, f, (size_t)g.pitch * 8, (size_t)g.ny * 8, g.nx,
                          cudaMemcpyDeviceToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return STRM_OK;
 }
 
+int strm_residual_history(strm_sim *s, double *out, int cap, int *n) {
+  if (!s || !n || cap < 0 || (cap > 0 && !out)) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  int rc = sync_state(s);
+  if (rc) return rc;
+  const int have = (int)s->h_st->hist_n;
+  *n = have;
+  const int k = have < cap ? have : cap;
+  if (k > 0) {
+    CK(cudaMemcpyAsync(out, s->h_st->hist, sizeof(double) * 2 * (size_t)k,
+                       cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  return STRM_OK;
+}
+
+int strm_autotune_sweeps(strm_sim *s, int reps, int *best, double *ms_per_sweep) {
+  if (!s || reps < 1) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  const int m = s->cfg.inner_sweeps;
+  cudaEvent_t ev[2];
+  CK(cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return fail(STRM_ERR_CUDA, "cudaEventCreate failed");
+  }
+  RunCfg r = s->cfg;
+  int best_v = 1;
+  double best_t = 0.0;
+  cudaError_t e = cudaSuccess;
+  for (int v = 1; v < STRM_SWEEPS_COUNT && e == cudaSuccess; ++v) {
+    r.sweep_schedule = v - 1;
+    e = launch_mixed_sweeps(s->d, r, s->stream, m);  // warm-up (and smem opt-in)
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s->stream);
+    for (int i = 0; i < reps && e == cudaSuccess; ++i)
+      e = launch_mixed_sweeps(s->d, r, s->stream, m);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    const double per = (double)ms / ((double)reps * m);
+    if (ms_per_sweep) ms_per_sweep[v] = per;
+    if (e == cudaSuccess && (v == 1 || per < best_t)) {
+      best_t = per;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  CK(e);
+  if (ms_per_sweep) ms_per_sweep[0] = best_t;
+  if (best) *best = best_v;
+  s->mode.sweep_schedule = best_v;
+  return rebuild_graph(s);
+}
+
 int strm_sor_sweeps(strm_sim *s, int n, double *norm_squared) {
   if (!s || n < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
   CK(cudaSetDevice(s->dev));
-  for (int i = 0; i < n; ++i) CK(launch_sor_iteration(s->d, s->cfg, s->stream));
+  if (s->cfg.precision == 1)
+    CK(launch_mixed_sweeps(s->d, s->cfg, s->stream, n));
+  else
+    for (int i = 0; i < n; ++i) CK(launch_sor_iteration(s->d, s->cfg, s->stream));
   if (!norm_squared) return STRM_OK;
   int rc = sync_state(s);
   if (rc) return rc;

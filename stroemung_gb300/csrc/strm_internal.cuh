@@ -67,7 +67,20 @@ struct StepState {
   unsigned int counter;     // last-block-done ticket for grid reductions
   unsigned int log_pos;     // next slot of the per-step log
   unsigned int log_cap;
+  // residual history of the current step's solve: (sweeps, norm) pairs
+  double *hist;
+  unsigned int hist_n, hist_cap;
 };
+
+// Appends (sweeps, norm) to the solve's residual history (one thread).
+__device__ __forceinline__ void hist_push(StepState *st, unsigned int sweeps, double ns) {
+  const unsigned int n = st->hist_n;
+  if (st->hist && n < st->hist_cap) {
+    st->hist[2 * (size_t)n] = (double)sweeps;
+    st->hist[2 * (size_t)n + 1] = ns;
+    st->hist_n = n + 1;
+  }
+}
 
 // One record per completed step.
 struct StepLog {

@@ -163,6 +163,7 @@ __device__ __forceinline__ void step_begin(StepState *st, const Consts &c, doubl
   st->ns = 0.0;
   st->body_count = 0;
   st->overrun = 0;
+  st->hist_n = 0;
 }
 
 __global__ void __cluster_dims__(BC_CLUSTER, 1, 1) __launch_bounds__(BC_THREADS)
@@ -422,6 +423,22 @@ __global__ void __launch_bounds__(256)
 
 // What a residual launch does once the norm is known.
 enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2 };
+// bits of the `strict` argument of the residual kernels
+enum : int {
+  STOP_STRICT = 1,      // stop only at ns < eps^2 (not at ns < the initial norm)
+  STOP_FLUID_NORM = 2,  // sum the residual over fluid cells only (not every interior cell)
+  STOP_MEAN_FREE = 4,   // with STOP_FLUID_NORM: remove the residual's mean over fluid cells
+};
+
+// The norm from the block sums: sum r^2 (and sum r when mean_free, stored
+// interleaved), divided by fluid_cells; mean-free: (sum r^2 - (sum r)^2 / n) / n.
+__device__ __forceinline__ double finish_norm(const double *partials, int nblocks,
+                                              bool mean_free, double fluid_cells) {
+  if (!mean_free) return reduce_partials(partials, nblocks, 1, 0, OpAdd(), 0.0) / fluid_cells;
+  const double s2 = reduce_partials(partials, nblocks, 2, 0, OpAdd(), 0.0);
+  const double s1 = reduce_partials(partials, nblocks, 2, 1, OpAdd(), 0.0);
+  return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
 
 // Residual norm over every interior cell (src/simulation.rs:216-227), in
 // grid-stride tiles; the last block to finish sums the per-block partials in
@@ -430,10 +447,13 @@ enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2 };
 // WHILE loop.
 template <bool EXACT, bool IN_GRAPH>
 __global__ void __launch_bounds__(256)
-    residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs, Geom g,
-                    Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
-                    cudaGraphConditionalHandle h, unsigned int itermax, int strict, int mode) {
-  double acc = 0.0;
+    residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
+                    const uint8_t *__restrict__ flags, Geom g, Consts c, StepState *st,
+                    double *partials, int tiles_y, int ntiles, cudaGraphConditionalHandle h,
+                    unsigned int itermax, int strict, int mode) {
+  const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
+  const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
+  double acc = 0.0, acc1 = 0.0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int tx = t / tiles_y, ty = t % tiles_y;
     const int x = 1 + tx * RT_X + threadIdx.y;
@@ -444,14 +464,24 @@ __global__ void __launch_bounds__(256)
       const int y = yb + q;
       if (y <= g.ny - 2) {
         const size_t o = OFF(x, y);
+        if (fluid_only && flags[o] != 0) continue;
         const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
                                             p[o + 1], rhs[o], c);
         acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
+        acc1 += r;
       }
     }
   }
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
-  if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = bsum;
+  if (mean_free) {
+    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      partials[2 * blockIdx.x] = bsum;
+      partials[2 * blockIdx.x + 1] = bsum1;
+    }
+  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
+    partials[blockIdx.x] = bsum;
+  }
   if (IN_GRAPH && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     // Independent bound on the WHILE loop: the normal stop below ends it at
     // iteration itermax at the latest; should that bookkeeping ever fail,
@@ -463,10 +493,9 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (!last_block_done(&st->counter)) return;
-  const double total = reduce_partials(partials, gridDim.x, 1, 0, OpAdd(), 0.0);
+  const double ns = finish_norm(partials, gridDim.x, mean_free, st->fluid_cells);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->counter = 0;
-    const double ns = total / st->fluid_cells;
     if (mode == RES_NS0) {
       st->ns0 = ns;
     } else if (mode == RES_NORM) {
@@ -475,8 +504,9 @@ __global__ void __launch_bounds__(256)
       const unsigned int it = st->sor_iters + 1;
       st->sor_iters = it;
       st->ns = ns;
+      hist_push(st, it, ns);
       st->nonfinite = !isfinite(ns);
-      const bool done = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      const bool done = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
       if (done) st->converged = 1;
       else if (it >= itermax) st->exhausted = 1;
       if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
@@ -525,7 +555,7 @@ __global__ void __launch_bounds__(1024)
       for (int k = 0; k < NI * NJ; ++k) acc = acc + r2[k];
       ns = acc / st->fluid_cells;
       iters = it + 1;
-      conv = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      conv = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
       s_done = conv;
     }
     __syncthreads();
@@ -740,11 +770,92 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Temporal blocking of the same sweeps: one CTA loads a TX x TY tile of the
+// correction with an H-cell halo (and the defect and flags) into shared
+// memory, runs `n` red-black sweeps there (2n colour passes, n <= H/2; the
+// region that is still exact shrinks by one cell per pass) and writes the
+// tile back.  Reads come from `ein`, writes go to `eout` (another buffer:
+// neighbouring CTAs read this tile's cells as their halo).  Each cell sees
+// exactly the arithmetic of sor32_color_kernel in the same colour order, so
+// the result is bit-identical to n x (red, black) of that kernel.  The last
+// black pass skips its boundary copy when skip_last_copy is set.
+constexpr uint8_t kFrozen = 0xFF;  // cell code: never written (outside, edge-less boundary)
+
+template <int H, int TX, int TY>
+__global__ void __launch_bounds__(512)
+    sor32_tb_kernel(const float *__restrict__ ein, float *__restrict__ eout,
+                    const float *__restrict__ s, const uint8_t *__restrict__ flags, Geom g,
+                    Consts32 k, int tiles_y, int n, int skip_last_copy) {
+  constexpr int EX = TX + 2 * H, EY = TY + 2 * H, NC = EX * EY;
+  constexpr int WARPS = 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *se = reinterpret_cast<float *>(smem_raw);
+  float *ss = se + NC;
+  uint8_t *sc = reinterpret_cast<uint8_t *>(ss + NC);  // 0 SOR, 1..8 copy edge, kFrozen
+  const int gx0 = (int)(blockIdx.x / tiles_y) * TX - H;
+  const int gy0 = (int)(blockIdx.x % tiles_y) * TY - H;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int lx = warp; lx < EX; lx += WARPS) {
+    const int x = gx0 + lx;
+    for (int ly = lane; ly < EY; ly += 32) {
+      const int y = gy0 + ly;
+      const int i = lx * EY + ly;
+      float ev = 0.0f, sv = 0.0f;
+      uint8_t code = kFrozen;
+      if (x >= 0 && y >= 0 && x < g.nx && y < g.ny) {
+        const size_t o = OFF(x, y);
+        ev = ein[o];
+        sv = s[o];
+        const uint8_t fl = flags[o];
+        if (fl == 0) {
+          if (x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2) code = 0;
+        } else if (edge_of(fl) != E_NONE) {
+          code = edge_of(fl);
+        }
+      }
+      se[i] = ev;
+      ss[i] = sv;
+      sc[i] = code;
+    }
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 2 * n; ++pass) {
+    const int color = pass & 1;
+    const bool copy = !(skip_last_copy && pass == 2 * n - 1);
+    const int lo = pass + 1, hix = EX - 2 - pass, hiy = EY - 2 - pass;
+    for (int lx = lo + warp; lx <= hix; lx += WARPS) {
+      // first column of the colour in this row: (x + y) & 1 == color
+      const int ly0 = lo + ((gx0 + lx + gy0 + lo + color) & 1);
+      for (int ly = ly0 + 2 * lane; ly <= hiy; ly += 64) {
+        const int li = lx * EY + ly;
+        const uint8_t code = sc[li];
+        if (code == 0) {
+          const float sum_x = se[li - EY] + se[li + EY];
+          const float sum_y = se[li - 1] + se[li + 1];
+          se[li] = fmaf(k.omw, se[li], fmaf(k.a, sum_x, fmaf(k.b, sum_y, ss[li])));
+        } else if (copy && code != kFrozen) {
+          se[li] = ss[li] + copy32(se, (size_t)li, EY, code);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int lx = H + warp; lx < H + TX; lx += WARPS) {
+    const int x = gx0 + lx;
+    if (x >= g.nx) break;
+    for (int ly = H + lane; ly < H + TY; ly += 32) {
+      const int y = gy0 + ly;
+      if (y < g.ny) eout[OFF(x, y)] = se[lx * EY + ly];
+    }
+  }
+}
+
 // p += e on fluid interior cells and boundary cells with an edge (apply != 0),
-// then e = 0 everywhere.
+// then ez = 0 everywhere (the buffer the next sweeps start from; e itself
+// when the sweeps ended where they started).
 __global__ void __launch_bounds__(256)
-    refine_kernel(double *__restrict__ p, float *__restrict__ e, const uint8_t *__restrict__ flags,
-                  Geom g, int apply) {
+    refine_kernel(double *__restrict__ p, const float *e, float *ez,
+                  const uint8_t *__restrict__ flags, Geom g, int apply) {
   const int x = blockIdx.y * blockDim.y + threadIdx.y;
   const int y0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (x >= g.nx) return;
@@ -757,7 +868,7 @@ __global__ void __launch_bounds__(256)
     const bool fluid_in = fl == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
     if (apply && (fluid_in || (is_bnd(fl) && edge_of(fl) != E_NONE)))
       p[o] = p[o] + (double)e[o];
-    e[o] = 0.0f;
+    ez[o] = 0.0f;
   }
 }
 
@@ -795,7 +906,9 @@ __global__ void __launch_bounds__(256)
                           Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
                           cudaGraphConditionalHandle h, unsigned int itermax, int strict,
                           int sweeps, int check) {
-  double acc = 0.0;
+  const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
+  const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
+  double acc = 0.0, acc1 = 0.0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
     if (x > g.nx - 2) continue;
@@ -807,13 +920,25 @@ __global__ void __launch_bounds__(256)
         const size_t o = OFF(x, y);
         const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
                                             p[o + 1], rhs[o], c);
-        acc = fma(r, r, acc);
-        if (flags[o] == 0) s[o] = (float)(c.middle * r);
+        const bool fluid = flags[o] == 0;
+        if (fluid || !fluid_only) {
+          acc = fma(r, r, acc);
+          acc1 += r;
+        }
+        if (fluid) s[o] = (float)(c.middle * r);
       }
     }
   }
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
-  if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = bsum;
+  if (mean_free) {
+    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      partials[2 * blockIdx.x] = bsum;
+      partials[2 * blockIdx.x + 1] = bsum1;
+    }
+  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
+    partials[blockIdx.x] = bsum;
+  }
   if (IN_GRAPH && check && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     // independent bound on the WHILE loop, as in residual_kernel
     const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
@@ -823,16 +948,16 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (!last_block_done(&st->counter)) return;
-  const double total = reduce_partials(partials, gridDim.x, 1, 0, OpAdd(), 0.0);
+  const double ns = finish_norm(partials, gridDim.x, mean_free, st->fluid_cells);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->counter = 0;
-    const double ns = total / st->fluid_cells;
     st->ns = ns;
+    hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
     if (check) {
       const unsigned int it = st->sor_iters + sweeps;
       st->sor_iters = it;
       st->nonfinite = !isfinite(ns);
-      const bool done = strict ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      const bool done = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
       const bool room = it + sweeps <= itermax;
       if (done) st->converged = 1;
       else if (!room) st->exhausted = 1;
@@ -982,6 +1107,118 @@ int residual_blocks(const Geom &g) {
 
 static const dim3 kRedBlock(RT_Y / 2, RT_X);
 
+// The sweep schedules: 0 is one launch per colour pass; the others are
+// temporal-blocking tile shapes, `sweeps` red-black sweeps per launch.
+struct TbShape {
+  int halo, tx, ty, sweeps;
+  const void *fn;
+};
+
+static const TbShape kTbShapes[] = {
+    {0, 0, 0, 1, nullptr},
+    {4, 64, 64, 2, (const void *)sor32_tb_kernel<4, 64, 64>},
+    {8, 64, 64, 4, (const void *)sor32_tb_kernel<8, 64, 64>},
+    {16, 64, 64, 8, (const void *)sor32_tb_kernel<16, 64, 64>},
+    {8, 32, 128, 4, (const void *)sor32_tb_kernel<8, 32, 128>},
+    {8, 96, 96, 4, (const void *)sor32_tb_kernel<8, 96, 96>},
+    {16, 96, 96, 8, (const void *)sor32_tb_kernel<16, 96, 96>},
+};
+constexpr int kNumSchedules = (int)(sizeof(kTbShapes) / sizeof(kTbShapes[0]));
+
+int num_sweep_schedules() { return kNumSchedules; }
+
+static size_t tb_smem(const TbShape &t) {
+  const size_t nc = (size_t)(t.tx + 2 * t.halo) * (t.ty + 2 * t.halo);
+  return nc * (4 + 4 + 1);
+}
+
+// One launch of a sweep schedule: what it reads, writes and how.
+struct SweepLaunch {
+  const void *fn;
+  dim3 grid, block;
+  size_t smem;
+  const float *ein;
+  float *eout;
+  int tiles_y, n, skip_last_copy;
+  int color, copy;  // schedule 0
+};
+
+// The launches of m inner sweeps (colour passes or blocked tiles) starting
+// from correction buffer a; *final receives the buffer holding the result.
+static std::vector<SweepLaunch> sweep_plan(const DevFields &d, const Geom &g, int m, int sched,
+                                           float **final) {
+  std::vector<SweepLaunch> v;
+  if (sched <= 0 || sched >= kNumSchedules) {
+    dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (g.nx + kRedBlock.y - 1) / kRedBlock.y);
+    for (int i = 0; i < m; ++i)
+      for (int color = 0; color < 2; ++color) {
+        SweepLaunch l{};
+        l.fn = (const void *)sor32_color_kernel;
+        l.grid = pgrid;
+        l.block = kRedBlock;
+        l.ein = d.e32;
+        l.eout = d.e32;
+        l.color = color;
+        l.copy = (color == 0 || i < m - 1) ? 1 : 0;
+        v.push_back(l);
+      }
+    *final = d.e32;
+    return v;
+  }
+  const TbShape &t = kTbShapes[sched];
+  const int tiles_x = (g.nx + t.tx - 1) / t.tx, tiles_y = (g.ny + t.ty - 1) / t.ty;
+  float *bufs[2] = {d.e32, d.e32b};
+  int cur = 0;
+  for (int done = 0; done < m; done += t.sweeps) {
+    SweepLaunch l{};
+    l.fn = t.fn;
+    l.grid = dim3(tiles_x * tiles_y);
+    l.block = dim3(512);
+    l.smem = tb_smem(t);
+    l.ein = bufs[cur];
+    l.eout = bufs[cur ^ 1];
+    l.tiles_y = tiles_y;
+    l.n = m - done < t.sweeps ? m - done : t.sweeps;
+    l.skip_last_copy = done + l.n >= m ? 1 : 0;
+    v.push_back(l);
+    cur ^= 1;
+  }
+  *final = bufs[cur];
+  return v;
+}
+
+// Opts the blocked kernels into their shared-memory size, once per device.
+static cudaError_t tb_prepare() {
+  static bool done_on[64] = {};
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return e0;
+  bool &done = done_on[dev & 63];
+  if (done) return cudaSuccess;
+  for (int i = 1; i < kNumSchedules; ++i) {
+    cudaError_t e = cudaFuncSetAttribute(kTbShapes[i].fn,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tb_smem(kTbShapes[i]));
+    if (e != cudaSuccess) return e;
+  }
+  done = true;
+  return cudaSuccess;
+}
+
+static cudaError_t issue_sweep(const SweepLaunch &l, const float *s, const uint8_t *flags,
+                               const Geom &g, const Consts32 &k32, cudaStream_t st) {
+  if (l.smem == 0) {
+    sor32_color_kernel<<<l.grid, l.block, 0, st>>>(l.eout, s, flags, g, k32, l.color, l.copy);
+  } else {
+    void *args[] = {(void *)&l.ein, (void *)&l.eout, (void *)&s, (void *)&flags, (void *)&g,
+                    (void *)&k32, (void *)&l.tiles_y, (void *)&l.n, (void *)&l.skip_last_copy};
+    return cudaLaunchKernel(l.fn, l.grid, l.block, args, l.smem, st);
+  }
+  return cudaGetLastError();
+}
+
+
 cudaError_t launch_classify(const DevFields &d, const Geom &g, cudaStream_t s) {
   dim3 blk(64, 4), grd((g.ny + 63) / 64, (g.nx + 3) / 4);
   classify_kernel<<<grd, blk, 0, s>>>(d.flags, g, d.fluid_count, d.first_bad);
@@ -1021,7 +1258,7 @@ cudaError_t launch_norm(const DevFields &d, const RunCfg &r, cudaStream_t s, int
     return cudaSuccess;
   }
   int nb = residual_blocks(r.g);
-  residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st, d.partials,
+  residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st, d.partials,
                                                         ty, nt, 0, r.itermax, r.strict_eps,
                                                         set_ns0 ? RES_NS0 : RES_NORM);
   return cudaGetLastError();
@@ -1039,7 +1276,7 @@ cudaError_t launch_norm_one_block_per_tile(const double *p, const double *rhs, c
   int ty, nt;
   tiles_of(g, 1, &ty, &nt);
   if (nt == 0) return cudaSuccess;
-  residual_kernel<true, false><<<nt, kRedBlock, 0, s>>>(p, rhs, g, c, st, partials, ty, nt, 0,
+  residual_kernel<true, false><<<nt, kRedBlock, 0, s>>>(p, rhs, nullptr, g, c, st, partials, ty, nt, 0,
                                                         0u, 0, RES_NORM);
   return cudaGetLastError();
 }
@@ -1063,23 +1300,33 @@ cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, i
   return cudaGetLastError();
 }
 
+static Consts32 consts32_of(const Consts &c) {
+  Consts32 k32;
+  k32.omw = (float)c.one_minus_w;
+  k32.a = (float)(c.middle * c.r_dx2);
+  k32.b = (float)(c.middle * c.r_dy2);
+  return k32;
+}
+
+cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_t s, int n) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = tb_prepare();
+  if (e != cudaSuccess) return e;
+  float *final = nullptr;
+  const Consts32 k32 = consts32_of(r.c);
+  for (const SweepLaunch &l : sweep_plan(d, r.g, n, r.sweep_schedule, &final))
+    if ((e = issue_sweep(l, d.r32, d.flags, r.g, k32, s)) != cudaSuccess) return e;
+  if (final != d.e32)
+    e = cudaMemcpyAsync(d.e32, final, sizeof(float) * (size_t)r.g.nx * r.g.pitch,
+                        cudaMemcpyDeviceToDevice, s);
+  return e;
+}
+
 cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s) {
   int ty, nt;
   tiles_of(r.g, 1, &ty, &nt);
   if (nt == 0) return cudaSuccess;
-  if (r.precision == 1) {
-    // one FP32 red-black sweep of the correction equation on the current
-    // defect (the inner iteration of the mixed-precision solve)
-    Consts32 k32;
-    k32.omw = (float)r.c.one_minus_w;
-    k32.a = (float)(r.c.middle * r.c.r_dx2);
-    k32.b = (float)(r.c.middle * r.c.r_dy2);
-    dim3 pgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
-               (r.g.nx + kRedBlock.y - 1) / kRedBlock.y);
-    for (int color = 0; color < 2; ++color)
-      sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, r.g, k32, color, 1);
-    return cudaGetLastError();
-  }
+  if (r.precision == 1) return launch_mixed_sweeps(d, r, s, 1);
   cudaError_t e = launch_pcopy(d, r.g, s);
   if (e != cudaSuccess) return e;
   dim3 sgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
@@ -1092,11 +1339,11 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
       sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
   }
   if (r.arith)
-    residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st,
+    residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
                                                            r.strict_eps, RES_NORM);
   else
-    residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, r.g, r.c, d.st,
+    residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                           d.partials, ty, nt, 0, r.itermax,
                                                           r.strict_eps, RES_NORM);
   return cudaGetLastError();
@@ -1145,23 +1392,21 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     if ((e = launch_sor_lex(d, r, s)) != cudaSuccess) return e;
   } else if (r.precision == 1 && nt_int > 0 && r.itermax > 0) {
     const int m = (int)((unsigned)r.inner_sweeps < r.itermax ? (unsigned)r.inner_sweeps : r.itermax);
-    Consts32 k32;
-    k32.omw = (float)c.one_minus_w;
-    k32.a = (float)(c.middle * c.r_dx2);
-    k32.b = (float)(c.middle * c.r_dy2);
+    const Consts32 k32 = consts32_of(c);
     dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx + kRedBlock.y - 1) / kRedBlock.y);
-    refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 0);
+    if ((e = tb_prepare()) != cudaSuccess) return e;
+    float *final = nullptr;
+    const std::vector<SweepLaunch> plan = sweep_plan(d, g, m, r.sweep_schedule, &final);
+    refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0);
     launch_delta(d, g, s);
     mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
                                                           d.partials, ty_int, nt_int, 0,
                                                           r.itermax, r.strict_eps, m, 0);
     while (!done) {
-      for (int i = 0; i < m; ++i)
-        for (int color = 0; color < 2; ++color)
-          sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color,
-                                                         (color == 0 || i < m - 1) ? 1 : 0);
-      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.flags, g, 1);
+      for (const SweepLaunch &l : plan)
+        if ((e = issue_sweep(l, d.r32, d.flags, g, k32, s)) != cudaSuccess) return e;
+      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1);
       launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
@@ -1180,11 +1425,11 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
           sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
       }
       if (r.arith)
-        residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, g, c, d.st, d.partials,
+        residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                                ty_int, nt_int, 0, r.itermax,
                                                                r.strict_eps, RES_SOLVE);
       else
-        residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, g, c, d.st, d.partials,
+        residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                               ty_int, nt_int, 0, r.itermax,
                                                               r.strict_eps, RES_SOLVE);
       if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
@@ -1220,6 +1465,25 @@ struct GraphBuilder {
     kp.gridDim = grid;
     kp.blockDim = block;
     kp.sharedMemBytes = 0;
+    kp.kernelParams = ptrs;
+    kp.extra = nullptr;
+    cudaGraphNode_t node = nullptr;
+    err = cudaGraphAddKernelNode(&node, gr, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+    return node;
+  }
+
+  template <typename... Args>
+  cudaGraphNode_t kernel_smem(cudaGraph_t gr, cudaGraphNode_t dep, const void *fn, dim3 grid,
+                              dim3 block, size_t smem, Args... args) {
+    if (err != cudaSuccess) return nullptr;
+    void *ptrs[sizeof...(Args) + 1];
+    size_t i = 0;
+    (void)std::initializer_list<int>{(ptrs[i++] = keep(args), 0)...};
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void *>(fn);
+    kp.gridDim = grid;
+    kp.blockDim = block;
+    kp.sharedMemBytes = (unsigned int)smem;
     kp.kernelParams = ptrs;
     kp.extra = nullptr;
     cudaGraphNode_t node = nullptr;
@@ -1267,17 +1531,17 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                  d.n_pcopy, g, c, d.st, d.pw, r.itermax, r.strict_eps);
   } else if (r.precision == 1 && nt_int > 0 && r.itermax > 0) {
     const int m = (int)((unsigned)r.inner_sweeps < r.itermax ? (unsigned)r.inner_sweeps : r.itermax);
-    Consts32 k32;
-    k32.omw = (float)c.one_minus_w;
-    k32.a = (float)(c.middle * c.r_dx2);
-    k32.b = (float)(c.middle * c.r_dy2);
+    const Consts32 k32 = consts32_of(c);
     dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx + kRedBlock.y - 1) / kRedBlock.y);
+    if (b.err == cudaSuccess) b.err = tb_prepare();
+    float *final = nullptr;
+    const std::vector<SweepLaunch> plan = sweep_plan(d, g, m, r.sweep_schedule, &final);
     cudaGraphConditionalHandle h;
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
-    n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
-                 (const uint8_t *)d.flags, g, 0);
+    n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
+                 (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0);
     if (d.n_pcopy > 0)
       n = b.kernel(b.graph, n, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
                    dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
@@ -1296,13 +1560,17 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     if (b.err == cudaSuccess) {
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
-      for (int i = 0; i < m; ++i)
-        for (int color = 0; color < 2; ++color)
-          bn = b.kernel(body, bn, (const void *)sor32_color_kernel, pgrid, kRedBlock, d.e32,
-                        (const float *)d.r32, (const uint8_t *)d.flags, g, k32, color,
-                        (color == 0 || i < m - 1) ? 1 : 0);
-      bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p, d.e32,
-                    (const uint8_t *)d.flags, g, 1);
+      for (const SweepLaunch &l : plan) {
+        if (l.smem == 0)
+          bn = b.kernel(body, bn, l.fn, l.grid, l.block, l.eout, (const float *)d.r32,
+                        (const uint8_t *)d.flags, g, k32, l.color, l.copy);
+        else
+          bn = b.kernel_smem(body, bn, l.fn, l.grid, l.block, l.smem, l.ein, l.eout,
+                             (const float *)d.r32, (const uint8_t *)d.flags, g, k32, l.tiles_y,
+                             l.n, l.skip_last_copy);
+      }
+      bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
+                    (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1);
       if (d.n_pcopy > 0)
         bn = b.kernel(body, bn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
                       dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
@@ -1340,7 +1608,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
                       (const uint8_t *)d.flags, g, c, color);
       bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
-                    (const double *)d.rhs, g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax,
+                    (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax,
                     r.strict_eps, (int)RES_SOLVE);
     }
     n = wnode;

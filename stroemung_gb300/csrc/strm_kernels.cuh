@@ -17,6 +17,7 @@ struct DevFields {
   uint8_t *flags;
   // mixed-precision pressure solve
   float *e32, *r32;       // FP32 correction and defect
+  float *e32b;            // second correction buffer (temporal-blocked sweeps)
   double *pw;             // FP64 work field
   StepState *st;
   double *partials;       // per-CTA residual partial sums
@@ -42,6 +43,7 @@ struct RunCfg {
   int arith;              // 0 exact, 1 fast
   int precision;          // 0 fp64, 1 mixed
   int inner_sweeps;
+  int sweep_schedule;     // FP32 sweep schedule (0 per-colour launches, 1.. blocked tiles)
   int eager;              // 1: launch kernels one by one instead of the graph
 };
 
@@ -58,6 +60,10 @@ cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, i
 cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s);
 // One red-black pressure iteration (copy, red, black, residual) without a stop test.
 cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s);
+// n FP32 red-black sweeps of the correction equation on the current defect
+// (the inner iteration of the mixed solve), by the configured schedule.
+cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_t s, int n);
+int num_sweep_schedules();
 
 // Colour map into a device RGBA8 image [ny][nx] (0 pressure, 1 speed).
 cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, void *rgba,

@@ -23,12 +23,13 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (ARITH_EXACT, ARITH_FAST, PREC_FP64, PREC_MIXED, SOR_LEXICOGRAPHIC,
-                   SOR_RED_BLACK, BoundaryTooThinError, NonFiniteError, StroemungError)
+from ._lib import (ARITH_EXACT, ARITH_FAST, NORM_ALL_INTERIOR, NORM_FLUID,
+                   NORM_FLUID_MEAN_FREE, PREC_FP64,
+                   PREC_MIXED, SOR_LEXICOGRAPHIC, SOR_RED_BLACK, BoundaryTooThinError, NonFiniteError, StroemungError)
 
 __all__ = ["Simulation", "BoundaryTooThinError", "NonFiniteError", "StroemungError",
            "SOR_RED_BLACK", "SOR_LEXICOGRAPHIC", "ARITH_EXACT", "ARITH_FAST", "PREC_FP64",
-           "PREC_MIXED"]
+           "PREC_MIXED", "NORM_ALL_INTERIOR", "NORM_FLUID", "NORM_FLUID_MEAN_FREE"]
 
 _FIELDS = {"u": _lib.FIELD_U, "v": _lib.FIELD_V, "p": _lib.FIELD_P, "pressure": _lib.FIELD_P,
            "f": _lib.FIELD_F, "g": _lib.FIELD_G, "rhs": _lib.FIELD_RHS}
@@ -51,7 +52,8 @@ class Simulation:
                  omega: float = 1.7, iterations: int = 0, time: float = 0.0,
                  initial_norm_squared=None, tau: float = 0.0, sor_order: int = SOR_RED_BLACK,
                  arithmetic: int = ARITH_EXACT, precision: int = PREC_FP64,
-                 strict_eps: bool = False, inner_sweeps: int = 0, execution: int = 0):
+                 strict_eps: bool = False, inner_sweeps: int = 0, execution: int = 0,
+                 norm_cells: int = NORM_ALL_INTERIOR, sweep_schedule: int = 0):
         L = _lib.load()
         kind = np.ascontiguousarray(grid["kind"], dtype=np.uint8)
         self.size = tuple(int(s) for s in kind.shape)
@@ -88,7 +90,8 @@ class Simulation:
         self._kind = kind.copy()
         self._wall = np.zeros((nx, ny, 2)) if wall is None else wall.copy()
         self.set_mode(sor_order=sor_order, arithmetic=arithmetic, precision=precision,
-                      strict_eps=strict_eps, inner_sweeps=inner_sweeps, execution=execution)
+                      strict_eps=strict_eps, inner_sweeps=inner_sweeps, execution=execution,
+                      norm_cells=norm_cells, sweep_schedule=sweep_schedule)
 
     @classmethod
     def from_json(cls, path_or_text, float_parser: str = "serde", **mode):
@@ -139,20 +142,52 @@ class Simulation:
 
     # ---- configuration ---------------------------------------------------
     def set_mode(self, *, sor_order=SOR_RED_BLACK, arithmetic=ARITH_EXACT, precision=PREC_FP64,
-                 strict_eps=False, inner_sweeps=0, execution=0):
+                 strict_eps=False, inner_sweeps=0, execution=0, norm_cells=NORM_ALL_INTERIOR,
+                 sweep_schedule=0):
         m = _lib.Mode(sor_order=sor_order, arithmetic=arithmetic, precision=precision,
                       strict_eps=1 if strict_eps else 0, inner_sweeps=inner_sweeps,
-                      execution=execution)
+                      execution=execution, norm_cells=norm_cells, sweep_schedule=sweep_schedule)
         _lib.check(_lib.load().strm_set_mode(self._h, ctypes.byref(m)))
         self.mode = {"sor_order": sor_order, "arithmetic": arithmetic, "precision": precision,
                      "strict_eps": bool(strict_eps), "inner_sweeps": inner_sweeps,
-                     "execution": execution}
+                     "execution": execution, "norm_cells": norm_cells,
+                     "sweep_schedule": sweep_schedule}
+
+    def residual_history(self) -> np.ndarray:
+        """(sweeps, norm_squared) rows of the last pressure solve."""
+        n = ctypes.c_int(0)
+        L = _lib.load()
+        _lib.check(L.strm_residual_history(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), 2))
+        _lib.check(L.strm_residual_history(self._h, _dp(out), n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def autotune_sweeps(self, reps: int = 5):
+        """Times every FP32 sweep schedule on this grid, keeps the fastest;
+        returns (schedule, {schedule: ms per sweep})."""
+        best = ctypes.c_int(0)
+        ms = (ctypes.c_double * _lib.SWEEPS_COUNT)()
+        _lib.check(_lib.load().strm_autotune_sweeps(self._h, int(reps), ctypes.byref(best), ms))
+        self.mode["sweep_schedule"] = best.value
+        return best.value, {v: ms[v] for v in range(1, _lib.SWEEPS_COUNT)}
 
     # ---- the timestep (src/simulation.rs:324-333) --------------------------
     def run_simulation_tick(self):
         it = ctypes.c_uint32(0)
         ns = ctypes.c_double(0.0)
         _lib.check(_lib.load().strm_tick(self._h, ctypes.byref(it), ctypes.byref(ns)))
+        return it.value, ns.value
+
+    def tick_prepare(self):
+        """First half of a tick: time step, boundary pass, F/G and RHS."""
+        _lib.check(_lib.load().strm_tick_prepare(self._h))
+
+    def tick_solve(self):
+        """Second half: pressure solve, velocity update, time bookkeeping;
+        returns what run_simulation_tick returns."""
+        it = ctypes.c_uint32(0)
+        ns = ctypes.c_double(0.0)
+        _lib.check(_lib.load().strm_tick_solve(self._h, ctypes.byref(it), ctypes.byref(ns)))
         return it.value, ns.value
 
     def step_n(self, n: int):

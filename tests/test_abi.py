@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol():
 def test_struct_sizes_match_header_layout():
     # strm_params: 7 doubles, 2 uint32, 3 doubles
     assert ctypes.sizeof(_lib.Params) == 7 * 8 + 2 * 4 + 3 * 8
-    assert ctypes.sizeof(_lib.Mode) == 6 * 4
+    assert ctypes.sizeof(_lib.Mode) == 8 * 4
     assert ctypes.sizeof(_lib.StepStats) == 24
 
 

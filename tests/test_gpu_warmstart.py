@@ -1,0 +1,210 @@
+"""Learned warm start on the GPU: input assembly, forward, loss, the full
+backward (every parameter gradient) and Adam against the torch-CPU oracle
+(oracle/unet_oracle.py), the fluid-cell norm option, and training."""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+
+def _planes_from_solver(imax=32, jmax=32, steps=3, batch=2):
+    """Real solver planes: a small channel with one obstacle, `batch`
+    consecutive steps exported between tick_prepare and tick_solve."""
+    from stroemung_gb300 import presets, warmstart
+    grid = presets.channel(imax, jmax, [(12, 12, 6, 5)])
+    sim = warmstart.make_simulation(grid, 200.0, 0.01, max_iterations=200)
+    planes = warmstart.PlaneBatch(batch, imax + 2, jmax + 2)
+    for _ in range(steps - batch):
+        sim.run_simulation_tick()
+    for i in range(batch):
+        sim.tick_prepare()
+        warmstart.export_sample(sim, planes, i)
+        sim.tick_solve()
+    sim.close()
+    return planes
+
+
+def _net_with_random_head(seed=3):
+    import torch
+    from stroemung_gb300.unet import UNet
+    net = UNet(seed=seed)
+    th = net.theta.detach().cpu().numpy().copy()
+    rng = np.random.default_rng(seed)
+    th[-33:] = rng.normal(0.0, 0.3, 33).astype(np.float32)
+    net.load_state_dict({"theta": th, "step": 0})
+    torch.cuda.synchronize()
+    return net, th
+
+
+def test_unet_parameter_layout_matches_oracle():
+    from stroemung_gb300.unet import UNet
+    net = UNet(seed=0)
+    expected = sum((-(-9 * (-(-ci // 8) * 8) // 64) * 64) * co + co
+                   for ci, co in U.conv_shapes()) + 33
+    assert net.n_params == expected
+    convs, wh, bh = U.unpack(net.theta.detach().cpu().numpy())
+    assert len(convs) == 14 and wh.numel() == 32 and bh.numel() == 1
+    # the head starts at zero, the convolutions He-initialised
+    assert float(wh.abs().max()) == 0.0 and float(convs[0][0].abs().max()) > 0.0
+
+
+def test_prepare_input_matches_oracle():
+    import torch
+    from stroemung_gb300 import warmstart
+    from stroemung_gb300.unet import UNet
+    planes = _planes_from_solver()
+    net = UNet(seed=0)
+    tr = warmstart.Trainer(net, planes.nx, planes.ny, 0.01, 0.01, batch=2)
+    rhs, flags, pprev = (planes.rhs.cpu().numpy(), planes.flags.cpu().numpy(),
+                         planes.p.cpu().numpy())
+    tr.loss(planes, 0)
+    torch.cuda.synchronize()
+    xin_ref, s_ref, mean_ref = U.prepare_input(rhs, flags, pprev, 1e-4)
+    np.testing.assert_allclose(tr.smax.cpu().numpy(), s_ref.numpy(), rtol=1e-6)
+    np.testing.assert_allclose(tr.pmean.cpu().numpy(), mean_ref.numpy(), rtol=1e-4, atol=1e-6)
+    got = tr.xin.float().cpu().numpy()
+    ref = xin_ref.numpy()
+    # one BF16 ulp where the FP32 mean differs in its last bits
+    np.testing.assert_allclose(got, ref, rtol=1e-2, atol=1e-3)
+    assert np.mean(got == ref) > 0.98
+
+
+def test_forward_loss_and_every_gradient_match_oracle():
+    """GPU forward + relative-residual loss + backward (tcgen05 wgrad and
+    dgrad, pooling / upsampling adjoints, head, loss adjoint) vs torch
+    autograd on the same BF16-rounded network.  Tolerances: q and the loss
+    within 2e-2 relative (BF16 activations, different summation order),
+    every layer's weight and bias gradient within a relative L2 tolerance
+    that grows with the layer's distance from the loss (both sides round
+    activation gradients to BF16 where the kernels store them; summation
+    orders and double roundings differ) and cosine > 0.99."""
+    import torch
+    from stroemung_gb300 import warmstart
+    planes = _planes_from_solver()
+    net, theta = _net_with_random_head()
+    tr = warmstart.Trainer(net, planes.nx, planes.ny, 0.01, 0.01, batch=2)
+    rhs, flags, pprev = (planes.rhs.cpu().numpy(), planes.flags.cpu().numpy(),
+                         planes.p.cpu().numpy())
+    loss_gpu, per_gpu = tr.loss(planes, 0)
+    q_gpu = net._bufs[(2, planes.nx - 2, planes.ny - 2)]["q"].cpu().numpy()
+    net.zero_grad()
+    L = net.L
+    net._check(L.strm_nn_residual_loss_grad(tr.r.data_ptr(), planes.flags.data_ptr(),
+                                            tr.sum_b2.data_ptr(), tr.smax.data_ptr(), tr.dx2,
+                                            tr.rdx2, tr.rdy2, tr.gp.data_ptr(), tr.gq.data_ptr(),
+                                            2, planes.nx, planes.ny, None), "loss grad")
+    net.backward(tr.gq, 2, planes.nx - 2, planes.ny - 2)
+    torch.cuda.synchronize()
+    g_gpu = net.grad.cpu().numpy()
+
+    loss_ref, per_ref, q_ref, g_ref = U.loss_and_grads(theta, rhs, flags, pprev, 0.01, 0.01)
+    assert np.linalg.norm(q_gpu - q_ref) <= 2e-2 * np.linalg.norm(q_ref)
+    np.testing.assert_allclose(per_gpu, per_ref, rtol=2e-2)
+    assert abs(loss_gpu - loss_ref) <= 2e-2 * loss_ref
+    # per layer
+    o = 0
+    names = [f"conv{i}.{k}" for i in range(14) for k in ("w", "b")] + ["head.w", "head.b"]
+    sizes = []
+    for ci, co in U.conv_shapes():
+        kp = -(-9 * (-(-ci // 8) * 8) // 64) * 64
+        sizes += [co * kp, co]
+    sizes += [32, 1]
+    stats = []
+    for name, n in zip(names, sizes):
+        a, b = g_gpu[o:o + n].astype(np.float64), g_ref[o:o + n].astype(np.float64)
+        o += n
+        nb = np.linalg.norm(b)
+        assert nb > 0.0, name
+        rel = np.linalg.norm(a - b) / nb
+        cos = float(a @ b / (np.linalg.norm(a) * nb))
+        stats.append((name, round(rel, 4), round(cos, 5)))
+    assert o == g_gpu.size
+    print("per-layer gradient (name, rel L2, cosine):", stats)
+    # BF16 rounding noise grows with the depth of the backward chain (the
+    # head is closest to the loss, conv0 the farthest): 1.5e-2 at the head
+    # end, 8e-2 for the first layers; bias sums of many terms get twice that
+    bad = []
+    for i, (name, rel, cos) in enumerate(stats):
+        depth = (len(stats) - 1 - i) / (len(stats) - 1)  # 0 head .. 1 conv0
+        tol = (1.5e-2 + 6.5e-2 * depth) * (2.0 if name.endswith(".b") else 1.0)
+        if not (rel <= tol and cos >= 0.99):
+            bad.append((name, rel, cos, round(tol, 3)))
+    assert not bad, bad
+
+
+def test_adam_matches_oracle():
+    import torch
+    from stroemung_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(5)
+    n = 10007
+    th = rng.normal(size=n).astype(np.float32)
+    gr = rng.normal(size=n).astype(np.float32)
+    m = rng.normal(size=n).astype(np.float32) * 0.1
+    v = np.abs(rng.normal(size=n)).astype(np.float32) * 0.01
+    t = [torch.tensor(a, device="cuda") for a in (th, gr, m, v)]
+    wbf = torch.empty(n, dtype=torch.bfloat16, device="cuda")
+    assert L.strm_nn_adam(t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), t[3].data_ptr(), n,
+                          1e-3, 0.9, 0.999, 1e-8, 7, wbf.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    th2, m2, v2 = U.adam(th, gr, m, v, 7, 1e-3)
+    np.testing.assert_allclose(t[2].cpu().numpy(), m2, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(t[3].cpu().numpy(), v2, rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(t[0].cpu().numpy(), th2, rtol=1e-6, atol=1e-6)
+    np.testing.assert_array_equal(wbf.float().cpu().numpy(),
+                                  t[0].to(torch.bfloat16).float().cpu().numpy())
+
+
+def test_fluid_norm_excludes_obstacles():
+    """The fluid-cell norm equals the residual sum over fluid cells only; the
+    reference norm includes obstacle cells."""
+    from stroemung_gb300 import presets
+    from stroemung_gb300.simulation import (NORM_ALL_INTERIOR, NORM_FLUID, NORM_FLUID_MEAN_FREE,
+                                            Simulation)
+    grid = presets.channel(48, 24, [(20, 8, 6, 6)])
+    sim = Simulation(grid=grid, cell_size=(0.01, 0.01), delt=0.005, gamma=0.9, reynolds=100.0,
+                     max_iterations=50, tau=0.5)
+    for _ in range(3):
+        sim.run_simulation_tick()
+    sim.copy_pressure_to_boundaries()
+    p, rhs = sim.download("p"), sim.download("rhs")
+    dx2 = 0.01 * 0.01
+    r = ((p[2:, 1:-1] - p[1:-1, 1:-1]) - (p[1:-1, 1:-1] - p[:-2, 1:-1])) / dx2 + \
+        ((p[1:-1, 2:] - p[1:-1, 1:-1]) - (p[1:-1, 1:-1] - p[1:-1, :-2])) / dx2 - rhs[1:-1, 1:-1]
+    fluid = sim._kind[1:-1, 1:-1] == 0
+    nf = float(sim.state()["fluid_cells"])
+    ns_all = sim.calculate_norm_squared()
+    sim.set_mode(norm_cells=NORM_FLUID, strict_eps=True)
+    ns_fluid = sim.calculate_norm_squared()
+    sim.set_mode(norm_cells=NORM_FLUID_MEAN_FREE, strict_eps=True)
+    ns_mf = sim.calculate_norm_squared()
+    np.testing.assert_allclose(ns_all, (r ** 2).sum() / nf, rtol=1e-10)
+    np.testing.assert_allclose(ns_fluid, (r[fluid] ** 2).sum() / nf, rtol=1e-10)
+    rf = r[fluid]
+    np.testing.assert_allclose(ns_mf, ((rf ** 2).sum() - rf.sum() ** 2 / nf) / nf, rtol=1e-9)
+    assert ns_mf <= ns_fluid < ns_all
+    # the residual's fluid sum is -sum(rhs): the Laplacian with the boundary
+    # copy sums to zero over fluid cells
+    np.testing.assert_allclose(rf.sum(), -rhs[1:-1, 1:-1][fluid].sum(),
+                               rtol=1e-6, atol=1e-6 * np.abs(rf).sum())
+    sim.set_mode(norm_cells=NORM_ALL_INTERIOR)
+    sim.close()
+
+
+def test_training_lowers_the_loss():
+    """A few hundred Adam steps on solver snapshots lower the relative
+    residual of the corrected pressure on held-out snapshots."""
+    from stroemung_gb300 import warmstart
+    from stroemung_gb300.unet import UNet
+    train = warmstart.generate_snapshots(256, imax=64, jmax=32, steps_per_problem=16, seed=1,
+                                         max_iterations=300)
+    held = warmstart.generate_snapshots(32, imax=64, jmax=32, steps_per_problem=16, seed=2,
+                                        max_iterations=300)
+    net = UNet(seed=0)
+    tr = warmstart.Trainer(net, 66, 34, 0.01, 0.01, batch=32)
+    before, _ = tr.loss(held, 0)
+    tr.fit(train, epochs=40, lr=1e-3)
+    after, _ = tr.loss(held, 0)
+    assert after < 0.8 * before, (before, after)
