@@ -88,11 +88,11 @@ enum {
 
 /* FP32 sweep schedules of the mixed solve (strm_mode.sweep_schedule). */
 enum {
-    STRM_SWEEPS_DEFAULT = 0,    /* 64 x 64 blocked tiles, 4 sweeps per launch */
+    STRM_SWEEPS_DEFAULT = 0,    /* 48 x 112 blocked tiles, 4 sweeps per launch */
     STRM_SWEEPS_PER_COLOUR = 1, /* one launch per colour pass */
-    /* 2..7: tiles kept in shared memory for several sweeps (temporal
-       blocking): 64x64 by 2, 64x64 by 4, 64x64 by 8, 32x128 by 4,
-       96x96 by 4, 96x96 by 8 sweeps per launch */
+    /* 2..7: tiles (rows x columns) kept in shared memory for several sweeps
+       (temporal blocking): 56x120 by 2, 48x112 by 4, 32x96 by 8, 80x112 by
+       4, 112x112 by 4, 64x96 by 8 sweeps per launch */
     STRM_SWEEPS_COUNT = 8
 };
 
@@ -250,6 +250,30 @@ int strm_calculate_speed_range(strm_sim *sim);     /* src/grid/mod.rs:253-268 */
  * Asynchronous when norm_squared is NULL (see strm_synchronize); otherwise
  * waits and returns the last iteration's norm. */
 int strm_sor_sweeps(strm_sim *sim, int n, double *norm_squared);
+
+/* Batches (no reference counterpart): one CUDA graph steps several
+ * simulations of any sizes and parameters together.  Each member's boundary
+ * pass, F/G/RHS, pressure range and velocity update run as parallel graph
+ * branches; the mixed-precision pressure solves of all members run as one
+ * WHILE loop of table-driven kernels (every blocked sweep launch, refinement
+ * and norm covers all members still solving).  Every member ends exactly
+ * where stepping it alone (strm_tick, same schedule) ends.  Members must use
+ * STRM_PREC_MIXED, a red-black order and graph execution, and have
+ * max_iterations >= inner_sweeps (0 = 16); they stay owned by the caller and
+ * must outlive the batch; their other entry points stay usable between
+ * batch steps (a mode change needs a new batch). */
+typedef struct strm_batch strm_batch;
+int strm_batch_create(strm_sim *const *sims, int n, int inner_sweeps, strm_batch **out);
+int strm_batch_destroy(strm_batch *batch);
+/* n steps of every member, one host synchronisation; stats (may be NULL)
+ * receives n entries per member, member-major. */
+int strm_batch_step(strm_batch *batch, int n, strm_step_stats *stats);
+/* Blocked sweep schedule of the batch (2..STRM_SWEEPS_COUNT-1). */
+int strm_batch_set_schedule(strm_batch *batch, int schedule);
+/* Times `reps` whole batch steps under each blocked schedule (members'
+ * u, v, p and step state restored afterwards), keeps the fastest; best and
+ * ms_per_step[STRM_SWEEPS_COUNT] (per schedule, [0] the best) may be NULL. */
+int strm_batch_autotune(strm_batch *batch, int reps, int *best, double *ms_per_step);
 
 /* Residual history of the last pressure solve: (sweeps done, norm_squared)
  * pairs into out[2*cap], one per norm the solve took (every iteration in

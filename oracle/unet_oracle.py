@@ -88,8 +88,13 @@ def pack_grads(grads_convs, g_wh, g_bh):
     return np.concatenate(out)
 
 
+_EMULATE_BF16 = [True]
+
+
 def _bf(t):
     import torch
+    if not _EMULATE_BF16[0]:
+        return t
     return t.to(torch.bfloat16).to(torch.float32)
 
 
@@ -209,8 +214,19 @@ def loss(q, rhs, flags, pprev, s, dx2, rdx2, rdy2):
     return per.mean(), per
 
 
-def loss_and_grads(theta, rhs, flags, pprev, dx, dy):
-    """Forward + loss + autograd: (loss, per-sample, q, flat gradient)."""
+def loss_and_grads(theta, rhs, flags, pprev, dx, dy, bf16=True):
+    """Forward + loss + autograd: (loss, per-sample, q, flat gradient).
+    bf16=False runs the same network in plain FP32 (no rounding points):
+    the difference between the two measures the BF16 noise of a layer's
+    gradient."""
+    _EMULATE_BF16[0] = bool(bf16)
+    try:
+        return _loss_and_grads(theta, rhs, flags, pprev, dx, dy)
+    finally:
+        _EMULATE_BF16[0] = True
+
+
+def _loss_and_grads(theta, rhs, flags, pprev, dx, dy):
     import torch
     convs, wh, bh = unpack(theta)
     # unpack returns views into one tensor; make them independent leaves

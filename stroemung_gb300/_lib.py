@@ -104,6 +104,12 @@ SIGNATURES = {
     "strm_export_planes": [_vp, _vp, _vp, _vp],
     "strm_autotune_sweeps": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
     "strm_residual_history": [_vp, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+    "strm_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                          ctypes.POINTER(ctypes.c_void_p)],
+    "strm_batch_destroy": [_vp],
+    "strm_batch_step": [_vp, ctypes.c_int, _vp],
+    "strm_batch_set_schedule": [_vp, ctypes.c_int],
+    "strm_batch_autotune": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
     "strm_apply_correction": [_vp, _vp, ctypes.c_double],
     "strm_copy_field_device": [_vp, ctypes.c_int, _vp, ctypes.c_int],
     "strm_render_rgba": [_vp, ctypes.c_int, _u8p],

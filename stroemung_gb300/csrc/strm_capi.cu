@@ -126,7 +126,7 @@ void update_cfg(strm_sim *s) {
   r.arith = s->mode.arithmetic == STRM_ARITH_FAST ? 1 : 0;
   r.precision = s->mode.precision;
   r.inner_sweeps = s->mode.inner_sweeps > 0 ? s->mode.inner_sweeps : 16;
-  // public schedule numbers: 0 default (64 x 64 tiles, 4 sweeps per launch),
+  // public schedule numbers: 0 default (48 x 112 tiles, 4 sweeps per launch),
   // 1 one launch per colour pass, 2.. the blocked tile shapes
   r.sweep_schedule = s->mode.sweep_schedule == 0 ? 2 : s->mode.sweep_schedule - 1;
   r.eager = s->mode.execution == STRM_EXEC_EAGER ? 1 : 0;
@@ -684,6 +684,205 @@ int strm_copy_field_device(strm_sim *s, int field, double *dense, int to_sim) {
                          cudaMemcpyDeviceToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return STRM_OK;
+}
+
+// ------------------------------------------------------------------------
+// Batches
+// ------------------------------------------------------------------------
+
+struct strm_batch {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<strm_sim *> sims;
+  int schedule = 0;     // public sweep schedule number (2..)
+  int inner = 16;
+  BatchPlan plan{};
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int batch_rebuild(strm_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  free_batch(&b->plan);
+  std::vector<BatchMember> mem;
+  for (strm_sim *s : b->sims) mem.push_back(BatchMember{s->d, s->cfg});
+  cudaError_t e = build_batch(mem, b->schedule - 1, b->inner, &b->plan);
+  if (e == cudaErrorInvalidValue)
+    return fail(STRM_ERR_INVALID, "a batch member has max_iterations below the inner sweeps");
+  CK(e);
+  CK(cudaGraphInstantiate(&b->exec, b->plan.graph, 0));
+  return STRM_OK;
+}
+
+}  // namespace
+
+int strm_batch_create(strm_sim *const *sims, int n, int inner_sweeps, strm_batch **out) {
+  if (!sims || n < 1 || !out || inner_sweeps < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
+  *out = nullptr;
+  const int dev = sims[0] ? sims[0]->dev : 0;
+  for (int i = 0; i < n; ++i) {
+    strm_sim *s = sims[i];
+    if (!s) return fail(STRM_ERR_INVALID, "sims[%d] is NULL", i);
+    for (int j = 0; j < i; ++j)
+      if (sims[j] == s) return fail(STRM_ERR_INVALID, "sims[%d] repeats sims[%d]", i, j);
+    if (s->dev != dev) return fail(STRM_ERR_INVALID, "batch members must share a device");
+    if (s->cfg.precision != 1 || s->cfg.sor_order != 0 || s->cfg.eager)
+      return fail(STRM_ERR_INVALID, "batch members need mixed precision, red-black order and "
+                                    "graph execution (sims[%d])", i);
+  }
+  CK(cudaSetDevice(dev));
+  strm_batch *b = new strm_batch();
+  b->dev = dev;
+  b->sims.assign(sims, sims + n);
+  b->inner = inner_sweeps > 0 ? inner_sweeps : 16;
+  b->schedule = 3;  // 48 x 112 tiles, 4 sweeps per launch
+  int rc = STRM_OK;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(STRM_ERR_CUDA, "cudaStreamCreate failed");
+  if (rc == STRM_OK) rc = batch_rebuild(b);
+  if (rc != STRM_OK) {
+    strm_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return STRM_OK;
+}
+
+int strm_batch_destroy(strm_batch *b) {
+  if (!b) return STRM_OK;
+  cudaSetDevice(b->dev);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  free_batch(&b->plan);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return STRM_OK;
+}
+
+int strm_batch_set_schedule(strm_batch *b, int schedule) {
+  if (!b || schedule < 2 || schedule > num_sweep_schedules())
+    return fail(STRM_ERR_INVALID, "batches take the blocked schedules 2..%d",
+                num_sweep_schedules());
+  CK(cudaSetDevice(b->dev));
+  CK(cudaStreamSynchronize(b->stream));
+  b->schedule = schedule;
+  return batch_rebuild(b);
+}
+
+int strm_batch_step(strm_batch *b, int n, strm_step_stats *stats) {
+  if (!b || n < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
+  if (n > kLogCap) return fail(STRM_ERR_INVALID, "at most %d steps per call", kLogCap);
+  CK(cudaSetDevice(b->dev));
+  const unsigned int zero = 0;
+  // the members' own streams may hold work (uploads, edits): order after it
+  for (strm_sim *s : b->sims) {
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  }
+  CK(cudaMemsetAsync((char *)b->plan.state + kBatchOverrunOffset, 0, sizeof(unsigned int),
+                     b->stream));
+  for (int i = 0; i < n; ++i) CK(cudaGraphLaunch(b->exec, b->stream));
+  unsigned int overrun = 0;
+  CK(cudaMemcpyAsync(&overrun, (char *)b->plan.state + kBatchOverrunOffset, sizeof overrun,
+                     cudaMemcpyDeviceToHost, b->stream));
+  const int ns = (int)b->sims.size();
+  for (int k = 0; k < ns; ++k) {
+    strm_sim *s = b->sims[k];
+    CK(cudaMemcpyAsync(s->h_st, s->d.st, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    if (stats && n > 0)
+      CK(cudaMemcpyAsync(s->h_log, s->d.log, sizeof(StepLog) * n, cudaMemcpyDeviceToHost,
+                         b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (stats)
+      for (int i = 0; i < n; ++i) {
+        strm_step_stats &o = stats[(size_t)k * n + i];
+        o.sor_iterations = s->h_log[i].sor_iters;
+        o.converged = s->h_log[i].converged;
+        o.norm_squared = s->h_log[i].ns;
+        o.delt = s->h_log[i].dt;
+      }
+  }
+  if (overrun) return fail(STRM_ERR_TIMEOUT, "batch pressure loop passed its bound");
+  for (strm_sim *s : b->sims)
+    if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return STRM_OK;
+}
+
+int strm_batch_autotune(strm_batch *b, int reps, int *best, double *ms_per_step) {
+  if (!b || reps < 1) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(b->dev));
+  // times whole batch steps under every blocked schedule on copies of the
+  // members' state, then restores it: the members end where they started
+  std::vector<std::vector<char>> saved(b->sims.size());
+  std::vector<void *> dsave(b->sims.size(), nullptr);
+  size_t k = 0;
+  for (strm_sim *s : b->sims) {
+    size_t bytes = 0;
+    CK(cudaStreamSynchronize(s->stream));
+    const size_t nfield = (size_t)s->g.nx * s->g.pitch;
+    bytes = nfield * 8 * 3 + sizeof(StepState);
+    CK(cudaMalloc(&dsave[k], bytes));
+    char *d = (char *)dsave[k];
+    CK(cudaMemcpy(d, s->d.u, nfield * 8, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(d + nfield * 8, s->d.v, nfield * 8, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(d + 2 * nfield * 8, s->d.p, nfield * 8, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(d + 3 * nfield * 8, s->d.st, sizeof(StepState), cudaMemcpyDeviceToDevice));
+    ++k;
+  }
+  auto restore = [&]() -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    size_t i = 0;
+    for (strm_sim *s : b->sims) {
+      const size_t nfield = (size_t)s->g.nx * s->g.pitch;
+      const char *d = (const char *)dsave[i++];
+      if (e == cudaSuccess) e = cudaMemcpy(s->d.u, d, nfield * 8, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(s->d.v, d + nfield * 8, nfield * 8, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(s->d.p, d + 2 * nfield * 8, nfield * 8, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(s->d.st, d + 3 * nfield * 8, sizeof(StepState), cudaMemcpyDeviceToDevice);
+    }
+    return e;
+  };
+  cudaEvent_t ev[2];
+  cudaEventCreate(&ev[0]);
+  cudaEventCreate(&ev[1]);
+  int best_v = b->schedule;
+  double best_t = -1.0;
+  int rc = STRM_OK;
+  for (int v = 2; v <= num_sweep_schedules() && rc == STRM_OK; ++v) {
+    b->schedule = v;
+    rc = batch_rebuild(b);
+    if (rc != STRM_OK) break;
+    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], b->stream);
+    for (int i = 0; i < reps && e == cudaSuccess; ++i) e = cudaGraphLaunch(b->exec, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    if (e == cudaSuccess) e = restore();
+    if (e != cudaSuccess) {
+      rc = fail(STRM_ERR_CUDA, "CUDA error %s", cudaGetErrorString(e));
+      break;
+    }
+    const double per = (double)ms / reps;
+    if (ms_per_step) ms_per_step[v] = per;
+    if (best_t < 0.0 || per < best_t) {
+      best_t = per;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  for (void *d : dsave) cudaFree(d);
+  if (rc != STRM_OK) return rc;
+  if (ms_per_step) ms_per_step[0] = best_t;
+  if (best) *best = best_v;
+  b->schedule = best_v;
+  return batch_rebuild(b);
 }
 
 int strm_residual_history(strm_sim *s, double *out, int cap, int *n) {

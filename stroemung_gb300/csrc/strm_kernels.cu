@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(256)
         const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
                                             p[o + 1], rhs[o], c);
         acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
-        acc1 += r;
+        if (mean_free) acc1 += r;
       }
     }
   }
@@ -771,35 +771,57 @@ __global__ void __launch_bounds__(256)
 }
 
 // Temporal blocking of the same sweeps: one CTA loads a TX x TY tile of the
-// correction with an H-cell halo (and the defect and flags) into shared
+// correction with an H-cell halo (and the defect and cell codes) into shared
 // memory, runs `n` red-black sweeps there (2n colour passes, n <= H/2; the
 // region that is still exact shrinks by one cell per pass) and writes the
 // tile back.  Reads come from `ein`, writes go to `eout` (another buffer:
-// neighbouring CTAs read this tile's cells as their halo).  Each cell sees
-// exactly the arithmetic of sor32_color_kernel in the same colour order, so
-// the result is bit-identical to n x (red, black) of that kernel.  The last
-// black pass skips its boundary copy when skip_last_copy is set.
+// neighbouring CTAs read this tile's cells as their halo).
+//
+// Shared memory holds each colour compacted: row lx of colour c keeps the
+// cells y = 2j + ((lx + c) & 1), j = 0 .. EY/2-1 (tile origins are even, so
+// local and global colours agree).  A colour-c cell (lx, j) then finds its
+// four neighbours in the other colour at (lx-1, j), (lx+1, j), (lx, j-1+p)
+// and (lx, j+p), p = (lx + c) & 1: consecutive lanes touch consecutive
+// words, no bank conflicts, every lane busy.  Each cell sees exactly the
+// arithmetic of sor32_color_kernel in the same colour order, so the result
+// is bit-identical to n x (red, black) of that kernel.  The last black pass
+// skips its boundary copy when skip_last_copy is set.
 constexpr uint8_t kFrozen = 0xFF;  // cell code: never written (outside, edge-less boundary)
 
+__device__ __forceinline__ float copy_rb(int code, float up, float dn, float lf, float rt) {
+  switch (code) {
+    case E_N: return lf;
+    case E_NE: return (lf + dn) * 0.5f;
+    case E_E: return dn;
+    case E_SE: return (rt + dn) * 0.5f;
+    case E_S: return rt;
+    case E_SW: return (rt + up) * 0.5f;
+    case E_W: return up;
+    default: return (lf + up) * 0.5f;  // E_NW
+  }
+}
+
 template <int H, int TX, int TY>
-__global__ void __launch_bounds__(512)
-    sor32_tb_kernel(const float *__restrict__ ein, float *__restrict__ eout,
-                    const float *__restrict__ s, const uint8_t *__restrict__ flags, Geom g,
-                    Consts32 k, int tiles_y, int n, int skip_last_copy) {
-  constexpr int EX = TX + 2 * H, EY = TY + 2 * H, NC = EX * EY;
+__device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
+                                              float *__restrict__ eout,
+                                              const float *__restrict__ s,
+                                              const uint8_t *__restrict__ flags, const Geom &g,
+                                              const Consts32 &k, int tile, int tiles_y, int n,
+                                              int skip_last_copy, unsigned char *smem_raw) {
+  static_assert(H % 2 == 0 && TX % 2 == 0 && TY % 2 == 0, "tile origins must be even");
+  constexpr int EX = TX + 2 * H, EY = TY + 2 * H, W = EY / 2, NC = EX * W;
   constexpr int WARPS = 16;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *se = reinterpret_cast<float *>(smem_raw);
-  float *ss = se + NC;
-  uint8_t *sc = reinterpret_cast<uint8_t *>(ss + NC);  // 0 SOR, 1..8 copy edge, kFrozen
-  const int gx0 = (int)(blockIdx.x / tiles_y) * TX - H;
-  const int gy0 = (int)(blockIdx.x % tiles_y) * TY - H;
+  float *se = reinterpret_cast<float *>(smem_raw);  // [2][EX][W]
+  float *ss = se + 2 * NC;                            // [2][EX][W]
+  uint8_t *sc = reinterpret_cast<uint8_t *>(ss + 2 * NC);  // [2][EX][W]: 0 SOR, 1..8 copy, kFrozen
+  const int gx0 = (tile / tiles_y) * TX - H;
+  const int gy0 = (tile % tiles_y) * TY - H;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int lx = warp; lx < EX; lx += WARPS) {
     const int x = gx0 + lx;
     for (int ly = lane; ly < EY; ly += 32) {
       const int y = gy0 + ly;
-      const int i = lx * EY + ly;
+      const int i = ((lx + ly) & 1) * NC + lx * W + (ly >> 1);
       float ev = 0.0f, sv = 0.0f;
       uint8_t code = kFrozen;
       if (x >= 0 && y >= 0 && x < g.nx && y < g.ny) {
@@ -820,21 +842,26 @@ __global__ void __launch_bounds__(512)
   }
   __syncthreads();
   for (int pass = 0; pass < 2 * n; ++pass) {
-    const int color = pass & 1;
+    const int c = pass & 1;
     const bool copy = !(skip_last_copy && pass == 2 * n - 1);
     const int lo = pass + 1, hix = EX - 2 - pass, hiy = EY - 2 - pass;
+    float *ec = se + c * NC;
+    const float *eo = se + (1 - c) * NC;
+    const float *sv = ss + c * NC;
+    const uint8_t *cc = sc + c * NC;
     for (int lx = lo + warp; lx <= hix; lx += WARPS) {
-      // first column of the colour in this row: (x + y) & 1 == color
-      const int ly0 = lo + ((gx0 + lx + gy0 + lo + color) & 1);
-      for (int ly = ly0 + 2 * lane; ly <= hiy; ly += 64) {
-        const int li = lx * EY + ly;
-        const uint8_t code = sc[li];
+      const int p = (lx + c) & 1;
+      const int jlo = (lo - p + 1) >> 1, jhi = (hiy - p) >> 1;
+      const int row = lx * W;
+      for (int j = jlo + lane; j <= jhi; j += 32) {
+        const int i = row + j;
+        const uint8_t code = cc[i];
         if (code == 0) {
-          const float sum_x = se[li - EY] + se[li + EY];
-          const float sum_y = se[li - 1] + se[li + 1];
-          se[li] = fmaf(k.omw, se[li], fmaf(k.a, sum_x, fmaf(k.b, sum_y, ss[li])));
+          const float sum_x = eo[i - W] + eo[i + W];
+          const float sum_y = eo[i - 1 + p] + eo[i + p];
+          ec[i] = fmaf(k.omw, ec[i], fmaf(k.a, sum_x, fmaf(k.b, sum_y, sv[i])));
         } else if (copy && code != kFrozen) {
-          se[li] = ss[li] + copy32(se, (size_t)li, EY, code);
+          ec[i] = sv[i] + copy_rb(code, eo[i - W], eo[i + W], eo[i - 1 + p], eo[i + p]);
         }
       }
     }
@@ -845,19 +872,29 @@ __global__ void __launch_bounds__(512)
     if (x >= g.nx) break;
     for (int ly = H + lane; ly < H + TY; ly += 32) {
       const int y = gy0 + ly;
-      if (y < g.ny) eout[OFF(x, y)] = se[lx * EY + ly];
+      if (y < g.ny) eout[OFF(x, y)] = se[((lx + ly) & 1) * NC + lx * W + (ly >> 1)];
     }
   }
+}
+
+template <int H, int TX, int TY>
+__global__ void __launch_bounds__(512)
+    sor32_tb_kernel(const float *__restrict__ ein, float *__restrict__ eout,
+                    const float *__restrict__ s, const uint8_t *__restrict__ flags, Geom g,
+                    Consts32 k, int tiles_y, int n, int skip_last_copy) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  sor32_tb_tile<H, TX, TY>(ein, eout, s, flags, g, k, (int)blockIdx.x, tiles_y, n,
+                           skip_last_copy, smem_raw);
 }
 
 // p += e on fluid interior cells and boundary cells with an edge (apply != 0),
 // then ez = 0 everywhere (the buffer the next sweeps start from; e itself
 // when the sweeps ended where they started).
-__global__ void __launch_bounds__(256)
-    refine_kernel(double *__restrict__ p, const float *e, float *ez,
-                  const uint8_t *__restrict__ flags, Geom g, int apply) {
-  const int x = blockIdx.y * blockDim.y + threadIdx.y;
-  const int y0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void refine_cells(double *__restrict__ p, const float *e, float *ez,
+                                             const uint8_t *__restrict__ flags, const Geom &g,
+                                             int apply, int bx, int by) {
+  const int x = by * blockDim.y + threadIdx.y;
+  const int y0 = 2 * (bx * blockDim.x + threadIdx.x);
   if (x >= g.nx) return;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
@@ -872,16 +909,19 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+__global__ void __launch_bounds__(256)
+    refine_kernel(double *__restrict__ p, const float *e, float *ez,
+                  const uint8_t *__restrict__ flags, Geom g, int apply) {
+  refine_cells(p, e, ez, flags, g, apply, blockIdx.x, blockIdx.y);
+}
+
 // delta_b = copy(p) - p_b on boundary cells with an edge (FP64, stored FP32
 // in s and as the starting correction e_b).
-__global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s,
-                             float *__restrict__ e, const PCopy *__restrict__ pc, int n,
-                             int pitch) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const long long o = pc[k].off;
+__device__ __forceinline__ void delta_entry(const double *__restrict__ p, float *__restrict__ s,
+                                            float *__restrict__ e, const PCopy &pc, int pitch) {
+  const long long o = pc.off;
   double c;
-  switch (pc[k].edge) {
+  switch (pc.edge) {
     case E_N: c = p[o - 1]; break;
     case E_NE: c = (p[o - 1] + p[o + pitch]) * 0.5; break;
     case E_E: c = p[o + pitch]; break;
@@ -896,20 +936,26 @@ __global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s
   e[o] = d;
 }
 
+__global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s,
+                             float *__restrict__ e, const PCopy *__restrict__ pc, int n,
+                             int pitch) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  delta_entry(p, s, e, pc[k], pitch);
+}
+
 // FP64 norm of the residual on every interior cell (the reference's norm),
 // the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
-// and the stop rule every m sweeps.
-template <bool IN_GRAPH>
-__global__ void __launch_bounds__(256)
-    mixed_residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
-                          const uint8_t *__restrict__ flags, float *__restrict__ s, Geom g,
-                          Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
-                          cudaGraphConditionalHandle h, unsigned int itermax, int strict,
-                          int sweeps, int check) {
+// and the stop rule every m sweeps.  Block `bid` of `nblocks` sums its tiles
+// into partials[bid] (interleaved with the residual sum when mean-free).
+__device__ __forceinline__ void mixed_residual_partial(
+    const double *__restrict__ p, const double *__restrict__ rhs,
+    const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
+    double *partials, int tiles_y, int ntiles, int strict, int bid, int nblocks) {
   const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
   const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
   double acc = 0.0, acc1 = 0.0;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  for (int t = bid; t < ntiles; t += nblocks) {
     const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
     if (x > g.nx - 2) continue;
     const int yb = 1 + (t % tiles_y) * RT_Y + 2 * threadIdx.x;
@@ -923,7 +969,7 @@ __global__ void __launch_bounds__(256)
         const bool fluid = flags[o] == 0;
         if (fluid || !fluid_only) {
           acc = fma(r, r, acc);
-          acc1 += r;
+          if (mean_free) acc1 += r;
         }
         if (fluid) s[o] = (float)(c.middle * r);
       }
@@ -933,24 +979,25 @@ __global__ void __launch_bounds__(256)
   if (mean_free) {
     const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-      partials[2 * blockIdx.x] = bsum;
-      partials[2 * blockIdx.x + 1] = bsum1;
+      partials[2 * bid] = bsum;
+      partials[2 * bid + 1] = bsum1;
     }
   } else if (threadIdx.x == 0 && threadIdx.y == 0) {
-    partials[blockIdx.x] = bsum;
+    partials[bid] = bsum;
   }
-  if (IN_GRAPH && check && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-    // independent bound on the WHILE loop, as in residual_kernel
-    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
-    if ((unsigned long long)launches * (unsigned long long)sweeps >= itermax + 2ull * sweeps) {
-      st->overrun = 1;
-      cudaGraphSetConditional(h, 0);
-    }
-  }
-  if (!last_block_done(&st->counter)) return;
-  const double ns = finish_norm(partials, gridDim.x, mean_free, st->fluid_cells);
+}
+
+// The norm from the partials and the stop rule (every thread of one block
+// calls it; thread 0 updates the state).  Returns, in thread 0, whether the
+// solve goes on.
+__device__ __forceinline__ bool mixed_residual_stop(const double *partials, int nblocks,
+                                                    StepState *st, const Consts &c,
+                                                    unsigned int itermax, int strict, int sweeps,
+                                                    int check) {
+  const bool mean_free = (strict & STOP_FLUID_NORM) && (strict & STOP_MEAN_FREE);
+  const double ns = finish_norm(partials, nblocks, mean_free, st->fluid_cells);
+  bool go_on = true;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    st->counter = 0;
     st->ns = ns;
     hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
     if (check) {
@@ -961,8 +1008,35 @@ __global__ void __launch_bounds__(256)
       const bool room = it + sweeps <= itermax;
       if (done) st->converged = 1;
       else if (!room) st->exhausted = 1;
-      if (IN_GRAPH && (done || !room)) cudaGraphSetConditional(h, 0);
+      go_on = !(done || !room);
     }
+  }
+  return go_on;
+}
+
+template <bool IN_GRAPH>
+__global__ void __launch_bounds__(256)
+    mixed_residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
+                          const uint8_t *__restrict__ flags, float *__restrict__ s, Geom g,
+                          Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
+                          cudaGraphConditionalHandle h, unsigned int itermax, int strict,
+                          int sweeps, int check) {
+  mixed_residual_partial(p, rhs, flags, s, g, c, partials, tiles_y, ntiles, strict, blockIdx.x,
+                         gridDim.x);
+  if (IN_GRAPH && check && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    // independent bound on the WHILE loop, as in residual_kernel
+    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
+    if ((unsigned long long)launches * (unsigned long long)sweeps >= itermax + 2ull * sweeps) {
+      st->overrun = 1;
+      cudaGraphSetConditional(h, 0);
+    }
+  }
+  if (!last_block_done(&st->counter)) return;
+  const bool go_on = mixed_residual_stop(partials, gridDim.x, st, c, itermax, strict, sweeps,
+                                         check);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    if (IN_GRAPH && check && !go_on) cudaGraphSetConditional(h, 0);
   }
 }
 
@@ -1116,12 +1190,12 @@ struct TbShape {
 
 static const TbShape kTbShapes[] = {
     {0, 0, 0, 1, nullptr},
-    {4, 64, 64, 2, (const void *)sor32_tb_kernel<4, 64, 64>},
-    {8, 64, 64, 4, (const void *)sor32_tb_kernel<8, 64, 64>},
-    {16, 64, 64, 8, (const void *)sor32_tb_kernel<16, 64, 64>},
-    {8, 32, 128, 4, (const void *)sor32_tb_kernel<8, 32, 128>},
-    {8, 96, 96, 4, (const void *)sor32_tb_kernel<8, 96, 96>},
-    {16, 96, 96, 8, (const void *)sor32_tb_kernel<16, 96, 96>},
+    {4, 56, 120, 2, (const void *)sor32_tb_kernel<4, 56, 120>},
+    {8, 48, 112, 4, (const void *)sor32_tb_kernel<8, 48, 112>},
+    {16, 32, 96, 8, (const void *)sor32_tb_kernel<16, 32, 96>},
+    {8, 80, 112, 4, (const void *)sor32_tb_kernel<8, 80, 112>},
+    {8, 112, 112, 4, (const void *)sor32_tb_kernel<8, 112, 112>},
+    {16, 64, 96, 8, (const void *)sor32_tb_kernel<16, 64, 96>},
 };
 constexpr int kNumSchedules = (int)(sizeof(kTbShapes) / sizeof(kTbShapes[0]));
 
@@ -1514,7 +1588,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
   const int nb = residual_blocks(g);
 
   cudaGraphNode_t n = nullptr;
-  if (part != 2) {
+  if (part != 2 && part != 3) {
     n = b.kernel(b.graph, nullptr, (const void *)bc_kernel, dim3(BC_CLUSTER), dim3(BC_THREADS),
                  d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc, d.bc_val, d.n_bc, d.st, c, r.tau,
                  r.delt, r.itermax, 1);
@@ -1523,8 +1597,9 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                  (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
                  (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
   }
-  if (part == 1) {
-    // the first half of a step ends after the RHS
+  if (part == 1 || part == 3) {
+    // the first half of a step ends after the RHS; part 3 is the second
+    // half without the pressure solve (run by a batch)
   } else if (r.sor_order == 1) {
     n = b.kernel(b.graph, n, (const void *)sor_lex_kernel, dim3(1), dim3(1024), d.p,
                  (const double *)d.rhs, (const uint8_t *)d.flags, (const PCopy *)d.pcopy,
@@ -1630,4 +1705,335 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
   return cudaSuccess;
 }
 
+
+// ------------------------------------------------------------------------
+// Batches: many independent simulations stepped by one graph.  Each
+// instance's boundary pass, F/G/RHS, pressure range and velocity update are
+// its own kernels (parallel branches of the graph); the mixed-precision
+// pressure solve of all instances is one WHILE loop whose kernels cover
+// every instance through tables of (instance, block / tile / entry) pairs,
+// skip instances whose solve has stopped, and run each instance's work with
+// exactly its single-instance block shapes and reduction order, so every
+// instance ends bit-identical to a run of its own.
+// ------------------------------------------------------------------------
+
+struct BInst {
+  double *p, *rhs;
+  const uint8_t *flags;
+  float *e32, *e32b, *r32;
+  StepState *st;
+  double *partials;
+  const PCopy *pcopy;
+  Geom g;
+  Consts c;
+  Consts32 k32;
+  unsigned int itermax;
+  int strict;
+  int solve;             // 0: no pressure solve (no interior or max_iterations 0)
+  int nb, ty_int, nt_int;
+  int pgx;               // refine grid width (blocks)
+  int tb_tiles_y;
+};
+
+struct BatchState {
+  unsigned int counter;
+  unsigned int active;
+  unsigned int body_count;
+  unsigned int overrun;
+  unsigned int launches;  // independent count of loop bodies (block 0)
+};
+
+__device__ __forceinline__ bool inst_stopped(const StepState *st) {
+  return st->converged || st->exhausted;
+}
+
+__global__ void __launch_bounds__(256)
+    batch_refine_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int apply,
+                        int final_b) {
+  const int2 e = tab[blockIdx.x];
+  const BInst &b = I[e.x];
+  if (!b.solve || (apply && inst_stopped(b.st))) return;
+  refine_cells(b.p, final_b ? b.e32b : b.e32, b.e32, b.flags, b.g, apply, e.y % b.pgx,
+               e.y / b.pgx);
+}
+
+__global__ void batch_delta_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab,
+                                   int n, int check) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int2 e = tab[k];
+  const BInst &b = I[e.x];
+  if (!b.solve || (check && inst_stopped(b.st))) return;
+  delta_entry(b.p, b.r32, b.e32, b.pcopy[e.y], b.g.pitch);
+}
+
+template <int H, int TX, int TY>
+__global__ void __launch_bounds__(512)
+    batch_tb_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int n,
+                    int skip_last_copy, int src_b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 e = tab[blockIdx.x];
+  const BInst &b = I[e.x];
+  if (!b.solve || inst_stopped(b.st)) return;
+  sor32_tb_tile<H, TX, TY>(src_b ? b.e32b : b.e32, src_b ? b.e32 : b.e32b, b.r32, b.flags, b.g,
+                           b.k32, e.y, b.tb_tiles_y, n, skip_last_copy, smem_raw);
+}
+
+__global__ void __launch_bounds__(256)
+    batch_residual_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int check) {
+  const int2 e = tab[blockIdx.x];
+  const BInst &b = I[e.x];
+  if (!b.solve || (check && inst_stopped(b.st))) return;
+  mixed_residual_partial(b.p, b.rhs, b.flags, b.r32, b.g, b.c, b.partials, b.ty_int, b.nt_int,
+                         b.strict, e.y, b.nb);
+}
+
+// One block per instance: its norm and stop rule; the last block to finish
+// ends the WHILE loop once no instance goes on, or when the loop passes its
+// bound (max max_iterations / sweeps + 2 launches).
+__global__ void __launch_bounds__(256)
+    batch_finish_kernel(const BInst *__restrict__ I, int n, BatchState *bs,
+                        cudaGraphConditionalHandle h, int sweeps, int check,
+                        unsigned int itermax_all) {
+  const BInst &b = I[blockIdx.x];
+  const bool active = b.solve && !(check && inst_stopped(b.st));
+  if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    // Independent bound on the WHILE loop: the normal stop below ends it
+    // after max max_iterations / sweeps bodies at the latest; should that
+    // bookkeeping ever fail, this ends it two bodies later.
+    if (!check) {
+      bs->launches = 0;
+    } else {
+      const unsigned int l = atomicAdd(&bs->launches, 1u) + 1;
+      if ((unsigned long long)l * sweeps >= itermax_all + 2ull * sweeps) {
+        bs->overrun = 1;
+        cudaGraphSetConditional(h, 0);
+      }
+    }
+  }
+  __syncthreads();
+  bool go_on = false;
+  if (active)
+    go_on = mixed_residual_stop(b.partials, b.nb, b.st, b.c, b.itermax, b.strict, sweeps, check);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (active && go_on) atomicAdd(&bs->active, 1u);
+    __threadfence();
+    const unsigned int t = atomicAdd(&bs->counter, 1u);
+    if (t == (unsigned int)n - 1) {
+      __threadfence();
+      const unsigned int act = atomicAdd(&bs->active, 0u);
+      if (check) {
+        const unsigned int body = bs->body_count + 1;
+        bs->body_count = body;
+        if (act == 0) {
+          cudaGraphSetConditional(h, 0);
+        } else if ((unsigned long long)body * sweeps >= itermax_all + 2ull * sweeps) {
+          bs->overrun = 1;
+          cudaGraphSetConditional(h, 0);
+        }
+      } else {
+        bs->body_count = 0;
+      }
+      bs->active = 0;
+      bs->counter = 0;
+    }
+  }
+}
+
+static const void *batch_tb_fn(int sched) {
+  switch (sched) {
+    case 1: return (const void *)batch_tb_kernel<4, 56, 120>;
+    case 2: return (const void *)batch_tb_kernel<8, 48, 112>;
+    case 3: return (const void *)batch_tb_kernel<16, 32, 96>;
+    case 4: return (const void *)batch_tb_kernel<8, 80, 112>;
+    case 5: return (const void *)batch_tb_kernel<8, 112, 112>;
+    case 6: return (const void *)batch_tb_kernel<16, 64, 96>;
+    default: return nullptr;
+  }
+}
+
+void free_batch(BatchPlan *bp) {
+  if (bp->graph) cudaGraphDestroy(bp->graph);
+  if (bp->dev) cudaFree(bp->dev);
+  bp->graph = nullptr;
+  bp->dev = nullptr;
+  bp->state = nullptr;
+}
+
+cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp) {
+  *bp = BatchPlan{};
+  const int n = (int)mem.size();
+  if (n < 1 || m < 1 || sched < 1 || sched >= kNumSchedules) return cudaErrorInvalidValue;
+  cudaError_t e = tb_prepare();
+  if (e != cudaSuccess) return e;
+  for (int s2 = 1; s2 < kNumSchedules; ++s2) {
+    e = cudaFuncSetAttribute(batch_tb_fn(s2), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tb_smem(kTbShapes[s2]));
+    if (e != cudaSuccess) return e;
+  }
+  const TbShape &shape = kTbShapes[sched];
+  std::vector<BInst> inst(n);
+  std::vector<int2> t_res, t_ref, t_del, t_tb;
+  unsigned int itermax_all = 0;
+  for (int i = 0; i < n; ++i) {
+    const DevFields &d = mem[i].d;
+    const RunCfg &r = mem[i].r;
+    BInst &b = inst[i];
+    b.p = d.p;
+    b.rhs = d.rhs;
+    b.flags = d.flags;
+    b.e32 = d.e32;
+    b.e32b = d.e32b;
+    b.r32 = d.r32;
+    b.st = d.st;
+    b.partials = d.partials;
+    b.pcopy = d.pcopy;
+    b.g = r.g;
+    b.c = r.c;
+    b.k32 = consts32_of(r.c);
+    b.itermax = r.itermax;
+    b.strict = r.strict_eps;
+    int ty_int, nt_int;
+    tiles_of(r.g, 1, &ty_int, &nt_int);
+    b.solve = (nt_int > 0 && r.itermax > 0) ? 1 : 0;
+    b.nb = residual_blocks(r.g);
+    b.ty_int = ty_int;
+    b.nt_int = nt_int;
+    b.pgx = (r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x;
+    const int pgy = (r.g.nx + kRedBlock.y - 1) / kRedBlock.y;
+    b.tb_tiles_y = (r.g.ny + shape.ty - 1) / shape.ty;
+    const int tb_tiles_x = (r.g.nx + shape.tx - 1) / shape.tx;
+    if (!b.solve) continue;
+    if (r.itermax < (unsigned int)m) return cudaErrorInvalidValue;
+    if (r.itermax > itermax_all) itermax_all = r.itermax;
+    for (int k = 0; k < b.nb; ++k) t_res.push_back(make_int2(i, k));
+    for (int k = 0; k < b.pgx * pgy; ++k) t_ref.push_back(make_int2(i, k));
+    for (int k = 0; k < d.n_pcopy; ++k) t_del.push_back(make_int2(i, k));
+    for (int k = 0; k < b.tb_tiles_y * tb_tiles_x; ++k) t_tb.push_back(make_int2(i, k));
+  }
+  // device tables: instances, the four block tables, the batch state
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_inst = 0, o_res = o_inst + al(sizeof(BInst) * n);
+  const size_t o_ref = o_res + al(sizeof(int2) * (t_res.size() + 1));
+  const size_t o_del = o_ref + al(sizeof(int2) * (t_ref.size() + 1));
+  const size_t o_tb = o_del + al(sizeof(int2) * (t_del.size() + 1));
+  const size_t o_bs = o_tb + al(sizeof(int2) * (t_tb.size() + 1));
+  const size_t total = o_bs + al(sizeof(BatchState));
+  char *dev = nullptr;
+  if ((e = cudaMalloc(&dev, total)) != cudaSuccess) return e;
+  bp->dev = dev;
+  const BInst *d_inst = (const BInst *)(dev + o_inst);
+  const int2 *d_res = (const int2 *)(dev + o_res), *d_ref = (const int2 *)(dev + o_ref);
+  const int2 *d_del = (const int2 *)(dev + o_del), *d_tb = (const int2 *)(dev + o_tb);
+  BatchState *d_bs = (BatchState *)(dev + o_bs);
+  bp->state = d_bs;
+  e = cudaMemset(dev, 0, total);
+  if (e == cudaSuccess) e = cudaMemcpy(dev + o_inst, inst.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !t_res.empty())
+    e = cudaMemcpy(dev + o_res, t_res.data(), sizeof(int2) * t_res.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !t_ref.empty())
+    e = cudaMemcpy(dev + o_ref, t_ref.data(), sizeof(int2) * t_ref.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !t_del.empty())
+    e = cudaMemcpy(dev + o_del, t_del.data(), sizeof(int2) * t_del.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !t_tb.empty())
+    e = cudaMemcpy(dev + o_tb, t_tb.data(), sizeof(int2) * t_tb.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    free_batch(bp);
+    return e;
+  }
+
+  GraphBuilder b;
+  if ((e = cudaGraphCreate(&b.graph, 0)) != cudaSuccess) {
+    free_batch(bp);
+    return e;
+  }
+  b.store.reserve(64);
+  // per-instance first halves, in parallel
+  std::vector<cudaGraphNode_t> pre(n, nullptr);
+  for (int i = 0; i < n && b.err == cudaSuccess; ++i) {
+    cudaGraph_t child = nullptr;
+    b.err = build_step_graph(mem[i].d, mem[i].r, &child, 1);
+    if (b.err == cudaSuccess) {
+      b.err = cudaGraphAddChildGraphNode(&pre[i], b.graph, nullptr, 0, child);
+      cudaGraphDestroy(child);
+    }
+  }
+  cudaGraphNode_t nd = nullptr;
+  if (b.err == cudaSuccess)
+    b.err = cudaGraphAddEmptyNode(&nd, b.graph, pre.data(), (size_t)n);
+  const int nres = (int)t_res.size(), nref = (int)t_ref.size(), ndel = (int)t_del.size();
+  const int ntb = (int)t_tb.size();
+  cudaGraphConditionalHandle h{};
+  if (b.err == cudaSuccess)
+    b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
+  if (nres > 0) {
+    nd = b.kernel(b.graph, nd, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
+                  d_ref, 0, 0);
+    if (ndel > 0)
+      nd = b.kernel(b.graph, nd, (const void *)batch_delta_kernel, dim3((ndel + 255) / 256),
+                    dim3(256), d_inst, d_del, ndel, 0);
+    nd = b.kernel(b.graph, nd, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
+                  d_inst, d_res, 0);
+    nd = b.kernel(b.graph, nd, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
+                  d_bs, h, m, 0, itermax_all);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&wnode, b.graph, &nd, nullptr, 1, &cp);
+    if (b.err == cudaSuccess) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      cudaGraphNode_t bn = nullptr;
+      int launches = 0;
+      for (int done = 0; done < m; done += shape.sweeps, ++launches) {
+        const int cnt = m - done < shape.sweeps ? m - done : shape.sweeps;
+        bn = b.kernel_smem(body, bn, batch_tb_fn(sched), dim3(ntb), dim3(512), tb_smem(shape),
+                           d_inst, d_tb, cnt, done + cnt >= m ? 1 : 0, launches & 1);
+      }
+      bn = b.kernel(body, bn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
+                    d_ref, 1, launches & 1);
+      if (ndel > 0)
+        bn = b.kernel(body, bn, (const void *)batch_delta_kernel, dim3((ndel + 255) / 256),
+                      dim3(256), d_inst, d_del, ndel, 1);
+      bn = b.kernel(body, bn, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
+                    d_inst, d_res, 1);
+      bn = b.kernel(body, bn, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
+                    d_bs, h, m, 1, itermax_all);
+    }
+    nd = wnode;
+  }
+  // per-instance second halves, in parallel
+  for (int i = 0; i < n && b.err == cudaSuccess; ++i) {
+    cudaGraph_t child = nullptr;
+    b.err = build_step_graph(mem[i].d, mem[i].r, &child, 3);
+    if (b.err == cudaSuccess) {
+      cudaGraphNode_t post = nullptr;
+      b.err = cudaGraphAddChildGraphNode(&post, b.graph, nd ? &nd : nullptr, nd ? 1 : 0, child);
+      cudaGraphDestroy(child);
+    }
+  }
+  if (b.err != cudaSuccess) {
+    cudaGraphDestroy(b.graph);
+    free_batch(bp);
+    return b.err;
+  }
+  bp->graph = b.graph;
+  return cudaSuccess;
+}
+
+cudaError_t batch_sweeps(const std::vector<BatchMember> &mem, int sched, int m,
+                         cudaStream_t s) {
+  // standalone timing helper of the autotuner: m sweeps of every instance
+  // with schedule `sched`, one launch per instance per blocked launch
+  cudaError_t e = tb_prepare();
+  for (const BatchMember &bm : mem) {
+    if (e != cudaSuccess) break;
+    RunCfg r = bm.r;
+    r.sweep_schedule = sched;
+    e = launch_mixed_sweeps(bm.d, r, s, m);
+  }
+  return e;
+}
 }  // namespace strm

@@ -95,4 +95,24 @@ cudaError_t launch_norm_one_block_per_tile(const double *p, const double *rhs, c
                                            const Consts &c, StepState *st, double *partials,
                                            cudaStream_t s);
 
+
+// Batches (strm_batch_*): one graph steps many simulations; their pressure
+// solves share one WHILE loop of table-driven kernels.
+struct BatchMember {
+  DevFields d;
+  RunCfg r;
+};
+struct BatchState;
+struct BatchPlan {
+  void *dev = nullptr;          // device tables (one allocation)
+  BatchState *state = nullptr;  // in dev: loop counters and the overrun flag
+  cudaGraph_t graph = nullptr;
+};
+// sched: internal blocked schedule (1..num_sweep_schedules()-1); m: sweeps
+// per refinement (every member needs max_iterations >= m).
+cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp);
+void free_batch(BatchPlan *bp);
+// Offset of BatchState::overrun in bytes (the host reads it after steps).
+constexpr size_t kBatchOverrunOffset = 3 * sizeof(unsigned int);
+
 }  // namespace strm

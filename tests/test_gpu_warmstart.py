@@ -76,10 +76,10 @@ def test_forward_loss_and_every_gradient_match_oracle():
     dgrad, pooling / upsampling adjoints, head, loss adjoint) vs torch
     autograd on the same BF16-rounded network.  Tolerances: q and the loss
     within 2e-2 relative (BF16 activations, different summation order),
-    every layer's weight and bias gradient within a relative L2 tolerance
-    that grows with the layer's distance from the loss (both sides round
-    activation gradients to BF16 where the kernels store them; summation
-    orders and double roundings differ) and cosine > 0.99."""
+    every layer's weight and bias gradient within twice that layer's own BF16
+    noise (the oracle's BF16-rounded gradient against its plain FP32 one;
+    both sides round activation gradients to BF16 where the kernels store
+    them, summation orders differ) plus 1e-2, relative L2, and cosine > 0.99."""
     import torch
     from stroemung_gb300 import warmstart
     planes = _planes_from_solver()
@@ -100,37 +100,36 @@ def test_forward_loss_and_every_gradient_match_oracle():
     g_gpu = net.grad.cpu().numpy()
 
     loss_ref, per_ref, q_ref, g_ref = U.loss_and_grads(theta, rhs, flags, pprev, 0.01, 0.01)
+    _, _, _, g_fp32 = U.loss_and_grads(theta, rhs, flags, pprev, 0.01, 0.01, bf16=False)
     assert np.linalg.norm(q_gpu - q_ref) <= 2e-2 * np.linalg.norm(q_ref)
     np.testing.assert_allclose(per_gpu, per_ref, rtol=2e-2)
     assert abs(loss_gpu - loss_ref) <= 2e-2 * loss_ref
-    # per layer
-    o = 0
     names = [f"conv{i}.{k}" for i in range(14) for k in ("w", "b")] + ["head.w", "head.b"]
     sizes = []
     for ci, co in U.conv_shapes():
         kp = -(-9 * (-(-ci // 8) * 8) // 64) * 64
         sizes += [co * kp, co]
     sizes += [32, 1]
-    stats = []
+    assert sum(sizes) == g_gpu.size
+    stats, bad = [], []
+    o = 0
     for name, n in zip(names, sizes):
-        a, b = g_gpu[o:o + n].astype(np.float64), g_ref[o:o + n].astype(np.float64)
+        a, b, c = (g[o:o + n].astype(np.float64) for g in (g_gpu, g_ref, g_fp32))
         o += n
-        nb = np.linalg.norm(b)
-        assert nb > 0.0, name
-        rel = np.linalg.norm(a - b) / nb
-        cos = float(a @ b / (np.linalg.norm(a) * nb))
-        stats.append((name, round(rel, 4), round(cos, 5)))
-    assert o == g_gpu.size
-    print("per-layer gradient (name, rel L2, cosine):", stats)
-    # BF16 rounding noise grows with the depth of the backward chain (the
-    # head is closest to the loss, conv0 the farthest): 1.5e-2 at the head
-    # end, 8e-2 for the first layers; bias sums of many terms get twice that
-    bad = []
-    for i, (name, rel, cos) in enumerate(stats):
-        depth = (len(stats) - 1 - i) / (len(stats) - 1)  # 0 head .. 1 conv0
-        tol = (1.5e-2 + 6.5e-2 * depth) * (2.0 if name.endswith(".b") else 1.0)
-        if not (rel <= tol and cos >= 0.99):
-            bad.append((name, rel, cos, round(tol, 3)))
+        if name == "head.b":
+            # a constant added to q on every fluid cell leaves the residual
+            # unchanged (pure Neumann problem): this gradient is 0 up to rounding
+            scale = np.linalg.norm(g_gpu[o - 33:o - 1])
+            if not (abs(a[0]) <= 1e-2 * scale and abs(b[0]) <= 1e-2 * scale):
+                bad.append((name, a[0], b[0], scale))
+            continue
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+        noise = np.linalg.norm(b - c) / np.linalg.norm(c)  # the layer's own BF16 noise
+        stats.append((name, round(rel, 4), round(cos, 5), round(noise, 4)))
+        if not (rel <= 2.0 * noise + 1e-2 and cos >= 0.99):
+            bad.append(stats[-1])
+    print("per-layer gradient (name, rel L2 vs oracle, cosine, BF16 noise):", stats)
     assert not bad, bad
 
 
