@@ -11,9 +11,23 @@ reference's stop rule, velocity update.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Prints one JSON line.  `value` is whole-job cell-updates/s (interior cells x
-steps / device time), inputs resident in HBM; `e2e` is the same metric
-through the public API with host (pinned) buffers uploaded and downloaded
-every step.  Under torchrun each rank runs its own replica (weak scaling).
+steps / device time) of the plain FP64 red-black path, inputs resident in
+HBM; `e2e` is the same metric through the public API with host (pinned)
+buffers uploaded and downloaded every step.  Under torchrun each rank runs
+its own replica (weak scaling).  Further blocks on rank 0:
+
+* `mixed_precision`: FP32 sweeps + FP64 norm/refinement on the same
+  workload (autotuned sweep schedule), its speed-up over the plain path and
+  each field's error against the plain FP64 run after `--err-steps` steps;
+* `learned`: the BF16 U-Net warm start, trained here on snapshots of
+  512 x 128 channels, judged in the loop on the same workload against the
+  mixed solve from identical states (sweeps to the same residual, time);
+* `cavity_mixed`: the 2048 x 2048 lid-driven cavity (Re 1000, omega 1.8,
+  eps 1e-5 on the residual relative to the solve's start), mixed against
+  FP64: Poisson time-to-residual per step and the fields' error;
+* `batched`: many channel simulations of uneven sizes stepped as one batch
+  against the same instances run one after another on the plain FP64 path.
+
 `--impl reference` times the reference algorithm's CPU restatement (the
 oracle; the Rust crate cannot be built here) on bounded samples of the same
 workload.
@@ -49,6 +63,17 @@ def load_peaks():
         d = json.loads(p.read_text())
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
+
+
+def load_bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("bf16_tflops", 1900.0))
+    return 1900.0
+
+
+BF16_PEAK = load_bf16_peak()
 
 
 def workload(seed: int):
@@ -178,6 +203,314 @@ def config_dict(args):
                   "no flush", "parallelism": f"replicas x{args.gpus}"}
 
 
+def field_errors(a_fields, b_fields, fluid):
+    """Relative L2 and max abs error per field; the pressure on fluid cells
+    with its mean removed (pure Neumann: each solve fixes its own constant)."""
+    import numpy as np
+    err = {}
+    for n in ("u", "v", "p"):
+        a, b = a_fields[n], b_fields[n]
+        if n == "p":
+            a, b = a[fluid] - a[fluid].mean(), b[fluid] - b[fluid].mean()
+        err[n] = {"rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
+                  "max_abs": float(np.abs(a - b).max())}
+    return err
+
+
+def timed_steps(sim, n, stream):
+    import torch
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = sim.step_n(n)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), stats
+
+
+def error_growth(args, grid):
+    """Field errors against the plain FP64 (fast arithmetic) run, stepped in
+    lockstep from the same initial state: the mixed-precision solve, and as a
+    control the FP64 run with the reference's exact operation order (the
+    two FP64 runs differ only by rounding)."""
+    from stroemung_gb300.simulation import PREC_MIXED, ARITH_EXACT, ARITH_FAST, Simulation
+    fast = Simulation(grid=grid, arithmetic=ARITH_FAST, **PARAMS)
+    exact = Simulation(grid=grid, arithmetic=ARITH_EXACT, **PARAMS)
+    mixed = Simulation(grid=grid, precision=PREC_MIXED, inner_sweeps=args.inner_sweeps,
+                       arithmetic=ARITH_FAST, **PARAMS)
+    fluid = grid["kind"] == 0
+    checkpoints = sorted({c for c in (1, 5, 10, 25, 50, args.err_steps) if c <= args.err_steps})
+    rows = []
+    done = 0
+    for c in checkpoints:
+        for sim in (fast, exact, mixed):
+            sim.step_n(c - done)
+        done = c
+        ref = {n: fast.download(n) for n in ("u", "v", "p")}
+        em = field_errors({n: mixed.download(n) for n in ("u", "v", "p")}, ref, fluid)
+        ex = field_errors({n: exact.download(n) for n in ("u", "v", "p")}, ref, fluid)
+        rows.append({"step": c, "mixed": {k: v["rel_l2"] for k, v in em.items()},
+                     "fp64_exact_order": {k: v["rel_l2"] for k, v in ex.items()}})
+    for sim in (fast, exact, mixed):
+        sim.close()
+    return rows
+
+
+def mixed_block(args, grid, fp64_ms_step, peak):
+    """Mixed precision on the same workload, from the same initial state."""
+    import torch
+    from stroemung_gb300.simulation import PREC_MIXED, ARITH_FAST, Simulation
+    sim = Simulation(grid=grid, precision=PREC_MIXED, inner_sweeps=args.inner_sweeps,
+                     arithmetic=ARITH_FAST, **PARAMS)
+    stream = torch.cuda.ExternalStream(sim.device_view()["stream"])
+    warm = sim.step_n(args.warmup)
+    best, sched_ms = sim.autotune_sweeps(reps=3)
+    ms, stats = timed_steps(sim, args.steps, stream)
+    iters = [x[0] for x in stats]
+    # the FP32 sweeps alone (the dominant kernel of this path), timed live
+    nsw = 16 * 4
+    sw0 = torch.cuda.Event(enable_timing=True)
+    sw1 = torch.cuda.Event(enable_timing=True)
+    sim.synchronize()
+    sw0.record(stream)
+    sim.sor_sweeps(nsw, wait=False)
+    sw1.record(stream)
+    sim.synchronize()
+    t_sw = sw0.elapsed_time(sw1) / 1e3 / nsw
+    sw_bytes = 13.0 * CELLS  # read e, s (8) + flags (1), write e (4)
+    sim.close()
+    growth = error_growth(args, grid) if args.err_steps > 0 else []
+    return {
+        "value": CELLS * args.steps / (ms / 1e3), "unit": "cell-updates/s",
+        "ms_per_step": ms / args.steps, "speedup_vs_fp64": fp64_ms_step / (ms / args.steps),
+        "inner_sweeps": min(args.inner_sweeps, PARAMS["max_iterations"]),
+        "sweep_schedule": {"chosen": best, "us_per_sweep": {str(k): v * 1e3
+                                                            for k, v in sched_ms.items()},
+                           "note": "1 = one launch per colour pass; 2..7 = shared-memory "
+                                   "tiles with 2-8 sweeps per launch (autotuned here)"},
+        "sor_iterations": {"mean": statistics.mean(iters), "min": min(iters), "max": max(iters),
+                           "warmup": [w[0] for w in warm]},
+        "error_vs_fp64": {
+            "rel_l2_by_step": growth,
+            "note": "relative L2 against the plain FP64 run (pressure on fluid cells, mean "
+                    "removed); the FP64 exact-order run is the control: it differs from the "
+                    "plain run by rounding only, and both errors grow at the flow's rate"},
+        "roofline_fp32_sweep": {"achieved": sw_bytes / t_sw / 1e9, "peak": peak, "unit": "GB/s",
+                                "frac": sw_bytes / t_sw / 1e9 / peak, "us_per_sweep": t_sw * 1e6,
+                                "algorithmic_bytes": sw_bytes},
+        "dtype": "f32 sweeps, f64 norm/refinement/dt",
+    }
+
+
+def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
+    """Train the U-Net on 512 x 128 snapshots, then step the workload with the
+    judged warm start, each step A/B against the plain mixed solve from the
+    identical state."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import warmstart
+    from stroemung_gb300.simulation import PREC_MIXED, ARITH_FAST, Simulation
+    from stroemung_gb300.unet import UNet
+    net = UNet(seed=0)
+    train_info = {}
+    if args.ws_weights:
+        net.load_state_dict({"theta": np.load(args.ws_weights), "step": 1})
+        train_info["weights"] = os.path.basename(args.ws_weights)
+    else:
+        t0 = time.perf_counter()
+        train = warmstart.generate_snapshots(args.ws_snapshots, imax=512, jmax=128,
+                                             steps_per_problem=32, seed=11)
+        held = warmstart.generate_snapshots(64, imax=512, jmax=128, steps_per_problem=32,
+                                            seed=12)
+        t_gen = time.perf_counter() - t0
+        tr = warmstart.Trainer(net, 514, 130, 0.01, 0.01, batch=32)
+        before, _ = tr.loss(held, 0)
+        t0 = time.perf_counter()
+        hist = tr.fit(train, epochs=args.ws_epochs, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        after, _ = tr.loss(held, 0)
+        train_info = {"snapshots": args.ws_snapshots, "grid": "512x128", "epochs": args.ws_epochs,
+                      "adam_steps": len(hist), "batch": 32, "lr": 1e-3,
+                      "held_out_relative_residual": {"before": before, "after": after},
+                      "generate_s": t_gen, "train_s": t_train,
+                      "train_ms_per_step": t_train / max(len(hist), 1) * 1e3}
+        del train, held, tr
+        torch.cuda.empty_cache()
+    # forward cost at the workload size and its tensor-pipe rate
+    x = torch.zeros(1, IMAX, JMAX, 8, dtype=torch.bfloat16, device="cuda")
+    net.forward(x, 1, IMAX, JMAX)
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(3):
+        net.forward(x, 1, IMAX, JMAX)
+    f1.record()
+    torch.cuda.synchronize()
+    fwd_ms = f0.elapsed_time(f1) / 3
+    flops = 0.0
+    pixel_scale = [1, 1, 4, 4, 16, 16, 64, 64, 16, 16, 4, 4, 1, 1]  # pixels per layer: 1/scale
+    for l, sc in zip(net.layers(), pixel_scale):
+        flops += 2.0 * 9 * l.cin * l.cout * IMAX * JMAX / sc
+    del x
+    net._bufs.clear()
+    torch.cuda.empty_cache()
+    mk = dict(precision=PREC_MIXED, inner_sweeps=args.inner_sweeps, arithmetic=ARITH_FAST)
+    plain = Simulation(grid=grid, **mk, **PARAMS)
+    wsim = Simulation(grid=grid, **mk, **PARAMS)
+    ws = warmstart.WarmStartSolver(wsim, net)
+    scratch = torch.zeros(IMAX + 2, JMAX + 2, dtype=torch.float64, device="cuda")
+    plain.step_n(args.warmup)
+    warmstart.sync_state(wsim, plain, scratch)
+    rows = []
+    for _ in range(args.ws_steps):
+        r = warmstart.compare_step(plain, ws, scratch)
+        hp, hw = r.pop("hist_plain"), r.pop("hist_ws")
+        # sweeps each run needs to reach the plain run's norm at 1/8, 1/2 and all of its sweeps
+        marks = {}
+        for frac in (0.125, 0.5, 1.0):
+            k = max(0, min(len(hp) - 1, int(round(frac * (len(hp) - 1)))))
+            target = hp[k, 1]
+            marks[str(frac)] = {"plain": int(hp[k, 0]),
+                                "learned": warmstart.sweeps_to_reach(hw, target)}
+        r["sweeps_to_plain_norm"] = marks
+        rows.append(r)
+    # the learned step as a user runs it: predict, judge, solve
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.ws_steps):
+        ws.step()
+    torch.cuda.synchronize()
+    learned_ms = (time.perf_counter() - t0) / args.ws_steps * 1e3
+    plain.close()
+    wsim.close()
+    acc = sum(1 for r in rows if r["accepted"])
+    ratio = [r["ns_pred"] / r["ns_prev"] for r in rows if r["ns_prev"] > 0]
+    saved = [r["sweeps_plain"] - r["ws_sweeps_to_plain_final"] for r in rows
+             if r["ws_sweeps_to_plain_final"] is not None]
+    return {
+        "value": CELLS / (learned_ms / 1e3), "unit": "cell-updates/s",
+        "ms_per_step": learned_ms, "speedup_vs_fp64": fp64_ms_step / learned_ms,
+        "speedup_vs_mixed": mixed_ms_step / learned_ms if mixed_ms_step else None,
+        "predict_ms": statistics.mean(r["predict_ms"] for r in rows),
+        "judge_ms": statistics.mean(r["judge_ms"] for r in rows),
+        "accepted": f"{acc}/{len(rows)}",
+        "initial_norm_ratio_median": statistics.median(ratio) if ratio else None,
+        "sweeps_saved_to_plain_final_norm": {"per_step": saved, "steps_reaching": len(saved),
+                                             "steps": len(rows)},
+        "per_step": [{k: r[k] for k in ("sweeps_plain", "sweeps_ws", "ns_plain", "ns_ws",
+                                         "ns_prev", "ns_pred", "accepted",
+                                         "sweeps_to_plain_norm")} for r in rows],
+        "cnn": {"forward_ms_at_workload": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9,
+                "tensor_frac_of_measured_bf16": (flops / fwd_ms / 1e9) / BF16_PEAK,
+                "params": net.parameter_count()},
+        "training": train_info,
+    }
+
+
+def cavity_block(args):
+    """Lid-driven cavity 2048 x 2048, Re 1000, omega 1.8, eps 1e-5 relative:
+    FP64 and mixed from the same state; Poisson time-to-residual per step."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import presets
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    n = args.cavity_n
+    grid = presets.cavity(n)
+    cfg = dict(cell_size=(1.0 / n, 1.0 / n), delt=1e-4, gamma=0.9, reynolds=1000.0,
+               sor_absolute_epsilon=1e-5, max_iterations=args.cavity_itermax, omega=1.8,
+               tau=0.5, arithmetic=ARITH_FAST, strict_eps=2)
+    out = {"grid": f"{n}x{n}", "steps": args.cavity_steps, "max_iterations": args.cavity_itermax,
+           "stop_rule": "ns < (1e-5)^2 x the norm the solve starts from"}
+    res = {}
+    fields = {}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        sim = Simulation(grid=grid, precision=prec, **cfg)
+        stream = torch.cuda.ExternalStream(sim.device_view()["stream"])
+        per = []
+        for _ in range(args.cavity_steps):
+            ms, st = timed_steps(sim, 1, stream)
+            per.append((ms, int(st[0][0]), bool(st[0][3])))
+        fields[name] = {k: sim.download(k) for k in ("u", "v", "p")}
+        sim.close()
+        res[name] = {"ms_per_step": [p[0] for p in per], "sweeps": [p[1] for p in per],
+                     "converged": [p[2] for p in per],
+                     "time_to_residual_ms_median": statistics.median(p[0] for p in per)}
+    out.update(res)
+    out["speedup_mixed_vs_fp64"] = (sum(res["fp64"]["ms_per_step"]) /
+                                    sum(res["mixed"]["ms_per_step"]))
+    out["error_mixed_vs_fp64"] = field_errors(fields["mixed"], fields["fp64"], grid["kind"] == 0)
+    return out
+
+
+def batched_block(args):
+    """Channel instances of uneven sizes (imax in 128..2048 step 128, jmax in
+    32..512 step 32, Re log-uniform in [50, 1000], 1..16 rectangles), stepped
+    as one batch vs one after another on the plain FP64 path."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import presets
+    from stroemung_gb300.batch import Batch
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    rng = np.random.default_rng(4)
+    specs = []
+    for k in range(args.batch_n):
+        imax = int(rng.integers(1, 17)) * 128
+        jmax = int(rng.integers(1, 17)) * 32
+        re = float(np.exp(rng.uniform(np.log(50.0), np.log(1000.0))))
+        nrect = int(rng.integers(1, 17))
+        side = (4, max(4, min(32, jmax // 4)))
+        rects = presets.random_rectangles(imax, jmax, nrect, 1000 + k, side=side,
+                                          x_margin=min(64, imax // 8))
+        specs.append((presets.channel(imax, jmax, rects), re, imax * jmax))
+    cfg = dict(cell_size=(0.01, 0.01), delt=0.005, gamma=0.9, sor_absolute_epsilon=1e-3,
+               max_iterations=2000, omega=1.7, tau=0.5, arithmetic=ARITH_FAST)
+    cells = sum(c for _, _, c in specs)
+    sims = [Simulation(grid=g, reynolds=re, precision=PREC_MIXED, inner_sweeps=16, **cfg)
+            for g, re, _ in specs]
+    batch = Batch(sims)
+    batch.step(1)
+    best, sched_ms = batch.autotune(reps=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = batch.step(args.batch_steps)
+    torch.cuda.synchronize()
+    t_batch = (time.perf_counter() - t0) / args.batch_steps
+    batch.close()
+    for s in sims:
+        s.close()
+    # the same instances one after another on the plain FP64 path (a sample,
+    # scaled by cells)
+    sample = list(range(0, len(specs), max(1, len(specs) // args.batch_seq_sample)))
+    t_seq, c_seq = 0.0, 0
+    for k in sample:
+        g, re, c = specs[k]
+        sim = Simulation(grid=g, reynolds=re, precision=PREC_FP64, **cfg)
+        sim.run_simulation_tick()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.step_n(1)
+        t_seq += time.perf_counter() - t0
+        c_seq += c
+        sim.close()
+    seq_rate = c_seq / t_seq
+    rate = cells / t_batch
+    return {
+        "instances": len(specs), "cells": cells, "steps": args.batch_steps,
+        "value": rate, "unit": "cell-updates/s", "ms_per_batch_step": t_batch * 1e3,
+        "sequential_fp64": {"value": seq_rate, "unit": "cell-updates/s",
+                            "sample_instances": len(sample)},
+        "speedup_vs_sequential_fp64": rate / seq_rate,
+        "sweep_schedule": {"chosen": best, "ms_per_batch_step": {str(k): v for k, v in
+                                                                 sched_ms.items()}},
+        "sor_iterations_mean": float(np.mean(st["sor_iterations"])),
+        "solver": "mixed precision (FP32 sweeps, FP64 norm/refinement), reference stop rule, "
+                  "eps 1e-3, max_iterations 2000; one graph per step",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,10 +522,25 @@ def main():
     ap.add_argument("--ref-cap", type=int, default=10)
     ap.add_argument("--cpu-ticks", type=int, default=3)
     ap.add_argument("--cpu-cap", type=int, default=50)
-    ap.add_argument("--mixed", type=int, default=1)
     ap.add_argument("--eager", type=int, default=0,
                     help="1: launch kernels one by one (for per-kernel profiling)")
     ap.add_argument("--inner-sweeps", type=int, default=16)
+    ap.add_argument("--mixed", type=int, default=1)
+    ap.add_argument("--err-steps", type=int, default=100,
+                    help="steps after which mixed precision is compared with FP64")
+    ap.add_argument("--learned", type=int, default=1)
+    ap.add_argument("--ws-weights", default="", help="trained U-Net parameters (.npy)")
+    ap.add_argument("--ws-snapshots", type=int, default=1024)
+    ap.add_argument("--ws-epochs", type=int, default=8)
+    ap.add_argument("--ws-steps", type=int, default=4)
+    ap.add_argument("--cavity", type=int, default=1)
+    ap.add_argument("--cavity-n", type=int, default=2048)
+    ap.add_argument("--cavity-steps", type=int, default=3)
+    ap.add_argument("--cavity-itermax", type=int, default=20000)
+    ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--batch-n", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-seq-sample", type=int, default=16)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -245,7 +593,6 @@ def main():
     iters = [s[0] for s in stats]
     n_pcopy_launch = 1
     launches = sum(2 + 3 + n_pcopy_launch + (3 + n_pcopy_launch) * (k - 1) + 2 for k in iters)
-    fp64_fields = {n: sim.download(n) for n in ("u", "v", "p")}
 
     # ---- dominant kernel: one red-black iteration, timed live ----
     nsweep = 20
@@ -282,57 +629,6 @@ def main():
     except Exception:
         pass
 
-    # ---- mixed precision on the same workload: FP32 sweeps, FP64 norm and
-    # refinement; same warm-up and timed steps from the same initial state ----
-    mixed = None
-    if args.mixed:
-        from stroemung_gb300.simulation import PREC_MIXED
-        simm = Simulation(grid=grid, precision=PREC_MIXED, inner_sweeps=args.inner_sweeps,
-                          execution=args.eager, **PARAMS)
-        stream_m = torch.cuda.ExternalStream(simm.device_view()["stream"])
-        warm_m = simm.step_n(args.warmup)
-        torch.cuda.synchronize()
-        m0 = torch.cuda.Event(enable_timing=True)
-        m1 = torch.cuda.Event(enable_timing=True)
-        m0.record(stream_m)
-        stats_m = simm.step_n(args.steps)
-        m1.record(stream_m)
-        torch.cuda.synchronize()
-        ms_m = m0.elapsed_time(m1)
-        iters_m = [x[0] for x in stats_m]
-        err = {}
-        fl = grid["kind"] == 0
-        for n in ("u", "v", "p"):
-            a, b = simm.download(n), fp64_fields[n]
-            if n == "p":  # pressure is defined up to a constant: fluid cells, mean removed
-                a, b = a[fl] - a[fl].mean(), b[fl] - b[fl].mean()
-            err[n] = {"rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
-                      "max_abs": float(np.abs(a - b).max())}
-        sw0 = torch.cuda.Event(enable_timing=True)
-        sw1 = torch.cuda.Event(enable_timing=True)
-        simm.synchronize()
-        sw0.record(stream_m)
-        simm.sor_sweeps(nsweep, wait=False)
-        sw1.record(stream_m)
-        simm.synchronize()
-        t_sw = sw0.elapsed_time(sw1) / 1e3 / nsweep
-        sw_bytes = 13.0 * interior  # read e, s (8) + flags (1), write e (4)
-        m_inner = min(args.inner_sweeps, PARAMS["max_iterations"])
-        mixed = {
-            "value": CELLS * args.steps * world / (ms_m / 1e3), "unit": "cell-updates/s",
-            "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m,
-            "inner_sweeps": m_inner,
-            "sor_iterations": {"mean": statistics.mean(iters_m), "min": min(iters_m),
-                               "max": max(iters_m), "warmup": [w[0] for w in warm_m]},
-            "error_vs_fp64_after_steps": {"steps": args.warmup + args.steps, **err},
-            "roofline_fp32_sweep": {"achieved": sw_bytes / t_sw / 1e9, "peak": peak,
-                                    "unit": "GB/s", "frac": sw_bytes / t_sw / 1e9 / peak,
-                                    "ms_per_sweep": t_sw * 1e3,
-                                    "algorithmic_bytes": sw_bytes},
-            "dtype": "f32 sweeps, f64 norm/refinement/dt",
-        }
-        simm.close()
-
     # ---- e2e: public API with host buffers, copies inside the timed region ----
     pin = {n: torch.empty((IMAX + 2, JMAX + 2), dtype=torch.float64, pin_memory=True)
            for n in ("u", "v", "p")}
@@ -357,7 +653,8 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     field_bytes = (IMAX + 2) * (JMAX + 2) * 8
-    e2e = {"value": CELLS * args.e2e_steps * world / e2e_s if args.e2e_steps else None, "unit": "cell-updates/s",
+    e2e = {"value": CELLS * args.e2e_steps * world / e2e_s if args.e2e_steps else None,
+           "unit": "cell-updates/s",
            "h2d_bytes_per_step": 3 * field_bytes, "d2h_bytes_per_step": 3 * field_bytes + 64,
            "steps": args.e2e_steps, "sor_iterations": e2e_iters,
            "path": "Simulation.upload(u,v,p) + run_simulation_tick() + download(u,v,p), "
@@ -383,7 +680,6 @@ def main():
                  "dgemm_tflops_measured": fp64_peak,
                  "note": "FP64 pipe operations (add, mul, fma each 1) of the solve"},
         "e2e": e2e,
-        "mixed_precision": mixed,
         "clocks": clocks.summary(),
         "gpu_launches": launches,
     }
@@ -397,9 +693,33 @@ def main():
                       f"{statistics.mean(iters):.0f} (the GPU steps' mean) x per-iteration "
                       f"({t_it * 1e3:.1f} ms) + post-solve",
             "host_cpu": os.uname().machine, "nproc": os.cpu_count()}
+
     if rank == 0:
+        fp64_ms_step = ms / args.steps
+        mixed_ms = None
+
+        def guarded(name, fn):
+            # an auxiliary block that fails is reported, not fatal to the line
+            try:
+                out[name] = fn()
+            except Exception as exc:  # noqa: BLE001
+                out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
+
+        sim.close()
+        sim = None
+        if args.mixed:
+            guarded("mixed_precision", lambda: mixed_block(args, grid, fp64_ms_step, peak))
+            mixed_ms = out["mixed_precision"].get("ms_per_step")
+        if args.learned:
+            guarded("learned", lambda: learned_block(args, grid, fp64_ms_step, mixed_ms))
+        if args.cavity:
+            guarded("cavity_mixed", lambda: cavity_block(args))
+        if args.batched:
+            guarded("batched", lambda: batched_block(args))
         print(json.dumps(out))
-    sim.close()
+    if sim is not None:
+        sim.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -86,6 +86,13 @@ enum {
                             debugging */
 };
 
+/* Stop rules of the pressure solve (strm_mode.strict_eps). */
+enum {
+    STRM_STOP_REFERENCE = 0, /* ns < initial_norm_squared or ns < eps^2 (src/simulation.rs:276-281) */
+    STRM_STOP_STRICT = 1,    /* ns < eps^2 */
+    STRM_STOP_RELATIVE = 2   /* ns < eps^2 * the solve's starting norm */
+};
+
 /* FP32 sweep schedules of the mixed solve (strm_mode.sweep_schedule). */
 enum {
     STRM_SWEEPS_DEFAULT = 0,    /* 48 x 112 blocked tiles, 4 sweeps per launch */
@@ -129,7 +136,10 @@ typedef struct {
     int sor_order;    /* STRM_SOR_* */
     int arithmetic;   /* STRM_ARITH_* */
     int precision;    /* STRM_PREC_* */
-    int strict_eps;   /* 1: stop only at ns < eps^2 (not at ns < initial norm) */
+    int strict_eps;   /* stop rule: 0 the reference's (ns < initial norm or
+                         ns < eps^2); 1 only ns < eps^2; 2 relative,
+                         ns < eps^2 * (norm the solve started from, before
+                         its first sweep; red-black orders) */
     int inner_sweeps; /* mixed precision: FP32 sweeps per FP64 refinement (0 = 16) */
     int execution;    /* STRM_EXEC_* */
     int norm_cells;   /* STRM_NORM_ALL_INTERIOR: the residual norm sums every

@@ -28,6 +28,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXEC_GRAPH, EXEC_EAGER = 0, 1
 NORM_ALL_INTERIOR, NORM_FLUID, NORM_FLUID_MEAN_FREE = 0, 1, 2
 SWEEPS_DEFAULT, SWEEPS_PER_COLOUR, SWEEPS_COUNT = 0, 1, 8
+STOP_REFERENCE, STOP_STRICT, STOP_RELATIVE = 0, 1, 2
 
 
 class Params(ctypes.Structure):

@@ -117,7 +117,7 @@ void update_cfg(strm_sim *s) {
   r.tau = s->prm.tau;
   r.delt = s->prm.delt;
   r.itermax = s->prm.max_iterations;
-  r.strict_eps = (s->mode.strict_eps ? 1 : 0) |
+  r.strict_eps = (s->mode.strict_eps == 1 ? 1 : 0) | (s->mode.strict_eps == 2 ? 8 : 0) |
                  (s->mode.norm_cells != STRM_NORM_ALL_INTERIOR ? 2 : 0) |
                  (s->mode.norm_cells == STRM_NORM_FLUID_MEAN_FREE ? 4 : 0);
   r.sor_order = s->mode.sor_order == STRM_SOR_LEXICOGRAPHIC ? 1 : 0;
@@ -406,6 +406,10 @@ int strm_set_mode(strm_sim *s, const strm_mode *mode) {
       mode->norm_cells < 0 || mode->norm_cells > 2 || mode->sweep_schedule < 0 ||
       mode->sweep_schedule > num_sweep_schedules())
     return fail(STRM_ERR_INVALID, "unknown mode value");
+  if (mode->strict_eps < 0 || mode->strict_eps > 2)
+    return fail(STRM_ERR_INVALID, "unknown stop rule %d", mode->strict_eps);
+  if (mode->strict_eps == 2 && mode->sor_order == STRM_SOR_LEXICOGRAPHIC)
+    return fail(STRM_ERR_INVALID, "the relative stop rule is available with red-black orders");
   if (mode->norm_cells != STRM_NORM_ALL_INTERIOR && mode->sor_order == STRM_SOR_LEXICOGRAPHIC)
     return fail(STRM_ERR_INVALID, "the fluid-cell norms are available with red-black orders");
   CK(cudaSetDevice(s->dev));

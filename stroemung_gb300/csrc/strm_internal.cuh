@@ -54,6 +54,7 @@ struct StepState {
   double fluid_cells;
   double umax, vmax;   // max |u|, |v| over every cell (adaptive dt input)
   double aux;          // result of a standalone norm
+  double ns_start;     // norm the current pressure solve started from
   unsigned long long iterations;
   unsigned int sor_iters;
   unsigned int converged;   // pressure solve met its stop rule

@@ -422,13 +422,21 @@ __global__ void __launch_bounds__(256)
 }
 
 // What a residual launch does once the norm is known.
-enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2 };
+enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2, RES_START = 3 };
 // bits of the `strict` argument of the residual kernels
 enum : int {
   STOP_STRICT = 1,      // stop only at ns < eps^2 (not at ns < the initial norm)
   STOP_FLUID_NORM = 2,  // sum the residual over fluid cells only (not every interior cell)
   STOP_MEAN_FREE = 4,   // with STOP_FLUID_NORM: remove the residual's mean over fluid cells
+  STOP_RELATIVE = 8,    // stop at ns < eps^2 * (the norm the solve started from)
 };
+
+__device__ __forceinline__ bool stop_rule(double ns, const Consts &c, const StepState *st,
+                                          int strict) {
+  if (strict & STOP_RELATIVE) return ns < c.eps2 * st->ns_start;
+  if (strict & STOP_STRICT) return ns < c.eps2;
+  return (ns < st->ns0) || (ns < c.eps2);
+}
 
 // The norm from the block sums: sum r^2 (and sum r when mean_free, stored
 // interleaved), divided by fluid_cells; mean-free: (sum r^2 - (sum r)^2 / n) / n.
@@ -438,6 +446,37 @@ __device__ __forceinline__ double finish_norm(const double *partials, int nblock
   const double s2 = reduce_partials(partials, nblocks, 2, 0, OpAdd(), 0.0);
   const double s1 = reduce_partials(partials, nblocks, 2, 1, OpAdd(), 0.0);
   return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
+
+// This thread's share of the residual sums over the block's tiles: sum r^2
+// (and sum r when MEAN_FREE) over interior cells, fluid cells only when FLUID.
+template <bool EXACT, bool FLUID, bool MEAN_FREE>
+__device__ __forceinline__ void residual_sum(const double *__restrict__ p,
+                                             const double *__restrict__ rhs,
+                                             const uint8_t *__restrict__ flags, const Geom &g,
+                                             const Consts &c, int tiles_y, int ntiles,
+                                             double *acc_out, double *acc1_out) {
+  double acc = 0.0, acc1 = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tx = t / tiles_y, ty = t % tiles_y;
+    const int x = 1 + tx * RT_X + threadIdx.y;
+    if (x > g.nx - 2) continue;
+    const int yb = 1 + ty * RT_Y + 2 * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = yb + q;
+      if (y <= g.ny - 2) {
+        const size_t o = OFF(x, y);
+        if (FLUID && flags[o] != 0) continue;
+        const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
+                                            p[o + 1], rhs[o], c);
+        acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
+        if (MEAN_FREE) acc1 += r;
+      }
+    }
+  }
+  *acc_out = acc;
+  *acc1_out = acc1;
 }
 
 // Residual norm over every interior cell (src/simulation.rs:216-227), in
@@ -454,24 +493,14 @@ __global__ void __launch_bounds__(256)
   const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
   const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
   double acc = 0.0, acc1 = 0.0;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int tx = t / tiles_y, ty = t % tiles_y;
-    const int x = 1 + tx * RT_X + threadIdx.y;
-    if (x > g.nx - 2) continue;
-    const int yb = 1 + ty * RT_Y + 2 * threadIdx.x;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int y = yb + q;
-      if (y <= g.ny - 2) {
-        const size_t o = OFF(x, y);
-        if (fluid_only && flags[o] != 0) continue;
-        const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
-                                            p[o + 1], rhs[o], c);
-        acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
-        if (mean_free) acc1 += r;
-      }
-    }
-  }
+  // the reference's sum (every interior cell) keeps its own loop: the solve is
+  // FP64-bound and pays for every extra operation
+  if (!fluid_only)
+    residual_sum<EXACT, false, false>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+  else if (!mean_free)
+    residual_sum<EXACT, true, false>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+  else
+    residual_sum<EXACT, true, true>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
   if (mean_free) {
     const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
@@ -498,6 +527,9 @@ __global__ void __launch_bounds__(256)
     st->counter = 0;
     if (mode == RES_NS0) {
       st->ns0 = ns;
+    } else if (mode == RES_START) {
+      st->ns_start = ns;
+      hist_push(st, 0u, ns);
     } else if (mode == RES_NORM) {
       st->aux = ns;
     } else {
@@ -506,7 +538,7 @@ __global__ void __launch_bounds__(256)
       st->ns = ns;
       hist_push(st, it, ns);
       st->nonfinite = !isfinite(ns);
-      const bool done = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      const bool done = stop_rule(ns, c, st, strict);
       if (done) st->converged = 1;
       else if (it >= itermax) st->exhausted = 1;
       if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
@@ -555,7 +587,7 @@ __global__ void __launch_bounds__(1024)
       for (int k = 0; k < NI * NJ; ++k) acc = acc + r2[k];
       ns = acc / st->fluid_cells;
       iters = it + 1;
-      conv = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      conv = stop_rule(ns, c, st, strict);
       s_done = conv;
     }
     __syncthreads();
@@ -944,16 +976,11 @@ __global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s
   delta_entry(p, s, e, pc[k], pitch);
 }
 
-// FP64 norm of the residual on every interior cell (the reference's norm),
-// the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
-// and the stop rule every m sweeps.  Block `bid` of `nblocks` sums its tiles
-// into partials[bid] (interleaved with the residual sum when mean-free).
-__device__ __forceinline__ void mixed_residual_partial(
+template <bool FLUID, bool MEAN_FREE>
+__device__ __forceinline__ void mixed_residual_sum(
     const double *__restrict__ p, const double *__restrict__ rhs,
     const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
-    double *partials, int tiles_y, int ntiles, int strict, int bid, int nblocks) {
-  const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
-  const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
+    int tiles_y, int ntiles, int bid, int nblocks, double *acc_out, double *acc1_out) {
   double acc = 0.0, acc1 = 0.0;
   for (int t = bid; t < ntiles; t += nblocks) {
     const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
@@ -967,14 +994,38 @@ __device__ __forceinline__ void mixed_residual_partial(
         const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
                                             p[o + 1], rhs[o], c);
         const bool fluid = flags[o] == 0;
-        if (fluid || !fluid_only) {
+        if (fluid || !FLUID) {
           acc = fma(r, r, acc);
-          if (mean_free) acc1 += r;
+          if (MEAN_FREE) acc1 += r;
         }
         if (fluid) s[o] = (float)(c.middle * r);
       }
     }
   }
+  *acc_out = acc;
+  *acc1_out = acc1;
+}
+
+// FP64 norm of the residual on every interior cell (the reference's norm),
+// the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
+// and the stop rule every m sweeps.  Block `bid` of `nblocks` sums its tiles
+// into partials[bid] (interleaved with the residual sum when mean-free).
+__device__ __forceinline__ void mixed_residual_partial(
+    const double *__restrict__ p, const double *__restrict__ rhs,
+    const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
+    double *partials, int tiles_y, int ntiles, int strict, int bid, int nblocks) {
+  const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
+  const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
+  double acc = 0.0, acc1 = 0.0;
+  if (!fluid_only)
+    mixed_residual_sum<false, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
+                                     &acc1);
+  else if (!mean_free)
+    mixed_residual_sum<true, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
+                                    &acc1);
+  else
+    mixed_residual_sum<true, true>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
+                                   &acc1);
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
   if (mean_free) {
     const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
@@ -1000,11 +1051,12 @@ __device__ __forceinline__ bool mixed_residual_stop(const double *partials, int 
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->ns = ns;
     hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
+    if (!check) st->ns_start = ns;
     if (check) {
       const unsigned int it = st->sor_iters + sweeps;
       st->sor_iters = it;
       st->nonfinite = !isfinite(ns);
-      const bool done = (strict & STOP_STRICT) ? (ns < c.eps2) : ((ns < st->ns0) || (ns < c.eps2));
+      const bool done = stop_rule(ns, c, st, strict);
       const bool room = it + sweeps <= itermax;
       if (done) st->converged = 1;
       else if (!room) st->exhausted = 1;
@@ -1490,6 +1542,17 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
   } else if (nt_int > 0 && r.itermax > 0) {
     dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+    if (r.strict_eps & STOP_RELATIVE) {
+      // the norm the solve starts from (relative stop rule)
+      if (r.arith)
+        residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st,
+                                                               d.partials, ty_int, nt_int, 0,
+                                                               r.itermax, r.strict_eps, RES_START);
+      else
+        residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st,
+                                                              d.partials, ty_int, nt_int, 0,
+                                                              r.itermax, r.strict_eps, RES_START);
+    }
     while (!done) {
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
       for (int color = 0; color < 2; ++color) {
@@ -1659,6 +1722,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     cudaGraphConditionalHandle h;
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
+    if (r.strict_eps & STOP_RELATIVE) {
+      // the norm the solve starts from (relative stop rule)
+      const void *k0 = r.arith ? (const void *)residual_kernel<false, false>
+                               : (const void *)residual_kernel<true, false>;
+      n = b.kernel(b.graph, n, k0, dim3(nb), kRedBlock, (const double *)d.p,
+                   (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
+                   ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_START);
+    }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;

@@ -144,12 +144,13 @@ class Simulation:
     def set_mode(self, *, sor_order=SOR_RED_BLACK, arithmetic=ARITH_EXACT, precision=PREC_FP64,
                  strict_eps=False, inner_sweeps=0, execution=0, norm_cells=NORM_ALL_INTERIOR,
                  sweep_schedule=0):
+        rule = int(strict_eps) if not isinstance(strict_eps, bool) else int(strict_eps)
         m = _lib.Mode(sor_order=sor_order, arithmetic=arithmetic, precision=precision,
-                      strict_eps=1 if strict_eps else 0, inner_sweeps=inner_sweeps,
+                      strict_eps=rule, inner_sweeps=inner_sweeps,
                       execution=execution, norm_cells=norm_cells, sweep_schedule=sweep_schedule)
         _lib.check(_lib.load().strm_set_mode(self._h, ctypes.byref(m)))
         self.mode = {"sor_order": sor_order, "arithmetic": arithmetic, "precision": precision,
-                     "strict_eps": bool(strict_eps), "inner_sweeps": inner_sweeps,
+                     "strict_eps": rule, "inner_sweeps": inner_sweeps,
                      "execution": execution, "norm_cells": norm_cells,
                      "sweep_schedule": sweep_schedule}
 

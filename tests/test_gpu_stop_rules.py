@@ -1,0 +1,39 @@
+"""Stop rules and residual histories of the pressure solve: the relative
+rule ends each solve at the first norm below eps^2 x the norm it started
+from, in FP64 and in mixed precision, in graph and eager execution."""
+import numpy as np
+import pytest
+
+from stroemung_gb300 import _lib, presets
+from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, Simulation
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_MIXED])
+@pytest.mark.parametrize("execution", [_lib.EXEC_GRAPH, _lib.EXEC_EAGER])
+def test_relative_rule_stops_at_first_norm_below_target(precision, execution):
+    eps = 1e-3
+    sim = Simulation(grid=presets.cavity(64), cell_size=(1 / 64, 1 / 64), delt=1e-3, gamma=0.9,
+                     reynolds=100.0, sor_absolute_epsilon=eps, max_iterations=5000, omega=1.8,
+                     tau=0.5, precision=precision, strict_eps=_lib.STOP_RELATIVE,
+                     execution=execution)
+    for _ in range(3):
+        it, ns = sim.run_simulation_tick()
+        h = sim.residual_history()
+        assert h[0, 0] == 0  # the starting norm
+        start = h[0, 1]
+        assert ns == h[-1, 1] and it == int(h[-1, 0])
+        assert ns < eps * eps * start
+        # no earlier recorded norm met the target
+        assert not (h[1:-1, 1] < eps * eps * start).any()
+        assert sim.state()["last_converged"]
+    sim.close()
+
+
+def test_relative_rule_is_refused_for_the_lexicographic_order():
+    sim = Simulation(grid=presets.cavity(16), cell_size=(1 / 16, 1 / 16), delt=1e-3, gamma=0.9,
+                     reynolds=100.0, max_iterations=10)
+    with pytest.raises(Exception):
+        sim.set_mode(sor_order=_lib.SOR_LEXICOGRAPHIC, strict_eps=_lib.STOP_RELATIVE)
+    sim.close()
