@@ -511,6 +511,34 @@ def batched_block(args):
     }
 
 
+def profile_target(what: str, steps: int) -> None:
+    """Small workloads for ncu (no timing, no JSON): `fp64` / `mixed` run
+    `steps` steps of the 4096 x 1024 channel with eager execution (every
+    kernel a separate launch); `sweeps` runs 16 FP32 sweeps of the mixed
+    solve after one step; `conv` runs two U-Net forwards at 4096 x 1024."""
+    import torch
+    from stroemung_gb300 import _lib
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    if what == "conv":
+        from stroemung_gb300.unet import UNet
+        net = UNet(seed=0)
+        x = torch.zeros(1, IMAX, JMAX, 8, dtype=torch.bfloat16, device="cuda")
+        for _ in range(2):
+            net.forward(x, 1, IMAX, JMAX)
+        torch.cuda.synchronize()
+        return
+    prec = PREC_FP64 if what == "fp64" else PREC_MIXED
+    sim = Simulation(grid=workload(SEED), precision=prec, arithmetic=ARITH_FAST,
+                     execution=_lib.EXEC_EAGER if what != "sweeps" else _lib.EXEC_GRAPH,
+                     **PARAMS)
+    for _ in range(steps):
+        print(sim.run_simulation_tick())
+    if what == "sweeps":
+        sim.sor_sweeps(16)
+    sim.synchronize()
+    sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -541,7 +569,12 @@ def main():
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-seq-sample", type=int, default=16)
+    ap.add_argument("--profile", default="", choices=["", "fp64", "mixed", "sweeps", "conv"],
+                    help="run a small workload for ncu instead of the benchmark")
     args = ap.parse_args()
+    if args.profile:
+        profile_target(args.profile, max(args.steps if args.steps != 10 else 1, 1))
+        return
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)

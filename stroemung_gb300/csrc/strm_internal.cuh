@@ -62,6 +62,8 @@ struct StepState {
   unsigned int nonfinite;   // last norm was NaN/Inf
   unsigned int body_count;  // launches of the pressure-loop body this step
   unsigned int overrun;     // the loop passed its bound without the normal stop
+  unsigned int replay;      // mixed solve: 1 redo the last outer iteration sweep by
+                            // sweep, 2 finish the remaining sweeps one by one
   // ordered-bit encodings of the ranges (see ord_enc); speeds are squared
   unsigned long long p_min, p_max, s2_min, s2_max;
   unsigned long long umax_bits, vmax_bits;

@@ -164,6 +164,7 @@ __device__ __forceinline__ void step_begin(StepState *st, const Consts &c, doubl
   st->body_count = 0;
   st->overrun = 0;
   st->hist_n = 0;
+  st->replay = 0;
 }
 
 __global__ void __cluster_dims__(BC_CLUSTER, 1, 1) __launch_bounds__(BC_THREADS)
@@ -783,12 +784,13 @@ __device__ __forceinline__ float copy32(const float *e, size_t o, int pitch, int
 // One colour over the whole grid: fluid interior cells of the colour get the
 // SOR update, boundary cells of the colour with an edge get the copy (when
 // copy_boundary is set).
-__global__ void __launch_bounds__(256)
-    sor32_color_kernel(float *__restrict__ e, const float *__restrict__ s,
-                       const uint8_t *__restrict__ flags, Geom g, Consts32 k, int color,
-                       int copy_boundary) {
-  const int x = blockIdx.y * blockDim.y + threadIdx.y;
-  const int y = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((x + color) & 1);
+__device__ __forceinline__ void sor32_color_cells(float *__restrict__ e,
+                                                  const float *__restrict__ s,
+                                                  const uint8_t *__restrict__ flags,
+                                                  const Geom &g, const Consts32 &k, int color,
+                                                  int copy_boundary, int bx, int by) {
+  const int x = by * blockDim.y + threadIdx.y;
+  const int y = 2 * (bx * blockDim.x + threadIdx.x) + ((x + color) & 1);
   if (x >= g.nx || y >= g.ny) return;
   const size_t o = OFF(x, y);
   const uint8_t fl = flags[o];
@@ -800,6 +802,13 @@ __global__ void __launch_bounds__(256)
   } else if (copy_boundary && edge_of(fl) != E_NONE) {
     e[o] = s[o] + copy32(e, o, g.pitch, edge_of(fl));
   }
+}
+
+__global__ void __launch_bounds__(256)
+    sor32_color_kernel(float *__restrict__ e, const float *__restrict__ s,
+                       const uint8_t *__restrict__ flags, Geom g, Consts32 k, int color,
+                       int copy_boundary) {
+  sor32_color_cells(e, s, flags, g, k, color, copy_boundary, blockIdx.x, blockIdx.y);
 }
 
 // Temporal blocking of the same sweeps: one CTA loads a TX x TY tile of the
@@ -833,6 +842,15 @@ __device__ __forceinline__ float copy_rb(int code, float up, float dn, float lf,
   }
 }
 
+// Cell code of one flag byte for the blocked sweeps.
+__device__ __forceinline__ uint8_t tb_code(uint8_t fl, int x, int y, const Geom &g) {
+  if (fl == 0) return (x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2) ? 0 : kFrozen;
+  return edge_of(fl) != E_NONE ? edge_of(fl) : kFrozen;
+}
+
+// One tile.  Extended rows are EY = 128 cells wide, so each colour row is 64
+// words and every lane owns two neighbouring compacted cells (j, j+1): the
+// four cells y = 4*lane .. 4*lane+3 of a row land as one pair per colour.
 template <int H, int TX, int TY>
 __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
                                               float *__restrict__ eout,
@@ -840,71 +858,127 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
                                               const uint8_t *__restrict__ flags, const Geom &g,
                                               const Consts32 &k, int tile, int tiles_y, int n,
                                               int skip_last_copy, unsigned char *smem_raw) {
-  static_assert(H % 2 == 0 && TX % 2 == 0 && TY % 2 == 0, "tile origins must be even");
-  constexpr int EX = TX + 2 * H, EY = TY + 2 * H, W = EY / 2, NC = EX * W;
+  static_assert(H % 4 == 0 && TX % 2 == 0 && TY % 4 == 0, "tile origins must be multiples of 4");
+  static_assert(TY + 2 * H == 128, "extended rows are 128 cells");
+  constexpr int EX = TX + 2 * H, EY = 128, W = EY / 2, NC = EX * W;
   constexpr int WARPS = 16;
-  float *se = reinterpret_cast<float *>(smem_raw);  // [2][EX][W]
-  float *ss = se + 2 * NC;                            // [2][EX][W]
+  float *se = reinterpret_cast<float *>(smem_raw);         // [2][EX][W]
+  float *ss = se + 2 * NC;                                   // [2][EX][W]
   uint8_t *sc = reinterpret_cast<uint8_t *>(ss + 2 * NC);  // [2][EX][W]: 0 SOR, 1..8 copy, kFrozen
   const int gx0 = (tile / tiles_y) * TX - H;
   const int gy0 = (tile % tiles_y) * TY - H;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j0 = 2 * lane;  // this lane's compacted pair in every row
+  // load: lane takes cells y0 .. y0+3 of each row (16-byte aligned: the tile
+  // origin and the pitch are multiples of 4 cells)
+  static_assert(EX % WARPS == 0, "rows per warp");
+#pragma unroll
   for (int lx = warp; lx < EX; lx += WARPS) {
     const int x = gx0 + lx;
-    for (int ly = lane; ly < EY; ly += 32) {
-      const int y = gy0 + ly;
-      const int i = ((lx + ly) & 1) * NC + lx * W + (ly >> 1);
-      float ev = 0.0f, sv = 0.0f;
-      uint8_t code = kFrozen;
-      if (x >= 0 && y >= 0 && x < g.nx && y < g.ny) {
-        const size_t o = OFF(x, y);
-        ev = ein[o];
-        sv = s[o];
-        const uint8_t fl = flags[o];
-        if (fl == 0) {
-          if (x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2) code = 0;
-        } else if (edge_of(fl) != E_NONE) {
-          code = edge_of(fl);
+    const int y0 = gy0 + 4 * lane;
+    float ev[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint8_t cv[4] = {kFrozen, kFrozen, kFrozen, kFrozen};
+    if (x >= 0 && x < g.nx) {
+      if (y0 >= 0 && y0 + 3 < g.ny) {
+        const size_t o = OFF(x, y0);
+        const float4 e4 = *reinterpret_cast<const float4 *>(ein + o);
+        const float4 s4 = *reinterpret_cast<const float4 *>(s + o);
+        const uchar4 f4 = *reinterpret_cast<const uchar4 *>(flags + o);
+        ev[0] = e4.x; ev[1] = e4.y; ev[2] = e4.z; ev[3] = e4.w;
+        sv[0] = s4.x; sv[1] = s4.y; sv[2] = s4.z; sv[3] = s4.w;
+        cv[0] = tb_code(f4.x, x, y0, g);
+        cv[1] = tb_code(f4.y, x, y0 + 1, g);
+        cv[2] = tb_code(f4.z, x, y0 + 2, g);
+        cv[3] = tb_code(f4.w, x, y0 + 3, g);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int y = y0 + q;
+          if (y >= 0 && y < g.ny) {
+            const size_t o = OFF(x, y);
+            ev[q] = ein[o];
+            sv[q] = s[o];
+            cv[q] = tb_code(flags[o], x, y, g);
+          }
         }
       }
-      se[i] = ev;
-      ss[i] = sv;
-      sc[i] = code;
     }
+    // cells 0, 2 have colour c0 = (lx + 4 lane) & 1 = lx & 1 (local = global colour)
+    const int c0 = lx & 1;
+    const int i0 = c0 * NC + lx * W + j0, i1 = (1 - c0) * NC + lx * W + j0;
+    *reinterpret_cast<float2 *>(se + i0) = make_float2(ev[0], ev[2]);
+    *reinterpret_cast<float2 *>(se + i1) = make_float2(ev[1], ev[3]);
+    *reinterpret_cast<float2 *>(ss + i0) = make_float2(sv[0], sv[2]);
+    *reinterpret_cast<float2 *>(ss + i1) = make_float2(sv[1], sv[3]);
+    *reinterpret_cast<uchar2 *>(sc + i0) = make_uchar2(cv[0], cv[2]);
+    *reinterpret_cast<uchar2 *>(sc + i1) = make_uchar2(cv[1], cv[3]);
   }
   __syncthreads();
+  // Each pass updates the colour on rows lo..hix, every column: a cell outside
+  // the region that is still exact gets a value from inexact neighbours, but
+  // no cell inside it ever reads such a value (the regions shrink by one cell
+  // per pass), and columns 0 / W-1 read the neighbouring row's edge word,
+  // which stays inside the tile.  Frozen cells keep their value; boundary
+  // cells take the copy.
   for (int pass = 0; pass < 2 * n; ++pass) {
     const int c = pass & 1;
     const bool copy = !(skip_last_copy && pass == 2 * n - 1);
-    const int lo = pass + 1, hix = EX - 2 - pass, hiy = EY - 2 - pass;
+    const int lo = pass + 1, hix = EX - 2 - pass;
     float *ec = se + c * NC;
     const float *eo = se + (1 - c) * NC;
-    const float *sv = ss + c * NC;
+    const float *svc = ss + c * NC;
     const uint8_t *cc = sc + c * NC;
     for (int lx = lo + warp; lx <= hix; lx += WARPS) {
       const int p = (lx + c) & 1;
-      const int jlo = (lo - p + 1) >> 1, jhi = (hiy - p) >> 1;
-      const int row = lx * W;
-      for (int j = jlo + lane; j <= jhi; j += 32) {
-        const int i = row + j;
-        const uint8_t code = cc[i];
-        if (code == 0) {
-          const float sum_x = eo[i - W] + eo[i + W];
-          const float sum_y = eo[i - 1 + p] + eo[i + p];
-          ec[i] = fmaf(k.omw, ec[i], fmaf(k.a, sum_x, fmaf(k.b, sum_y, sv[i])));
-        } else if (copy && code != kFrozen) {
-          ec[i] = sv[i] + copy_rb(code, eo[i - W], eo[i + W], eo[i - 1 + p], eo[i + p]);
-        }
+      const int i = lx * W + j0;
+      const uchar2 cd = *reinterpret_cast<const uchar2 *>(cc + i);
+      const float2 cur = *reinterpret_cast<const float2 *>(ec + i);
+      const float2 sv2 = *reinterpret_cast<const float2 *>(svc + i);
+      const float2 up = *reinterpret_cast<const float2 *>(eo + i - W);
+      const float2 dn = *reinterpret_cast<const float2 *>(eo + i + W);
+      const float2 mid = *reinterpret_cast<const float2 *>(eo + i);
+      // neighbours along y of cell j: (j-1+p, j+p) in the other colour
+      float lf0, rt0, lf1, rt1;
+      if (p) {
+        lf0 = mid.x;
+        rt0 = mid.y;
+        lf1 = mid.y;
+        rt1 = eo[i + 2];
+      } else {
+        lf0 = eo[i - 1];
+        rt0 = mid.x;
+        lf1 = mid.x;
+        rt1 = mid.y;
       }
+      const float s0 = fmaf(k.omw, cur.x, fmaf(k.a, up.x + dn.x, fmaf(k.b, lf0 + rt0, sv2.x)));
+      const float s1 = fmaf(k.omw, cur.y, fmaf(k.a, up.y + dn.y, fmaf(k.b, lf1 + rt1, sv2.y)));
+      float2 res = make_float2(cd.x == 0 ? s0 : cur.x, cd.y == 0 ? s1 : cur.y);
+      if ((cd.x | cd.y) != 0 && copy) {  // boundary cells of this pair (rare)
+        if (cd.x != 0 && cd.x != kFrozen) res.x = sv2.x + copy_rb(cd.x, up.x, dn.x, lf0, rt0);
+        if (cd.y != 0 && cd.y != kFrozen) res.y = sv2.y + copy_rb(cd.y, up.y, dn.y, lf1, rt1);
+      }
+      *reinterpret_cast<float2 *>(ec + i) = res;
     }
     __syncthreads();
   }
-  for (int lx = H + warp; lx < H + TX; lx += WARPS) {
-    const int x = gx0 + lx;
-    if (x >= g.nx) break;
-    for (int ly = H + lane; ly < H + TY; ly += 32) {
-      const int y = gy0 + ly;
-      if (y < g.ny) eout[OFF(x, y)] = se[((lx + ly) & 1) * NC + lx * W + (ly >> 1)];
+  // write the interior back: lane takes cells 4*lane .. 4*lane+3 of a row
+  const int ly0 = 4 * lane;
+  if (ly0 >= H && ly0 < H + TY) {
+    for (int lx = H + warp; lx < H + TX; lx += WARPS) {
+      const int x = gx0 + lx;
+      if (x >= g.nx) break;
+      const int c0 = lx & 1;
+      const float2 a = *reinterpret_cast<const float2 *>(se + c0 * NC + lx * W + j0);
+      const float2 b = *reinterpret_cast<const float2 *>(se + (1 - c0) * NC + lx * W + j0);
+      const int y0 = gy0 + ly0;
+      if (y0 + 3 < g.ny) {
+        *reinterpret_cast<float4 *>(eout + OFF(x, y0)) = make_float4(a.x, b.x, a.y, b.y);
+      } else {
+        const float v[4] = {a.x, b.x, a.y, b.y};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (y0 + q < g.ny) eout[OFF(x, y0 + q)] = v[q];
+      }
     }
   }
 }
@@ -922,9 +996,12 @@ __global__ void __launch_bounds__(512)
 // p += e on fluid interior cells and boundary cells with an edge (apply != 0),
 // then ez = 0 everywhere (the buffer the next sweeps start from; e itself
 // when the sweeps ended where they started).
+// save (may be NULL): receives p before the update on every cell (the state
+// a sweep-by-sweep redo of this outer iteration starts from).
 __device__ __forceinline__ void refine_cells(double *__restrict__ p, const float *e, float *ez,
                                              const uint8_t *__restrict__ flags, const Geom &g,
-                                             int apply, int bx, int by) {
+                                             int apply, int bx, int by,
+                                             double *__restrict__ save) {
   const int x = by * blockDim.y + threadIdx.y;
   const int y0 = 2 * (bx * blockDim.x + threadIdx.x);
   if (x >= g.nx) return;
@@ -935,6 +1012,7 @@ __device__ __forceinline__ void refine_cells(double *__restrict__ p, const float
     const size_t o = OFF(x, y);
     const uint8_t fl = flags[o];
     const bool fluid_in = fl == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+    if (save) save[o] = p[o];
     if (apply && (fluid_in || (is_bnd(fl) && edge_of(fl) != E_NONE)))
       p[o] = p[o] + (double)e[o];
     ez[o] = 0.0f;
@@ -943,8 +1021,8 @@ __device__ __forceinline__ void refine_cells(double *__restrict__ p, const float
 
 __global__ void __launch_bounds__(256)
     refine_kernel(double *__restrict__ p, const float *e, float *ez,
-                  const uint8_t *__restrict__ flags, Geom g, int apply) {
-  refine_cells(p, e, ez, flags, g, apply, blockIdx.x, blockIdx.y);
+                  const uint8_t *__restrict__ flags, Geom g, int apply, double *save) {
+  refine_cells(p, e, ez, flags, g, apply, blockIdx.x, blockIdx.y, save);
 }
 
 // delta_b = copy(p) - p_b on boundary cells with an edge (FP64, stored FP32
@@ -1039,15 +1117,18 @@ __device__ __forceinline__ void mixed_residual_partial(
 }
 
 // The norm from the partials and the stop rule (every thread of one block
-// calls it; thread 0 updates the state).  Returns, in thread 0, whether the
-// solve goes on.
-__device__ __forceinline__ bool mixed_residual_stop(const double *partials, int nblocks,
-                                                    StepState *st, const Consts &c,
-                                                    unsigned int itermax, int strict, int sweeps,
-                                                    int check) {
+// calls it; thread 0 updates the state).  Returns, in thread 0, SOLVE_GO_ON,
+// SOLVE_DONE (the stop rule fired) or SOLVE_NO_ROOM (another `sweeps` would
+// pass max_iterations).
+enum : int { SOLVE_GO_ON = 0, SOLVE_DONE = 1, SOLVE_NO_ROOM = 2 };
+
+__device__ __forceinline__ int mixed_residual_stop(const double *partials, int nblocks,
+                                                   StepState *st, const Consts &c,
+                                                   unsigned int itermax, int strict, int sweeps,
+                                                   int check) {
   const bool mean_free = (strict & STOP_FLUID_NORM) && (strict & STOP_MEAN_FREE);
   const double ns = finish_norm(partials, nblocks, mean_free, st->fluid_cells);
-  bool go_on = true;
+  int status = SOLVE_GO_ON;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->ns = ns;
     hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
@@ -1060,21 +1141,36 @@ __device__ __forceinline__ bool mixed_residual_stop(const double *partials, int 
       const bool room = it + sweeps <= itermax;
       if (done) st->converged = 1;
       else if (!room) st->exhausted = 1;
-      go_on = !(done || !room);
+      status = done ? SOLVE_DONE : (room ? SOLVE_GO_ON : SOLVE_NO_ROOM);
     }
   }
-  return go_on;
+  return status;
 }
 
+// After a coarse (m sweeps per check) loop stopped: which finishing pass the
+// solve needs so that it ends at the sweep the per-sweep rule would.
+__device__ __forceinline__ unsigned int replay_of(int status, const StepState *st,
+                                                  unsigned int itermax) {
+  if (status == SOLVE_DONE) return 1u;                                 // redo sweep by sweep
+  if (status == SOLVE_NO_ROOM && st->sor_iters < itermax) return 2u;  // the remainder
+  return 0u;
+}
+
+// check: 0 the solve's starting norm, 1 a stop test after `sweeps` sweeps,
+// 2 the defect only (no norm, no state change).  coarse: the loop checks
+// every `sweeps` > 1 sweeps; when it stops, st->replay says how the solve
+// finishes (and, in a graph, h_replay opens the finishing pass).
 template <bool IN_GRAPH>
 __global__ void __launch_bounds__(256)
     mixed_residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
                           const uint8_t *__restrict__ flags, float *__restrict__ s, Geom g,
                           Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
                           cudaGraphConditionalHandle h, unsigned int itermax, int strict,
-                          int sweeps, int check) {
+                          int sweeps, int check, cudaGraphConditionalHandle h_replay,
+                          int coarse) {
   mixed_residual_partial(p, rhs, flags, s, g, c, partials, tiles_y, ntiles, strict, blockIdx.x,
                          gridDim.x);
+  if (check == 2) return;
   if (IN_GRAPH && check && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     // independent bound on the WHILE loop, as in residual_kernel
     const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
@@ -1084,11 +1180,43 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (!last_block_done(&st->counter)) return;
-  const bool go_on = mixed_residual_stop(partials, gridDim.x, st, c, itermax, strict, sweeps,
+  const int status = mixed_residual_stop(partials, gridDim.x, st, c, itermax, strict, sweeps,
                                          check);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->counter = 0;
-    if (IN_GRAPH && check && !go_on) cudaGraphSetConditional(h, 0);
+    if (check && status != SOLVE_GO_ON) {
+      if (coarse) {
+        st->replay = replay_of(status, st, itermax);
+        if (IN_GRAPH && st->replay) cudaGraphSetConditional(h_replay, 1);
+      }
+      if (IN_GRAPH) cudaGraphSetConditional(h, 0);
+    }
+  }
+}
+
+// Start of a sweep-by-sweep finishing pass: with replay 1, p returns to its
+// value before the last outer iteration (saved in pw) and the iteration
+// count and residual history drop that iteration.
+__global__ void __launch_bounds__(256)
+    restore_kernel(double *__restrict__ p, const double *__restrict__ pw, Geom g, StepState *st,
+                   int sweeps) {
+  const unsigned int replay = st->replay;
+  if (replay == 2u && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    st->exhausted = 0;  // the remaining sweeps follow one by one
+  if (replay != 1u) return;
+  const int x = blockIdx.y * blockDim.y + threadIdx.y;
+  const int y0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (x < g.nx) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = y0 + q;
+      if (y < g.ny) p[OFF(x, y)] = pw[OFF(x, y)];
+    }
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    st->sor_iters -= (unsigned int)sweeps;
+    if (st->hist_n > 0) st->hist_n -= 1;
+    st->converged = 0;
   }
 }
 
@@ -1524,20 +1652,53 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     if ((e = tb_prepare()) != cudaSuccess) return e;
     float *final = nullptr;
     const std::vector<SweepLaunch> plan = sweep_plan(d, g, m, r.sweep_schedule, &final);
-    refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0);
+    const int coarse = m > 1 ? 1 : 0;
+    refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0, nullptr);
     launch_delta(d, g, s);
     mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
                                                           d.partials, ty_int, nt_int, 0,
-                                                          r.itermax, r.strict_eps, m, 0);
+                                                          r.itermax, r.strict_eps, m, 0, 0, coarse);
     while (!done) {
       for (const SweepLaunch &l : plan)
         if ((e = issue_sweep(l, d.r32, d.flags, g, k32, s)) != cudaSuccess) return e;
-      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1);
+      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1,
+                                                coarse ? d.pw : nullptr);
       launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
-                                                            r.itermax, r.strict_eps, m, 1);
+                                                            r.itermax, r.strict_eps, m, 1, 0,
+                                                            coarse);
       if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
+    }
+    unsigned int replay = 0;
+    if (coarse) {
+      if ((e = cudaMemcpyAsync(&h->replay, &d.st->replay, sizeof(unsigned int),
+                               cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return e;
+      replay = h->replay;
+    }
+    if (replay) {
+      // finish sweep by sweep so that the solve stops where a per-sweep test would
+      restore_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.pw, g, d.st, m);
+      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0, nullptr);
+      launch_delta(d, g, s);
+      mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
+                                                            d.st, d.partials, ty_int, nt_int, 0,
+                                                            r.itermax, r.strict_eps, 1, 2, 0, 0);
+      done = false;
+      while (!done) {
+        for (int color = 0; color < 2; ++color)
+          sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color,
+                                                         color == 0 ? 1 : 0);
+        refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 1, nullptr);
+        launch_delta(d, g, s);
+        mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
+                                                              d.st, d.partials, ty_int, nt_int,
+                                                              0, r.itermax, r.strict_eps, 1, 1, 0,
+                                                              0);
+        if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
+      }
     }
   } else if (nt_int > 0 && r.itermax > 0) {
     dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
@@ -1679,14 +1840,19 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
     n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
-                 (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0);
+                 (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0, (double *)nullptr);
     if (d.n_pcopy > 0)
       n = b.kernel(b.graph, n, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
                    dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
                    d.n_pcopy, g.pitch);
+    const int coarse = m > 1 ? 1 : 0;
+    cudaGraphConditionalHandle h_rep{};
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphConditionalHandleCreate(&h_rep, b.graph, 0, cudaGraphCondAssignDefault);
     n = b.kernel(b.graph, n, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                  (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32, g,
-                 c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 0);
+                 c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 0, h_rep,
+                 coarse);
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
@@ -1707,17 +1873,78 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                              (const float *)d.r32, (const uint8_t *)d.flags, g, k32, l.tiles_y,
                              l.n, l.skip_last_copy);
       }
+      // the refinement also keeps p before this outer iteration (for a redo)
       bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
-                    (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1);
+                    (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1,
+                    coarse ? d.pw : (double *)nullptr);
       if (d.n_pcopy > 0)
         bn = b.kernel(body, bn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
                       dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
                       d.n_pcopy, g.pitch);
       bn = b.kernel(body, bn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                     (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32,
-                    g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 1);
+                    g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 1,
+                    h_rep, coarse);
     }
     n = wnode;
+    if (coarse) {
+      // IF the coarse loop stopped between checks: redo / finish sweep by sweep
+      cudaGraphNodeParams ip = {};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = h_rep;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      cudaGraphNode_t inode = nullptr;
+      if (b.err == cudaSuccess)
+        b.err = cudaGraphAddNode(&inode, b.graph, &n, nullptr, 1, &ip);
+      if (b.err == cudaSuccess) {
+        cudaGraph_t ib = ip.conditional.phGraph_out[0];
+        cudaGraphNode_t fn = nullptr;
+        fn = b.kernel(ib, fn, (const void *)restore_kernel, pgrid, kRedBlock, d.p,
+                      (const double *)d.pw, g, d.st, m);
+        fn = b.kernel(ib, fn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
+                      (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0,
+                      (double *)nullptr);
+        if (d.n_pcopy > 0)
+          fn = b.kernel(ib, fn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
+                        dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
+                        d.n_pcopy, g.pitch);
+        cudaGraphConditionalHandle h_fine{};
+        if (b.err == cudaSuccess)
+          b.err = cudaGraphConditionalHandleCreate(&h_fine, ib, 1, cudaGraphCondAssignDefault);
+        fn = b.kernel(ib, fn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
+                      (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags,
+                      d.r32, g, c, d.st, d.partials, ty_int, nt_int, h_fine, r.itermax,
+                      r.strict_eps, 1, 2, h_fine, 0);
+        cudaGraphNodeParams fp = {};
+        fp.type = cudaGraphNodeTypeConditional;
+        fp.conditional.handle = h_fine;
+        fp.conditional.type = cudaGraphCondTypeWhile;
+        fp.conditional.size = 1;
+        cudaGraphNode_t fw = nullptr;
+        if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&fw, ib, &fn, nullptr, 1, &fp);
+        if (b.err == cudaSuccess) {
+          cudaGraph_t fb = fp.conditional.phGraph_out[0];
+          cudaGraphNode_t x = nullptr;
+          for (int color = 0; color < 2; ++color)
+            x = b.kernel(fb, x, (const void *)sor32_color_kernel, pgrid, kRedBlock, d.e32,
+                         (const float *)d.r32, (const uint8_t *)d.flags, g, k32, color,
+                         color == 0 ? 1 : 0);
+          x = b.kernel(fb, x, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
+                       (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 1,
+                       (double *)nullptr);
+          if (d.n_pcopy > 0)
+            x = b.kernel(fb, x, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
+                         dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
+                         d.n_pcopy, g.pitch);
+          x = b.kernel(fb, x, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
+                       (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags,
+                       d.r32, g, c, d.st, d.partials, ty_int, nt_int, h_fine, r.itermax,
+                       r.strict_eps, 1, 1, h_fine, 0);
+        }
+      }
+      n = inode;
+    }
   } else if (nt_int > 0 && r.itermax > 0) {
     cudaGraphConditionalHandle h;
     if (b.err == cudaSuccess)
@@ -1790,6 +2017,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
 
 struct BInst {
   double *p, *rhs;
+  double *pw;            // p before the current coarse outer iteration
   const uint8_t *flags;
   float *e32, *e32b, *r32;
   StepState *st;
@@ -1812,29 +2040,37 @@ struct BatchState {
   unsigned int body_count;
   unsigned int overrun;
   unsigned int launches;  // independent count of loop bodies (block 0)
+  unsigned int replays;   // members that finish sweep by sweep
 };
 
 __device__ __forceinline__ bool inst_stopped(const StepState *st) {
   return st->converged || st->exhausted;
 }
 
+// Phase of the batched solve a kernel serves: the coarse loop (m sweeps per
+// check; every solving member until it stops) or the sweep-by-sweep
+// finishing pass (members whose coarse loop stopped between checks).
+__device__ __forceinline__ bool in_phase(const BInst &b, int fine) {
+  return b.solve && (!fine || b.st->replay != 0u);
+}
+
 __global__ void __launch_bounds__(256)
     batch_refine_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int apply,
-                        int final_b) {
+                        int final_b, int fine, int save) {
   const int2 e = tab[blockIdx.x];
   const BInst &b = I[e.x];
-  if (!b.solve || (apply && inst_stopped(b.st))) return;
+  if (!in_phase(b, fine) || (apply && inst_stopped(b.st))) return;
   refine_cells(b.p, final_b ? b.e32b : b.e32, b.e32, b.flags, b.g, apply, e.y % b.pgx,
-               e.y / b.pgx);
+               e.y / b.pgx, (apply && !fine && save) ? b.pw : nullptr);
 }
 
 __global__ void batch_delta_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab,
-                                   int n, int check) {
+                                   int n, int check, int fine) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int2 e = tab[k];
   const BInst &b = I[e.x];
-  if (!b.solve || (check && inst_stopped(b.st))) return;
+  if (!in_phase(b, fine) || (check && inst_stopped(b.st))) return;
   delta_entry(b.p, b.r32, b.e32, b.pcopy[e.y], b.g.pitch);
 }
 
@@ -1851,10 +2087,46 @@ __global__ void __launch_bounds__(512)
 }
 
 __global__ void __launch_bounds__(256)
-    batch_residual_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int check) {
+    batch_restore_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int m) {
   const int2 e = tab[blockIdx.x];
   const BInst &b = I[e.x];
-  if (!b.solve || (check && inst_stopped(b.st))) return;
+  if (!b.solve) return;
+  StepState *st = b.st;
+  const unsigned int replay = st->replay;
+  const bool lead = e.y == 0 && threadIdx.x == 0 && threadIdx.y == 0;
+  if (replay == 2u && lead) st->exhausted = 0;
+  if (replay != 1u) return;
+  const Geom &g = b.g;
+  const int x = (e.y / b.pgx) * blockDim.y + threadIdx.y;
+  const int y0 = 2 * ((e.y % b.pgx) * blockDim.x + threadIdx.x);
+  if (x < g.nx) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (y0 + q < g.ny) b.p[OFF(x, y0 + q)] = b.pw[OFF(x, y0 + q)];
+  }
+  if (lead) {
+    st->sor_iters -= (unsigned int)m;
+    if (st->hist_n > 0) st->hist_n -= 1;
+    st->converged = 0;
+  }
+}
+
+// One colour pass of the finishing members
+__global__ void __launch_bounds__(256)
+    batch_color_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int color,
+                       int copy) {
+  const int2 e = tab[blockIdx.x];
+  const BInst &b = I[e.x];
+  if (!in_phase(b, 1) || inst_stopped(b.st)) return;
+  sor32_color_cells(b.e32, b.r32, b.flags, b.g, b.k32, color, copy, e.y % b.pgx, e.y / b.pgx);
+}
+
+__global__ void __launch_bounds__(256)
+    batch_residual_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int check,
+                          int fine) {
+  const int2 e = tab[blockIdx.x];
+  const BInst &b = I[e.x];
+  if (!in_phase(b, fine) || (check == 1 && inst_stopped(b.st))) return;
   mixed_residual_partial(b.p, b.rhs, b.flags, b.r32, b.g, b.c, b.partials, b.ty_int, b.nt_int,
                          b.strict, e.y, b.nb);
 }
@@ -1865,15 +2137,15 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     batch_finish_kernel(const BInst *__restrict__ I, int n, BatchState *bs,
                         cudaGraphConditionalHandle h, int sweeps, int check,
-                        unsigned int itermax_all) {
+                        unsigned int itermax_all, int fine, cudaGraphConditionalHandle h_rep) {
   const BInst &b = I[blockIdx.x];
-  const bool active = b.solve && !(check && inst_stopped(b.st));
+  const bool active = in_phase(b, fine) && !(check && inst_stopped(b.st));
   if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     // Independent bound on the WHILE loop: the normal stop below ends it
     // after max max_iterations / sweeps bodies at the latest; should that
     // bookkeeping ever fail, this ends it two bodies later.
     if (!check) {
-      bs->launches = 0;
+      if (!fine) bs->launches = 0;
     } else {
       const unsigned int l = atomicAdd(&bs->launches, 1u) + 1;
       if ((unsigned long long)l * sweeps >= itermax_all + 2ull * sweeps) {
@@ -1883,11 +2155,16 @@ __global__ void __launch_bounds__(256)
     }
   }
   __syncthreads();
-  bool go_on = false;
+  int status = SOLVE_GO_ON;
   if (active)
-    go_on = mixed_residual_stop(b.partials, b.nb, b.st, b.c, b.itermax, b.strict, sweeps, check);
+    status = mixed_residual_stop(b.partials, b.nb, b.st, b.c, b.itermax, b.strict, sweeps, check);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    if (active && go_on) atomicAdd(&bs->active, 1u);
+    if (active && status == SOLVE_GO_ON) atomicAdd(&bs->active, 1u);
+    if (active && check && status != SOLVE_GO_ON && !fine && sweeps > 1) {
+      const unsigned int rp = replay_of(status, b.st, b.itermax);
+      b.st->replay = rp;
+      if (rp) atomicAdd(&bs->replays, 1u);
+    }
     __threadfence();
     const unsigned int t = atomicAdd(&bs->counter, 1u);
     if (t == (unsigned int)n - 1) {
@@ -1898,12 +2175,14 @@ __global__ void __launch_bounds__(256)
         bs->body_count = body;
         if (act == 0) {
           cudaGraphSetConditional(h, 0);
+          if (!fine && atomicAdd(&bs->replays, 0u) > 0) cudaGraphSetConditional(h_rep, 1);
         } else if ((unsigned long long)body * sweeps >= itermax_all + 2ull * sweeps) {
           bs->overrun = 1;
           cudaGraphSetConditional(h, 0);
         }
-      } else {
+      } else if (!fine) {
         bs->body_count = 0;
+        bs->replays = 0;
       }
       bs->active = 0;
       bs->counter = 0;
@@ -1952,6 +2231,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     BInst &b = inst[i];
     b.p = d.p;
     b.rhs = d.rhs;
+    b.pw = d.pw;
     b.flags = d.flags;
     b.e32 = d.e32;
     b.e32b = d.e32b;
@@ -2038,15 +2318,19 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   if (b.err == cudaSuccess)
     b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
   if (nres > 0) {
+    cudaGraphConditionalHandle h_rep{};
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphConditionalHandleCreate(&h_rep, b.graph, 0, cudaGraphCondAssignDefault);
+    const dim3 g_del((ndel + 255) / 256);
     nd = b.kernel(b.graph, nd, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
-                  d_ref, 0, 0);
+                  d_ref, 0, 0, 0, 0);
     if (ndel > 0)
-      nd = b.kernel(b.graph, nd, (const void *)batch_delta_kernel, dim3((ndel + 255) / 256),
-                    dim3(256), d_inst, d_del, ndel, 0);
+      nd = b.kernel(b.graph, nd, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
+                    d_del, ndel, 0, 0);
     nd = b.kernel(b.graph, nd, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
-                  d_inst, d_res, 0);
+                  d_inst, d_res, 0, 0);
     nd = b.kernel(b.graph, nd, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
-                  d_bs, h, m, 0, itermax_all);
+                  d_bs, h, m, 0, itermax_all, 0, h_rep);
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
@@ -2064,16 +2348,66 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
                            d_inst, d_tb, cnt, done + cnt >= m ? 1 : 0, launches & 1);
       }
       bn = b.kernel(body, bn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
-                    d_ref, 1, launches & 1);
+                    d_ref, 1, launches & 1, 0, m > 1 ? 1 : 0);
       if (ndel > 0)
-        bn = b.kernel(body, bn, (const void *)batch_delta_kernel, dim3((ndel + 255) / 256),
-                      dim3(256), d_inst, d_del, ndel, 1);
+        bn = b.kernel(body, bn, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
+                      d_del, ndel, 1, 0);
       bn = b.kernel(body, bn, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
-                    d_inst, d_res, 1);
+                    d_inst, d_res, 1, 0);
       bn = b.kernel(body, bn, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
-                    d_bs, h, m, 1, itermax_all);
+                    d_bs, h, m, 1, itermax_all, 0, h_rep);
     }
     nd = wnode;
+    if (m > 1) {
+      // members whose coarse loop stopped between checks finish sweep by sweep
+      cudaGraphNodeParams ip = {};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = h_rep;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      cudaGraphNode_t inode = nullptr;
+      if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&inode, b.graph, &nd, nullptr, 1, &ip);
+      if (b.err == cudaSuccess) {
+        cudaGraph_t ib = ip.conditional.phGraph_out[0];
+        cudaGraphNode_t fn = nullptr;
+        fn = b.kernel(ib, fn, (const void *)batch_restore_kernel, dim3(nref), kRedBlock, d_inst,
+                      d_ref, m);
+        fn = b.kernel(ib, fn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
+                      d_ref, 0, 0, 1, 0);
+        if (ndel > 0)
+          fn = b.kernel(ib, fn, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
+                        d_del, ndel, 0, 1);
+        fn = b.kernel(ib, fn, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
+                      d_inst, d_res, 2, 1);
+        cudaGraphConditionalHandle h_fine{};
+        if (b.err == cudaSuccess)
+          b.err = cudaGraphConditionalHandleCreate(&h_fine, ib, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams fp = {};
+        fp.type = cudaGraphNodeTypeConditional;
+        fp.conditional.handle = h_fine;
+        fp.conditional.type = cudaGraphCondTypeWhile;
+        fp.conditional.size = 1;
+        cudaGraphNode_t fw = nullptr;
+        if (b.err == cudaSuccess) b.err = cudaGraphAddNode(&fw, ib, &fn, nullptr, 1, &fp);
+        if (b.err == cudaSuccess) {
+          cudaGraph_t fb = fp.conditional.phGraph_out[0];
+          cudaGraphNode_t x = nullptr;
+          for (int color = 0; color < 2; ++color)
+            x = b.kernel(fb, x, (const void *)batch_color_kernel, dim3(nref), kRedBlock, d_inst,
+                         d_ref, color, color == 0 ? 1 : 0);
+          x = b.kernel(fb, x, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
+                       d_ref, 1, 0, 1, 0);
+          if (ndel > 0)
+            x = b.kernel(fb, x, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
+                         d_del, ndel, 1, 1);
+          x = b.kernel(fb, x, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
+                       d_inst, d_res, 1, 1);
+          x = b.kernel(fb, x, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
+                       d_bs, h_fine, 1, 1, itermax_all, 1, h_fine);
+        }
+      }
+      nd = inode;
+    }
   }
   // per-instance second halves, in parallel
   for (int i = 0; i < n && b.err == cudaSuccess; ++i) {

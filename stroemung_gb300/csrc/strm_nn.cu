@@ -107,103 +107,176 @@ struct ConvShape {
   int kp;         // padded K = roundup(9*cin_p, 64)
 };
 
+// Pipelined and warp-specialised: warps 0-3 gather the im2col rows (A) and
+// the weights (B) of each 64-wide K chunk into a ring of S shared-memory
+// stages with cp.async (16-byte copies, zero-filled outside the image),
+// keeping LAG stages in flight; warp 4 (one lane) waits for a stage, issues
+// its four MMAs (K = 16 each) and commits them to the stage's "empty"
+// barrier, so the gather of later chunks overlaps the tensor-core work.
+// Warps 0-3 then read the accumulator out of TMEM (warp w owns lanes
+// 32w..32w+31) for the epilogue.  Every wait is bounded; a timeout sets
+// *err and the CTA still releases its TMEM.
 template <int BN>
-__global__ void __launch_bounds__(128)
+struct ConvPipe {
+  // narrow tiles keep fewer stages so that more CTAs (more gathering warps)
+  // share an SM
+  static constexpr int S = BN <= 32 ? 2 : (BN <= 64 ? 3 : 4);  // stages
+  static constexpr int LAG = S - 1 < 2 ? S - 1 : 2;            // gathers in flight per thread
+  static constexpr int A_BYTES = GM * 128;          // 128 rows x 64 BF16
+  static constexpr int B_BYTES = BN * 128;
+  static constexpr int STAGE = A_BYTES + B_BYTES;   // multiple of 1024
+  static constexpr int SMEM = S * STAGE + 1024;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(160)
     conv3x3_fwd_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
                        const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y,
                        float *__restrict__ y32, ConvShape s, int relu, unsigned int *err) {
+  using P = ConvPipe<BN>;
+  constexpr int S = P::S, LAG = P::LAG;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t mbar;
+  __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
   constexpr int TM_COLS = BN < 32 ? 32 : BN;
   const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
-  uint8_t *sA = smem_raw + pad;
-  uint8_t *sB = sA + GM * 128;
+  uint8_t *stage0 = smem_raw + pad;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long npix = (long long)s.batch * s.h * s.w;
   const long long q0 = (long long)blockIdx.x * GM;
+  const int nk = s.kp / GK;
 
-  if (warp == 0) tmem_alloc(&tmem_slot, TM_COLS);
-  if (tid == 0) mbar_init(&mbar, 1);
+  if (warp == 4) tmem_alloc(&tmem_slot, TM_COLS);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 128);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&done, 1);
+    fail = 0;
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = idesc_bf16_f32(GM, BN);
 
-  uint32_t phase = 0;
-  int ok = 1;
-  const uint4 zero4 = make_uint4(0, 0, 0, 0);
-  for (int k0 = 0; k0 < s.kp && ok; k0 += GK) {
-    for (int c = tid; c < GM * 8; c += 128) {
-      const int r = c >> 3, j = c & 7;
-      const long long q = q0 + r;
-      const int k = k0 + 8 * j;
-      const int tap = k / s.cin_p, ch = k - tap * s.cin_p;
-      uint4 val = zero4;
-      if (q < npix && tap < 9) {
-        const int xx = (int)(q % s.w);
-        const long long t = q / s.w;
-        const int yy = (int)(t % s.h);
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-        const int sy = yy + dy, sx = xx + dx;
-        if (sy >= 0 && sy < s.h && sx >= 0 && sx < s.w)
-          val = *reinterpret_cast<const uint4 *>(x + (q + (long long)dy * s.w + dx) * s.cs_in + ch);
+  if (warp < 4) {
+    // ---- producers: thread t owns chunk column j = t % 8 of rows t/8 + 16 i ----
+    // (pixel indices fit in 32 bits: the launcher checks npix < 2^31)
+    const int j = tid & 7, rbase = tid >> 3;
+    int px[8], py[8];
+    const __nv_bfloat16 *prow[8];  // this row's pixel, channel 0 (NULL past the end)
+    {
+      int q = (int)q0 + rbase;
+      int xx = q % s.w, yy = (q / s.w) % s.h;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        px[i] = xx;
+        py[i] = yy;
+        prow[i] = q < npix ? x + (size_t)q * s.cs_in : nullptr;
+        q += 16;
+        xx += 16;
+        while (xx >= s.w) {
+          xx -= s.w;
+          if (++yy == s.h) yy = 0;
+        }
       }
-      *reinterpret_cast<uint4 *>(sA + sw128_offset(r, j)) = val;
     }
-    for (int c = tid; c < BN * 8; c += 128) {
-      const int r = c >> 3, j = c & 7;
-      *reinterpret_cast<uint4 *>(sB + sw128_offset(r, j)) =
-          *reinterpret_cast<const uint4 *>(w + (size_t)r * s.kp + k0 + j * 8);
+    bool ok = true;
+    for (int kc = 0; kc < nk; ++kc) {
+      const int st = kc % S;
+      if (kc >= S && ok) ok = mbar_wait_bounded(&empty[st], ((kc / S) - 1) & 1, kWaitLimit);
+      if (ok) {
+        uint8_t *sA = stage0 + st * P::STAGE;
+        uint8_t *sB = sA + P::A_BYTES;
+        const int k = kc * GK + 8 * j;
+        const int tap = k / s.cin_p, ch = k - tap * s.cin_p;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        // the same element offset from every row's pixel
+        const long long off = ((long long)dy * s.w + dx) * s.cs_in + ch;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int r = rbase + 16 * i;
+          const int sy = py[i] + dy, sx = px[i] + dx;
+          const bool in = prow[i] && tap < 9 && sy >= 0 && sy < s.h && sx >= 0 && sx < s.w;
+          cp_async16(smem_u32(sA + sw128_offset(r, j)), in ? prow[i] + off : x, in ? 16u : 0u);
+        }
+        for (int c = tid; c < BN * 8; c += 128) {
+          const int r = c >> 3, jj = c & 7;
+          cp_async16(smem_u32(sB + sw128_offset(r, jj)), w + (size_t)r * s.kp + kc * GK + jj * 8,
+                     16u);
+        }
+      }
+      cp_async_commit();
+      if (kc >= LAG) {
+        cp_async_wait<LAG>();
+        fence_async_smem();
+        mbar_arrive(&full[(kc - LAG) % S]);
+      }
     }
+    cp_async_wait<0>();
     fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
+    for (int kc = nk - LAG < 0 ? 0 : nk - LAG; kc < nk; ++kc) mbar_arrive(&full[kc % S]);
+    if (!ok) atomicExch(&fail, 1);
+  } else if (lane == 0) {
+    // ---- MMA issuer ----
+    const uint32_t idesc = idesc_bf16_f32(GM, BN);
+    bool ok = true;
+    for (int kc = 0; kc < nk && ok; ++kc) {
+      const int st = kc % S;
+      ok = mbar_wait_bounded(&full[st], (kc / S) & 1, kWaitLimit);
+      if (!ok) break;
       tc_fence_after();
+      uint8_t *sA = stage0 + st * P::STAGE;
       const uint64_t da = desc_kmajor_sw128(smem_u32(sA));
-      const uint64_t db = desc_kmajor_sw128(smem_u32(sB));
+      const uint64_t db = desc_kmajor_sw128(smem_u32(sA + P::A_BYTES));
 #pragma unroll
       for (int kk = 0; kk < GK / 16; ++kk)
-        umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
-      umma_commit(&mbar);
+        umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+      umma_commit(&empty[st]);
     }
-    ok = __syncthreads_and(mbar_wait_bounded(&mbar, phase, kWaitLimit) ? 1 : 0);
-    phase ^= 1u;
+    if (ok) umma_commit(&done);
+    else atomicExch(&fail, 1);
   }
-  tc_fence_after();
-  if (ok) {
+  if (warp < 4) {
+    // ---- epilogue ----
+    const bool ok = mbar_wait_bounded(&done, 0, kWaitLimit);
+    tc_fence_after();
     const long long q = q0 + warp * 32 + lane;
+    if (ok) {
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-      if (q < npix) {
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+        if (q < npix) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          v[i] += bias ? bias[c + i] : 0.0f;
-          if (relu) v[i] = fmaxf(v[i], 0.0f);
-        }
-        if (y32) {
-          float *dst = y32 + q * s.cs_out + c;
+          for (int i = 0; i < 16; ++i) {
+            v[i] += bias ? bias[c + i] : 0.0f;
+            if (relu) v[i] = fmaxf(v[i], 0.0f);
+          }
+          if (y32) {
+            float *dst = y32 + q * s.cs_out + c;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) dst[i] = v[i];
-        } else {
-          __align__(16) __nv_bfloat16 o[16];
+            for (int i = 0; i < 16; ++i) dst[i] = v[i];
+          } else {
+            __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
-          uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
-          dst[0] = reinterpret_cast<const uint4 *>(o)[0];
-          dst[1] = reinterpret_cast<const uint4 *>(o)[1];
+            for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
+            uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
+            dst[0] = reinterpret_cast<const uint4 *>(o)[0];
+            dst[1] = reinterpret_cast<const uint4 *>(o)[1];
+          }
         }
       }
+    } else {
+      atomicExch(&fail, 1);
     }
-  } else if (tid == 0) {
-    atomicExch(err, 1u);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, TM_COLS);
+  if (tid == 0 && fail) atomicExch(err, 1u);
+  if (warp == 4) tmem_dealloc(tmem, TM_COLS);
 }
 
 // ------------------------------------------------------------------------
@@ -379,7 +452,7 @@ int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, cons
                 void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
                 cudaStream_t s, unsigned int *err) {
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
-  const int smem = GM * 128 + BN * 128 + 1024;
+  const int smem = ConvPipe<BN>::SMEM;
   static bool configured = false;
   if (!configured) {
     if (cudaFuncSetAttribute(conv3x3_fwd_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -388,8 +461,9 @@ int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, cons
     configured = true;
   }
   const long long npix = (long long)batch * h * width;
+  if (npix + GM >= (1LL << 31)) return STRM_NN_ERR_INVALID;
   const unsigned int grid = (unsigned int)((npix + GM - 1) / GM);
-  conv3x3_fwd_kernel<BN><<<grid, 128, smem, s>>>((const __nv_bfloat16 *)x,
+  conv3x3_fwd_kernel<BN><<<grid, 160, smem, s>>>((const __nv_bfloat16 *)x,
                                                  (const __nv_bfloat16 *)w, bias,
                                                  (__nv_bfloat16 *)y, y32, sh, relu, err);
   return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;

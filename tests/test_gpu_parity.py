@@ -300,7 +300,9 @@ def test_mixed_precision_matches_fp64_on_converged_cavity():
         i_r, n_r = ref.run_simulation_tick()
         i_m, n_m = mix.run_simulation_tick()
         assert n_r < 1e-14 and n_m < 1e-14, (i_r, n_r, i_m, n_m)
-        assert i_m % 16 == 0
+        # the coarse loop checks every 16 sweeps and redoes the last 16 one
+        # by one when it stops, so the mixed solve stops at the FP64 sweep
+        assert i_m == i_r, (i_m, i_r)
     for n in ("u", "v"):
         assert rel_l2(mix.download(n), ref.download(n)) < 1e-6, n
     assert rel_l2(p_fluid(mix.download("p"), g["kind"]), p_fluid(ref.download("p"), g["kind"])) < 1e-6
