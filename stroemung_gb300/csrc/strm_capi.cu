@@ -106,6 +106,7 @@ Consts make_consts(const strm_params &p) {
   // src/simulation.rs:240-246
   c.one_minus_w = 1.0 - p.omega;
   c.middle = p.omega / ((2.0 / c.dx2) + (2.0 / c.dy2));
+  c.two_r_sum = 2.0 * (c.r_dx2 + c.r_dy2);
   c.eps2 = p.eps * p.eps;
   return c;
 }

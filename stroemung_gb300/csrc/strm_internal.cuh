@@ -41,6 +41,7 @@ struct Consts {
   double r_dx, r_dy, r_dx2, r_dy2, r_four_dx, r_four_dy, r_re;
   // pressure solve
   double one_minus_w, middle;  // 1-omega, omega/((2/dx2)+(2/dy2))
+  double two_r_sum;            // 2 (1/dx^2 + 1/dy^2) (fast residual)
   double eps2;
 };
 

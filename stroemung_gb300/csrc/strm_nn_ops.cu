@@ -98,6 +98,123 @@ __global__ void upsample_bwd(const __nv_bfloat16 *gout, int cs_out, __nv_bfloat1
   }
 }
 
+// ---- 8-channel (16-byte) versions of the kernels above: same arithmetic per
+// element; used when channel counts, strides and addresses allow ----
+union V8 {
+  uint4 u;
+  __nv_bfloat16 h[8];
+};
+
+__device__ __forceinline__ V8 ld8(const __nv_bfloat16 *p) {
+  V8 v;
+  v.u = *reinterpret_cast<const uint4 *>(p);
+  return v;
+}
+__device__ __forceinline__ void st8(__nv_bfloat16 *p, const V8 &v) {
+  *reinterpret_cast<uint4 *>(p) = v.u;
+}
+
+__global__ void avgpool_fwd8(const __nv_bfloat16 *in, int cs_in, __nv_bfloat16 *out, int cs_out,
+                             int batch, int h, int w, int c) {
+  const int ho = h / 2, wo = w / 2, c8 = c / 8;
+  const long long n = (long long)batch * ho * wo * c8;
+  GRID_STRIDE(i, n) {
+    const int ch = 8 * (int)(i % c8);
+    const long long q = i / c8;
+    const int xo = (int)(q % wo);
+    const long long t = q / wo;
+    const int yo = (int)(t % ho);
+    const long long b = t / ho;
+    const long long q00 = (b * h + 2 * yo) * w + 2 * xo;
+    const V8 a = ld8(in + q00 * cs_in + ch), bb = ld8(in + (q00 + 1) * cs_in + ch);
+    const V8 cc = ld8(in + (q00 + w) * cs_in + ch), d = ld8(in + (q00 + w + 1) * cs_in + ch);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      o.h[k] = __float2bfloat16_rn(0.25f * (bf(a.h[k]) + bf(bb.h[k]) + bf(cc.h[k]) + bf(d.h[k])));
+    st8(out + q * cs_out + ch, o);
+  }
+}
+
+__global__ void avgpool_bwd8(const __nv_bfloat16 *gout, int cs_out, __nv_bfloat16 *gin,
+                             int cs_in, int batch, int h, int w, int c, int accumulate) {
+  const int c8 = c / 8;
+  const long long n = (long long)batch * h * w * c8;
+  GRID_STRIDE(i, n) {
+    const int ch = 8 * (int)(i % c8);
+    const long long q = i / c8;
+    const int xx = (int)(q % w);
+    const long long t = q / w;
+    const int yy = (int)(t % h);
+    const long long b = t / h;
+    const long long qo = (b * (h / 2) + yy / 2) * (w / 2) + xx / 2;
+    const V8 g = ld8(gout + qo * cs_out + ch);
+    V8 prev;
+    if (accumulate) prev = ld8(gin + q * cs_in + ch);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float v = 0.25f * bf(g.h[k]);
+      if (accumulate) v += bf(prev.h[k]);
+      o.h[k] = __float2bfloat16_rn(v);
+    }
+    st8(gin + q * cs_in + ch, o);
+  }
+}
+
+__global__ void upsample_fwd8(const __nv_bfloat16 *in, int cs_in, __nv_bfloat16 *out, int cs_out,
+                              int batch, int h, int w, int c) {
+  const int c8 = c / 8;
+  const long long n = (long long)batch * h * w * c8;
+  GRID_STRIDE(i, n) {
+    const int ch = 8 * (int)(i % c8);
+    const long long q = i / c8;
+    const int xx = (int)(q % w);
+    const long long t = q / w;
+    const int yy = (int)(t % h);
+    const long long b = t / h;
+    const long long qi = (b * (h / 2) + yy / 2) * (w / 2) + xx / 2;
+    st8(out + q * cs_out + ch, ld8(in + qi * cs_in + ch));
+  }
+}
+
+__global__ void upsample_bwd8(const __nv_bfloat16 *gout, int cs_out, __nv_bfloat16 *gin,
+                              int cs_in, int batch, int h, int w, int c) {
+  const int hi = h / 2, wi = w / 2, c8 = c / 8;
+  const long long n = (long long)batch * hi * wi * c8;
+  GRID_STRIDE(i, n) {
+    const int ch = 8 * (int)(i % c8);
+    const long long q = i / c8;
+    const int xi = (int)(q % wi);
+    const long long t = q / wi;
+    const int yi = (int)(t % hi);
+    const long long b = t / hi;
+    const long long q00 = (b * h + 2 * yi) * w + 2 * xi;
+    const V8 a = ld8(gout + q00 * cs_out + ch), bb = ld8(gout + (q00 + 1) * cs_out + ch);
+    const V8 cc = ld8(gout + (q00 + w) * cs_out + ch), d = ld8(gout + (q00 + w + 1) * cs_out + ch);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      o.h[k] = __float2bfloat16_rn(bf(a.h[k]) + bf(bb.h[k]) + bf(cc.h[k]) + bf(d.h[k]));
+    st8(gin + q * cs_in + ch, o);
+  }
+}
+
+__global__ void relu_mask8(const __nv_bfloat16 *g, int cs_g, const __nv_bfloat16 *y, int cs_y,
+                           __nv_bfloat16 *out, int cs_out, long long npix, int c) {
+  const int c8 = c / 8;
+  GRID_STRIDE(i, npix * c8) {
+    const int ch = 8 * (int)(i % c8);
+    const long long q = i / c8;
+    const V8 gv = ld8(g + q * cs_g + ch), yv = ld8(y + q * cs_y + ch);
+    V8 o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      o.h[k] = __float2bfloat16_rn(bf(yv.h[k]) > 0.0f ? bf(gv.h[k]) : 0.0f);
+    st8(out + q * cs_out + ch, o);
+  }
+}
+
 // g <- g * (y > 0) (ReLU adjoint), written to out (may alias g).
 __global__ void relu_mask(const __nv_bfloat16 *g, int cs_g, const __nv_bfloat16 *y, int cs_y,
                           __nv_bfloat16 *out, int cs_out, long long npix, int c) {
@@ -147,9 +264,19 @@ __global__ void flip_weights(const __nv_bfloat16 *w, int cout, int cin_p, int kp
 // 1x1 head, FP32: out[q] = sum_c wh[c] * act[q][c] + bh (bh a device scalar).
 __global__ void head_fwd(const __nv_bfloat16 *act, int cs, int c, const float *wh,
                          const float *bh, float *out, long long npix) {
+  const bool vec = (c % 8 == 0) && (cs % 8 == 0) &&
+                   ((reinterpret_cast<uintptr_t>(act) & 15u) == 0);
   GRID_STRIDE(q, npix) {
     float s = *bh;
-    for (int ch = 0; ch < c; ++ch) s = fmaf(wh[ch], bf(act[q * cs + ch]), s);
+    if (vec) {
+      for (int ch = 0; ch < c; ch += 8) {
+        const V8 a = ld8(act + q * cs + ch);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s = fmaf(wh[ch + k], bf(a.h[k]), s);
+      }
+    } else {
+      for (int ch = 0; ch < c; ++ch) s = fmaf(wh[ch], bf(act[q * cs + ch]), s);
+    }
     out[q] = s;
   }
 }
@@ -406,6 +533,12 @@ inline int grid_for(long long n, int block = 256) {
   return g < 1 ? 1 : (int)g;
 }
 inline int done() { return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA; }
+// 16-byte vector kernels apply: channel count and strides multiples of 8,
+// both base addresses 16-byte aligned
+inline bool vec8(const void *a, const void *b, int c, int cs_a, int cs_b) {
+  return c % 8 == 0 && cs_a % 8 == 0 && cs_b % 8 == 0 &&
+         ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15u) == 0;
+}
 typedef __nv_bfloat16 bf16;
 }  // namespace
 
@@ -416,6 +549,11 @@ extern "C" {
 int strm_nn_avgpool(const void *in, int cs_in, void *out, int cs_out, int batch, int h, int w,
                     int c, void *stream) {
   if (!in || !out || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
+  if (vec8(in, out, c, cs_in, cs_out)) {
+    avgpool_fwd8<<<grid_for((long long)batch * h * w * c / 32), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
+    return done();
+  }
   avgpool_fwd<<<grid_for((long long)batch * h * w * c / 4), 256, 0, (cudaStream_t)stream>>>(
       (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
   return done();
@@ -424,6 +562,11 @@ int strm_nn_avgpool(const void *in, int cs_in, void *out, int cs_out, int batch,
 int strm_nn_avgpool_bwd(const void *gout, int cs_out, void *gin, int cs_in, int batch, int h,
                         int w, int c, int accumulate, void *stream) {
   if (!gout || !gin || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
+  if (vec8(gout, gin, c, cs_out, cs_in)) {
+    avgpool_bwd8<<<grid_for((long long)batch * h * w * c / 8), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)gout, cs_out, (bf16 *)gin, cs_in, batch, h, w, c, accumulate);
+    return done();
+  }
   avgpool_bwd<<<grid_for((long long)batch * h * w * c), 256, 0, (cudaStream_t)stream>>>(
       (const bf16 *)gout, cs_out, (bf16 *)gin, cs_in, batch, h, w, c, accumulate);
   return done();
@@ -432,6 +575,11 @@ int strm_nn_avgpool_bwd(const void *gout, int cs_out, void *gin, int cs_in, int 
 int strm_nn_upsample(const void *in, int cs_in, void *out, int cs_out, int batch, int h, int w,
                      int c, void *stream) {
   if (!in || !out || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
+  if (vec8(in, out, c, cs_in, cs_out)) {
+    upsample_fwd8<<<grid_for((long long)batch * h * w * c / 8), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
+    return done();
+  }
   upsample_fwd<<<grid_for((long long)batch * h * w * c), 256, 0, (cudaStream_t)stream>>>(
       (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
   return done();
@@ -440,6 +588,11 @@ int strm_nn_upsample(const void *in, int cs_in, void *out, int cs_out, int batch
 int strm_nn_upsample_bwd(const void *gout, int cs_out, void *gin, int cs_in, int batch, int h,
                          int w, int c, void *stream) {
   if (!gout || !gin || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
+  if (vec8(gout, gin, c, cs_out, cs_in)) {
+    upsample_bwd8<<<grid_for((long long)batch * h * w * c / 32), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)gout, cs_out, (bf16 *)gin, cs_in, batch, h, w, c);
+    return done();
+  }
   upsample_bwd<<<grid_for((long long)batch * h * w * c / 4), 256, 0, (cudaStream_t)stream>>>(
       (const bf16 *)gout, cs_out, (bf16 *)gin, cs_in, batch, h, w, c);
   return done();
@@ -448,6 +601,11 @@ int strm_nn_upsample_bwd(const void *gout, int cs_out, void *gin, int cs_in, int
 int strm_nn_relu_mask(const void *g, int cs_g, const void *y, int cs_y, void *out, int cs_out,
                       long long npix, int c, void *stream) {
   if (!g || !y || !out) return STRM_NN_ERR_INVALID;
+  if (vec8(g, out, c, cs_g, cs_out) && vec8(y, y, c, cs_y, cs_y)) {
+    relu_mask8<<<grid_for(npix * c / 8), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)g, cs_g, (const bf16 *)y, cs_y, (bf16 *)out, cs_out, npix, c);
+    return done();
+  }
   relu_mask<<<grid_for(npix * c), 256, 0, (cudaStream_t)stream>>>(
       (const bf16 *)g, cs_g, (const bf16 *)y, cs_y, (bf16 *)out, cs_out, npix, c);
   return done();

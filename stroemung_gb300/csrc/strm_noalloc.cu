@@ -85,6 +85,7 @@ extern "C" int strm_norm_squared_noalloc(const double *p, const double *rhs, int
   c.dy2 = dy * dy;
   c.r_dx2 = 1.0 / c.dx2;
   c.r_dy2 = 1.0 / c.dy2;
+  c.two_r_sum = 2.0 * (c.r_dx2 + c.r_dy2);
   cudaStream_t s = (cudaStream_t)stream;
   noalloc_begin<<<1, 1, 0, s>>>(st, fluid_cells);
   if (cudaGetLastError() != cudaSuccess) return STRM_ERR_CUDA;
