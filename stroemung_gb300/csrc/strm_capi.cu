@@ -318,6 +318,7 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   const size_t o_fl = take(nfield);
   const size_t o_st = take(sizeof(StepState));
   const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
+  const size_t o_partb = take(sizeof(double) * 2 * (size_t)nb);
   const size_t o_log = take(sizeof(StepLog) * kLogCap);
   const size_t o_bad = take(8), o_fc = take(8);
   const size_t o_hist = take(sizeof(double) * 2 * kHistCap);
@@ -340,6 +341,7 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   d.st = (StepState *)(base + o_st);
   d.partials = (double *)(base + o_part);
   d.n_partials = 4 * nb;
+  d.partials_b = (double *)(base + o_partb);
   d.log = (StepLog *)(base + o_log);
   d.first_bad = (long long *)(base + o_bad);
   d.fluid_count = (unsigned long long *)(base + o_fc);

@@ -421,6 +421,45 @@ __global__ void __launch_bounds__(256)
   p[o] = sor_update<EXACT>(pc, pw, pe, pn, ps, rhs[o], c);
 }
 
+// The black pass of a FAST red-black iteration fused with the residual of the
+// black fluid cells: once they are updated their four (red) neighbours are
+// final, so r = t - 2(1/dx^2+1/dy^2) p_new with t from the update (the same
+// p_new as sor_color_kernel<false>).  The grid strides over the colour
+// pass's blocks (gx x gy of them, the layout of sor_color_kernel) so that a
+// block reduces once: its sums of r^2 (and r when mean-free) go to
+// partials_b[blockIdx.x]; residual_kernel adds the other cells.
+__global__ void __launch_bounds__(256)
+    sor_black_res_kernel(double *__restrict__ p, const double *__restrict__ rhs,
+                         const uint8_t *__restrict__ flags, Geom g, Consts c,
+                         double *__restrict__ partials_b, int mean_free, int gx, int nvb) {
+  double acc = 0.0, acc1 = 0.0;
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    const int x = 1 + (vb / gx) * blockDim.y + threadIdx.y;
+    const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + ((x + 1) & 1);
+    if (x > g.nx - 2 || y < 1 || y > g.ny - 2) continue;
+    const size_t o = OFF(x, y);
+    if (flags[o] != 0) continue;
+    const double pc = p[o];
+    const double t = fma(p[o + g.pitch] + p[o - g.pitch], c.r_dx2,
+                         fma(p[o + 1] + p[o - 1], c.r_dy2, -rhs[o]));
+    const double pn = fma(c.one_minus_w, pc, c.middle * t);
+    p[o] = pn;
+    const double r = fma(-c.two_r_sum, pn, t);
+    acc = fma(r, r, acc);
+    if (mean_free) acc1 += r;
+  }
+  const double bsum = block_reduce(acc, OpAdd(), 0.0);
+  if (mean_free) {
+    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      partials_b[2 * blockIdx.x] = bsum;
+      partials_b[2 * blockIdx.x + 1] = bsum1;
+    }
+  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
+    partials_b[blockIdx.x] = bsum;
+  }
+}
+
 // What a residual launch does once the norm is known.
 enum : int { RES_SOLVE = 0, RES_NORM = 1, RES_NS0 = 2, RES_START = 3 };
 // bits of the `strict` argument of the residual kernels
@@ -448,9 +487,21 @@ __device__ __forceinline__ double finish_norm(const double *partials, int nblock
   return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
 }
 
+// The same over two partial arrays (the residual pass and the fused black pass).
+__device__ __forceinline__ double finish_norm2(const double *pa, int na, const double *pb, int nb,
+                                               bool mean_free, double fluid_cells) {
+  const int st = mean_free ? 2 : 1;
+  const double s2 = reduce_partials(pa, na, st, 0, OpAdd(), 0.0) +
+                    reduce_partials(pb, nb, st, 0, OpAdd(), 0.0);
+  if (!mean_free) return s2 / fluid_cells;
+  const double s1 = reduce_partials(pa, na, 2, 1, OpAdd(), 0.0) +
+                    reduce_partials(pb, nb, 2, 1, OpAdd(), 0.0);
+  return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
+
 // This thread's share of the residual sums over the block's tiles: sum r^2
 // (and sum r when MEAN_FREE) over interior cells, fluid cells only when FLUID.
-template <bool EXACT, bool FLUID, bool MEAN_FREE>
+template <bool EXACT, bool FLUID, bool MEAN_FREE, bool SKIPB = false>
 __device__ __forceinline__ void residual_sum(const double *__restrict__ p,
                                              const double *__restrict__ rhs,
                                              const uint8_t *__restrict__ flags, const Geom &g,
@@ -468,6 +519,8 @@ __device__ __forceinline__ void residual_sum(const double *__restrict__ p,
       if (y <= g.ny - 2) {
         const size_t o = OFF(x, y);
         if (FLUID && flags[o] != 0) continue;
+        // black fluid cells: summed by the fused black pass
+        if (SKIPB && flags[o] == 0 && ((x + y) & 1) == 1) continue;
         const double r = residual_of<EXACT>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
                                             p[o + 1], rhs[o], c);
         acc = EXACT ? acc + sqd(r) : fma(r, r, acc);
@@ -489,18 +542,28 @@ __global__ void __launch_bounds__(256)
     residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
                     const uint8_t *__restrict__ flags, Geom g, Consts c, StepState *st,
                     double *partials, int tiles_y, int ntiles, cudaGraphConditionalHandle h,
-                    unsigned int itermax, int strict, int mode) {
+                    unsigned int itermax, int strict, int mode, const double *partials_b,
+                    int nbb) {
   const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
   const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
   double acc = 0.0, acc1 = 0.0;
   // the reference's sum (every interior cell) keeps its own loop: the solve is
-  // FP64-bound and pays for every extra operation
-  if (!fluid_only)
+  // FP64-bound and pays for every extra operation.  With partials_b the black
+  // fluid cells were summed by the fused black pass (sor_black_res_kernel).
+  if (partials_b) {
+    if (!fluid_only)
+      residual_sum<EXACT, false, false, true>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+    else if (!mean_free)
+      residual_sum<EXACT, true, false, true>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+    else
+      residual_sum<EXACT, true, true, true>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+  } else if (!fluid_only) {
     residual_sum<EXACT, false, false>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
-  else if (!mean_free)
+  } else if (!mean_free) {
     residual_sum<EXACT, true, false>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
-  else
+  } else {
     residual_sum<EXACT, true, true>(p, rhs, flags, g, c, tiles_y, ntiles, &acc, &acc1);
+  }
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
   if (mean_free) {
     const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
@@ -522,7 +585,9 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (!last_block_done(&st->counter)) return;
-  const double ns = finish_norm(partials, gridDim.x, mean_free, st->fluid_cells);
+  const double ns = partials_b ? finish_norm2(partials, gridDim.x, partials_b, nbb, mean_free,
+                                              st->fluid_cells)
+                               : finish_norm(partials, gridDim.x, mean_free, st->fluid_cells);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->counter = 0;
     if (mode == RES_NS0) {
@@ -1513,7 +1578,7 @@ cudaError_t launch_norm(const DevFields &d, const RunCfg &r, cudaStream_t s, int
   int nb = residual_blocks(r.g);
   residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st, d.partials,
                                                         ty, nt, 0, r.itermax, r.strict_eps,
-                                                        set_ns0 ? RES_NS0 : RES_NORM);
+                                                        set_ns0 ? RES_NS0 : RES_NORM, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -1530,7 +1595,7 @@ cudaError_t launch_norm_one_block_per_tile(const double *p, const double *rhs, c
   tiles_of(g, 1, &ty, &nt);
   if (nt == 0) return cudaSuccess;
   residual_kernel<true, false><<<nt, kRedBlock, 0, s>>>(p, rhs, nullptr, g, c, st, partials, ty, nt, 0,
-                                                        0u, 0, RES_NORM);
+                                                        0u, 0, RES_NORM, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -1594,11 +1659,11 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
   if (r.arith)
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
-                                                           r.strict_eps, RES_NORM);
+                                                           r.strict_eps, RES_NORM, nullptr, 0);
   else
     residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                           d.partials, ty, nt, 0, r.itermax,
-                                                          r.strict_eps, RES_NORM);
+                                                          r.strict_eps, RES_NORM, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -1702,33 +1767,39 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
   } else if (nt_int > 0 && r.itermax > 0) {
     dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+    const int nbb = (int)(sgrid.x * sgrid.y);
+    const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
     if (r.strict_eps & STOP_RELATIVE) {
       // the norm the solve starts from (relative stop rule)
       if (r.arith)
         residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st,
                                                                d.partials, ty_int, nt_int, 0,
-                                                               r.itermax, r.strict_eps, RES_START);
+                                                               r.itermax, r.strict_eps, RES_START,
+                                                               nullptr, 0);
       else
         residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st,
                                                               d.partials, ty_int, nt_int, 0,
-                                                              r.itermax, r.strict_eps, RES_START);
+                                                              r.itermax, r.strict_eps, RES_START,
+                                                              nullptr, 0);
     }
     while (!done) {
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
-      for (int color = 0; color < 2; ++color) {
-        if (r.arith)
-          sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
-        else
-          sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
-      }
-      if (r.arith)
+      if (r.arith) {
+        // fast arithmetic: the black pass also sums the black fluid cells' residual
+        sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, 0);
+        sor_black_res_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
+                                                      mean_free, (int)sgrid.x, nbb);
         residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                                ty_int, nt_int, 0, r.itermax,
-                                                               r.strict_eps, RES_SOLVE);
-      else
+                                                               r.strict_eps, RES_SOLVE,
+                                                               d.partials_b, nb);
+      } else {
+        for (int color = 0; color < 2; ++color)
+          sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
         residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                               ty_int, nt_int, 0, r.itermax,
-                                                              r.strict_eps, RES_SOLVE);
+                                                              r.strict_eps, RES_SOLVE, nullptr, 0);
+      }
       if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
     }
   }
@@ -1954,7 +2025,8 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                                : (const void *)residual_kernel<true, false>;
       n = b.kernel(b.graph, n, k0, dim3(nb), kRedBlock, (const double *)d.p,
                    (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
-                   ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_START);
+                   ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_START,
+                   (const double *)nullptr, 0);
     }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
@@ -1976,12 +2048,28 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                                : (const void *)sor_color_kernel<true>;
       const void *kr = r.arith ? (const void *)residual_kernel<false, true>
                                : (const void *)residual_kernel<true, true>;
-      for (int color = 0; color < 2; ++color)
+      const int nbb = (int)(sgrid.x * sgrid.y);
+      const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
+      if (r.arith) {
+        // fast arithmetic: the black pass also sums the black fluid cells' residual
         bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
-                      (const uint8_t *)d.flags, g, c, color);
-      bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
-                    (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax,
-                    r.strict_eps, (int)RES_SOLVE);
+                      (const uint8_t *)d.flags, g, c, 0);
+        bn = b.kernel(body, bn, (const void *)sor_black_res_kernel, dim3(nb), kRedBlock, d.p,
+                      (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
+                      mean_free, (int)sgrid.x, nbb);
+        bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
+                      (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
+                      ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_SOLVE,
+                      (const double *)d.partials_b, nb);
+      } else {
+        for (int color = 0; color < 2; ++color)
+          bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
+                        (const uint8_t *)d.flags, g, c, color);
+        bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
+                      (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
+                      ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_SOLVE,
+                      (const double *)nullptr, 0);
+      }
     }
     n = wnode;
   }

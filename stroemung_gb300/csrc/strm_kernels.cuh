@@ -22,6 +22,7 @@ struct DevFields {
   StepState *st;
   double *partials;       // per-CTA residual partial sums
   int n_partials;
+  double *partials_b;     // per-CTA sums of the fused black pass (2 per residual block)
   StepLog *log;
   BcEntry *bc;            // compiled boundary program
   double *bc_val;         // its gathered values
