@@ -203,6 +203,23 @@ def config_dict(args):
                   "no flush", "parallelism": f"replicas x{args.gpus}"}
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's time (replicas run independently; the whole job
+    ends with the last one)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells_per_step: float, steps: int, world: int, seconds: float) -> float:
+    """Whole-job cell-updates/s of `world` replicas, each doing `steps`
+    steps of `cells_per_step`, the job taking `seconds` (max over ranks)."""
+    return cells_per_step * steps * world / seconds
+
+
 def field_errors(a_fields, b_fields, fluid):
     """Relative L2 and max abs error per field; the pressure on fluid cells
     with its mean removed (pure Neumann: each solve fixes its own constant)."""
@@ -617,12 +634,8 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = CELLS * args.steps * world / (ms / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
+    value = replica_value(CELLS, args.steps, world, ms / 1e3)
     iters = [s[0] for s in stats]
     n_pcopy_launch = 1
     launches = sum(2 + 3 + n_pcopy_launch + (3 + n_pcopy_launch) * (k - 1) + 2 for k in iters)
@@ -682,13 +695,10 @@ def main():
             sim.download(n, out=host[n])
     torch.cuda.synchronize()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     field_bytes = (IMAX + 2) * (JMAX + 2) * 8
-    e2e = {"value": CELLS * args.e2e_steps * world / e2e_s if args.e2e_steps else None,
+    e2e = {"value": replica_value(CELLS, args.e2e_steps, world, e2e_s) if args.e2e_steps
+           else None,
            "unit": "cell-updates/s",
            "h2d_bytes_per_step": 3 * field_bytes, "d2h_bytes_per_step": 3 * field_bytes + 64,
            "steps": args.e2e_steps, "sor_iterations": e2e_iters,
