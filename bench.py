@@ -459,6 +459,36 @@ def cavity_block(args):
     out["speedup_mixed_vs_fp64"] = (sum(res["fp64"]["ms_per_step"]) /
                                     sum(res["mixed"]["ms_per_step"]))
     out["error_mixed_vs_fp64"] = field_errors(fields["mixed"], fields["fp64"], grid["kind"] == 0)
+    if args.cavity_small:
+        out["converging"] = time_to_residual(args.cavity_small, args.cavity_steps)
+    return out
+
+
+def time_to_residual(n, steps):
+    """Poisson time-to-residual where the solve converges: the n x n cavity
+    (Re 1000, omega 1.8, eps 1e-5 relative to each solve's starting norm),
+    FP64 and mixed; per step the device time of the whole step (the solve
+    dominates it) and the sweeps the solve took."""
+    import torch
+    from stroemung_gb300 import presets
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    grid = presets.cavity(n)
+    cfg = dict(cell_size=(1.0 / n, 1.0 / n), delt=1e-4, gamma=0.9, reynolds=1000.0,
+               sor_absolute_epsilon=1e-5, max_iterations=100000, omega=1.8, tau=0.5,
+               arithmetic=ARITH_FAST, strict_eps=2)
+    out = {"grid": f"{n}x{n}", "stop_rule": "ns < (1e-5)^2 x the norm the solve starts from"}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        sim = Simulation(grid=grid, precision=prec, **cfg)
+        stream = torch.cuda.ExternalStream(sim.device_view()["stream"])
+        rows = []
+        for _ in range(steps):
+            ms, st = timed_steps(sim, 1, stream)
+            rows.append({"ms": ms, "sweeps": int(st[0][0]), "converged": bool(st[0][3])})
+        sim.close()
+        out[name] = {"per_step": rows,
+                     "time_to_residual_ms_median": statistics.median(r["ms"] for r in rows)}
+    out["speedup_mixed_vs_fp64"] = (out["fp64"]["time_to_residual_ms_median"] /
+                                    out["mixed"]["time_to_residual_ms_median"])
     return out
 
 
@@ -582,6 +612,8 @@ def main():
     ap.add_argument("--cavity-n", type=int, default=2048)
     ap.add_argument("--cavity-steps", type=int, default=3)
     ap.add_argument("--cavity-itermax", type=int, default=20000)
+    ap.add_argument("--cavity-small", type=int, default=256,
+                    help="size of a cavity whose solves converge (time-to-residual); 0 skips")
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)

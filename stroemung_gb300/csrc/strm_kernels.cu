@@ -1650,20 +1650,24 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
   dim3 sgrid((r.g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
              (r.g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
   const int nb = residual_blocks(r.g);
-  for (int color = 0; color < 2; ++color) {
-    if (r.arith)
-      sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
-    else
-      sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
-  }
-  if (r.arith)
+  if (r.arith) {
+    // as in the solve: the black pass also sums the black fluid cells' residual
+    const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
+    sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, 0);
+    sor_black_res_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.partials_b,
+                                                  mean_free, (int)sgrid.x,
+                                                  (int)(sgrid.x * sgrid.y));
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
-                                                           r.strict_eps, RES_NORM, nullptr, 0);
-  else
+                                                           r.strict_eps, RES_NORM, d.partials_b,
+                                                           nb);
+  } else {
+    for (int color = 0; color < 2; ++color)
+      sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
     residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                           d.partials, ty, nt, 0, r.itermax,
                                                           r.strict_eps, RES_NORM, nullptr, 0);
+  }
   return cudaGetLastError();
 }
 

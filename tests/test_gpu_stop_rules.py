@@ -37,3 +37,36 @@ def test_relative_rule_is_refused_for_the_lexicographic_order():
     with pytest.raises(Exception):
         sim.set_mode(sor_order=_lib.SOR_LEXICOGRAPHIC, strict_eps=_lib.STOP_RELATIVE)
     sim.close()
+
+
+@pytest.mark.parametrize("norm_cells", [_lib.NORM_ALL_INTERIOR, _lib.NORM_FLUID,
+                                        _lib.NORM_FLUID_MEAN_FREE])
+def test_fast_solve_norm_matches_the_fields(norm_cells):
+    """FAST FP64 solves sum the black fluid cells' residual inside the black
+    pass and the other cells in the residual pass; the norm they report
+    equals the norm of the fields they leave (every residual kind)."""
+    from stroemung_gb300.simulation import ARITH_FAST
+    g = presets.channel(96, 40, [(30, 12, 8, 6), (60, 20, 5, 9)])
+    sim = Simulation(grid=g, cell_size=(0.01, 0.01), delt=0.002, gamma=0.9, reynolds=200.0,
+                     max_iterations=37, tau=0.5, arithmetic=ARITH_FAST,
+                     norm_cells=norm_cells, strict_eps=_lib.STOP_STRICT,
+                     sor_absolute_epsilon=1e-12)
+    for _ in range(3):
+        it, ns = sim.run_simulation_tick()
+    # the last solve's fields: p before the velocity update is what the norm saw
+    p, rhs = sim.download("p"), sim.download("rhs")
+    dx2 = 0.01 * 0.01
+    r = (p[2:, 1:-1] + p[:-2, 1:-1]) / dx2 + (p[1:-1, 2:] + p[1:-1, :-2]) / dx2 \
+        - 2 * (2 / dx2) * p[1:-1, 1:-1] - rhs[1:-1, 1:-1]
+    fluid = sim._kind[1:-1, 1:-1] == 0
+    nf = float(sim.state()["fluid_cells"])
+    if norm_cells == _lib.NORM_ALL_INTERIOR:
+        want = (r ** 2).sum() / nf
+    elif norm_cells == _lib.NORM_FLUID:
+        want = (r[fluid] ** 2).sum() / nf
+    else:
+        rf = r[fluid]
+        want = ((rf ** 2).sum() - rf.sum() ** 2 / nf) / nf
+    assert it == 37
+    np.testing.assert_allclose(ns, want, rtol=1e-8)
+    sim.close()
