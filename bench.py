@@ -297,11 +297,25 @@ def mixed_block(args, grid, fp64_ms_step, peak):
     t_sw = sw0.elapsed_time(sw1) / 1e3 / nsw
     sw_bytes = 13.0 * CELLS  # read e, s (8) + flags (1), write e (4)
     sim.close()
+    # the step time at other refinement intervals (same stop sweeps: the loop
+    # redoes the last interval sweep by sweep when the rule fires inside it)
+    by_inner = {}
+    for m in args.inner_alt:
+        alt = Simulation(grid=grid, precision=PREC_MIXED, inner_sweeps=m, arithmetic=ARITH_FAST,
+                         **PARAMS)
+        alt.step_n(1)
+        alt.autotune_sweeps(reps=2)
+        st_alt = torch.cuda.ExternalStream(alt.device_view()["stream"])
+        ms_alt, _ = timed_steps(alt, 3, st_alt)
+        by_inner[str(m)] = {"ms_per_step": ms_alt / 3,
+                            "speedup_vs_fp64": fp64_ms_step / (ms_alt / 3)}
+        alt.close()
     growth = error_growth(args, grid) if args.err_steps > 0 else []
     return {
         "value": CELLS * args.steps / (ms / 1e3), "unit": "cell-updates/s",
         "ms_per_step": ms / args.steps, "speedup_vs_fp64": fp64_ms_step / (ms / args.steps),
         "inner_sweeps": min(args.inner_sweeps, PARAMS["max_iterations"]),
+        "other_inner_sweeps": by_inner,
         "sweep_schedule": {"chosen": best, "us_per_sweep": {str(k): v * 1e3
                                                             for k, v in sched_ms.items()},
                            "note": "1 = one launch per colour pass; 2..7 = shared-memory "
@@ -600,6 +614,8 @@ def main():
     ap.add_argument("--eager", type=int, default=0,
                     help="1: launch kernels one by one (for per-kernel profiling)")
     ap.add_argument("--inner-sweeps", type=int, default=16)
+    ap.add_argument("--inner-alt", type=int, nargs="*", default=[40, 80],
+                    help="refinement intervals timed besides --inner-sweeps")
     ap.add_argument("--mixed", type=int, default=1)
     ap.add_argument("--err-steps", type=int, default=100,
                     help="steps after which mixed precision is compared with FP64")

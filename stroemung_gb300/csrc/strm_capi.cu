@@ -318,7 +318,7 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   const size_t o_fl = take(nfield);
   const size_t o_st = take(sizeof(StepState));
   const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
-  const size_t o_partb = take(sizeof(double) * 2 * (size_t)nb);
+  const size_t o_partb = take(sizeof(double) * 2 * (size_t)black_pass_blocks(s->g));
   const size_t o_log = take(sizeof(StepLog) * kLogCap);
   const size_t o_bad = take(8), o_fc = take(8);
   const size_t o_hist = take(sizeof(double) * 2 * kHistCap);

@@ -1425,6 +1425,17 @@ int residual_blocks(const Geom &g) {
 
 static const dim3 kRedBlock(RT_Y / 2, RT_X);
 
+// Blocks of the fused black pass: enough resident warps to keep the FP64
+// pipe busy, each block reducing once.
+int black_pass_blocks(const Geom &g) {
+  const long long gx = (g.ny / 2 + 1 + (int)kRedBlock.x - 1) / (int)kRedBlock.x;
+  const long long gy = (g.nx - 2 + (int)kRedBlock.y - 1) / (int)kRedBlock.y;
+  long long n = gx * (gy > 0 ? gy : 0);
+  const long long cap = 4LL * num_sms();  // measured: more blocks ran slower
+  if (n > cap) n = cap;
+  return n < 1 ? 1 : (int)n;
+}
+
 // The sweep schedules: 0 is one launch per colour pass; the others are
 // temporal-blocking tile shapes, `sweeps` red-black sweeps per launch.
 struct TbShape {
@@ -1654,13 +1665,14 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
     // as in the solve: the black pass also sums the black fluid cells' residual
     const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
     sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, 0);
-    sor_black_res_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.partials_b,
+    const int bb = black_pass_blocks(r.g);
+    sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.partials_b,
                                                   mean_free, (int)sgrid.x,
                                                   (int)(sgrid.x * sgrid.y));
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
                                                            r.strict_eps, RES_NORM, d.partials_b,
-                                                           nb);
+                                                           bb);
   } else {
     for (int color = 0; color < 2; ++color)
       sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
@@ -1791,12 +1803,13 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       if (r.arith) {
         // fast arithmetic: the black pass also sums the black fluid cells' residual
         sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, 0);
-        sor_black_res_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
+        const int bb = black_pass_blocks(g);
+        sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
                                                       mean_free, (int)sgrid.x, nbb);
         residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                                ty_int, nt_int, 0, r.itermax,
                                                                r.strict_eps, RES_SOLVE,
-                                                               d.partials_b, nb);
+                                                               d.partials_b, bb);
       } else {
         for (int color = 0; color < 2; ++color)
           sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
@@ -2058,13 +2071,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         // fast arithmetic: the black pass also sums the black fluid cells' residual
         bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
                       (const uint8_t *)d.flags, g, c, 0);
-        bn = b.kernel(body, bn, (const void *)sor_black_res_kernel, dim3(nb), kRedBlock, d.p,
+        const int bb = black_pass_blocks(g);
+        bn = b.kernel(body, bn, (const void *)sor_black_res_kernel, dim3(bb), kRedBlock, d.p,
                       (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
                       mean_free, (int)sgrid.x, nbb);
         bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
                       (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
                       ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_SOLVE,
-                      (const double *)d.partials_b, nb);
+                      (const double *)d.partials_b, bb);
       } else {
         for (int color = 0; color < 2; ++color)
           bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,

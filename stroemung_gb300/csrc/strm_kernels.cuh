@@ -22,7 +22,7 @@ struct DevFields {
   StepState *st;
   double *partials;       // per-CTA residual partial sums
   int n_partials;
-  double *partials_b;     // per-CTA sums of the fused black pass (2 per residual block)
+  double *partials_b;     // per-CTA sums of the fused black pass (2 per block)
   StepLog *log;
   BcEntry *bc;            // compiled boundary program
   double *bc_val;         // its gathered values
@@ -87,6 +87,8 @@ cudaError_t launch_apply_correction(const DevFields &d, const Geom &g, const flo
                                     double scale, cudaStream_t s);
 
 int residual_blocks(const Geom &g);
+// Blocks of the fused black pass of the FAST FP64 solve (2 partials each).
+int black_pass_blocks(const Geom &g);
 
 // Residual norm of raw pitched fields with one block per 8x64 tile of the
 // interior: partials[] must hold interior_tiles(g) doubles; st->fluid_cells
