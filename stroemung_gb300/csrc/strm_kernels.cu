@@ -984,6 +984,9 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
   // per pass), and columns 0 / W-1 read the neighbouring row's edge word,
   // which stays inside the tile.  Frozen cells keep their value; boundary
   // cells take the copy.
+  // Each warp takes a strip of consecutive rows so that the other colour's
+  // rows x-1, x, x+1 roll through registers: one new row per row.
+  constexpr int STRIP = (EX - 2 + WARPS - 1) / WARPS;
   for (int pass = 0; pass < 2 * n; ++pass) {
     const int c = pass & 1;
     const bool copy = !(skip_last_copy && pass == 2 * n - 1);
@@ -992,36 +995,44 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
     const float *eo = se + (1 - c) * NC;
     const float *svc = ss + c * NC;
     const uint8_t *cc = sc + c * NC;
-    for (int lx = lo + warp; lx <= hix; lx += WARPS) {
-      const int p = (lx + c) & 1;
-      const int i = lx * W + j0;
-      const uchar2 cd = *reinterpret_cast<const uchar2 *>(cc + i);
-      const float2 cur = *reinterpret_cast<const float2 *>(ec + i);
-      const float2 sv2 = *reinterpret_cast<const float2 *>(svc + i);
-      const float2 up = *reinterpret_cast<const float2 *>(eo + i - W);
-      const float2 dn = *reinterpret_cast<const float2 *>(eo + i + W);
-      const float2 mid = *reinterpret_cast<const float2 *>(eo + i);
-      // neighbours along y of cell j: (j-1+p, j+p) in the other colour
-      float lf0, rt0, lf1, rt1;
-      if (p) {
-        lf0 = mid.x;
-        rt0 = mid.y;
-        lf1 = mid.y;
-        rt1 = eo[i + 2];
-      } else {
-        lf0 = eo[i - 1];
-        rt0 = mid.x;
-        lf1 = mid.x;
-        rt1 = mid.y;
+    const int first = lo + warp * STRIP;
+    if (first <= hix) {
+      float2 up = *reinterpret_cast<const float2 *>(eo + (first - 1) * W + j0);
+      float2 mid = *reinterpret_cast<const float2 *>(eo + first * W + j0);
+#pragma unroll
+      for (int r = 0; r < STRIP; ++r) {
+        const int lx = first + r;
+        if (lx > hix) break;
+        const int p = (lx + c) & 1;
+        const int i = lx * W + j0;
+        const float2 dn = *reinterpret_cast<const float2 *>(eo + i + W);
+        const uchar2 cd = *reinterpret_cast<const uchar2 *>(cc + i);
+        const float2 cur = *reinterpret_cast<const float2 *>(ec + i);
+        const float2 sv2 = *reinterpret_cast<const float2 *>(svc + i);
+        // neighbours along y of cell j: (j-1+p, j+p) in the other colour
+        float lf0, rt0, lf1, rt1;
+        if (p) {
+          lf0 = mid.x;
+          rt0 = mid.y;
+          lf1 = mid.y;
+          rt1 = eo[i + 2];
+        } else {
+          lf0 = eo[i - 1];
+          rt0 = mid.x;
+          lf1 = mid.x;
+          rt1 = mid.y;
+        }
+        const float s0 = fmaf(k.omw, cur.x, fmaf(k.a, up.x + dn.x, fmaf(k.b, lf0 + rt0, sv2.x)));
+        const float s1 = fmaf(k.omw, cur.y, fmaf(k.a, up.y + dn.y, fmaf(k.b, lf1 + rt1, sv2.y)));
+        float2 res = make_float2(cd.x == 0 ? s0 : cur.x, cd.y == 0 ? s1 : cur.y);
+        if ((cd.x | cd.y) != 0 && copy) {  // boundary cells of this pair (rare)
+          if (cd.x != 0 && cd.x != kFrozen) res.x = sv2.x + copy_rb(cd.x, up.x, dn.x, lf0, rt0);
+          if (cd.y != 0 && cd.y != kFrozen) res.y = sv2.y + copy_rb(cd.y, up.y, dn.y, lf1, rt1);
+        }
+        *reinterpret_cast<float2 *>(ec + i) = res;
+        up = mid;
+        mid = dn;
       }
-      const float s0 = fmaf(k.omw, cur.x, fmaf(k.a, up.x + dn.x, fmaf(k.b, lf0 + rt0, sv2.x)));
-      const float s1 = fmaf(k.omw, cur.y, fmaf(k.a, up.y + dn.y, fmaf(k.b, lf1 + rt1, sv2.y)));
-      float2 res = make_float2(cd.x == 0 ? s0 : cur.x, cd.y == 0 ? s1 : cur.y);
-      if ((cd.x | cd.y) != 0 && copy) {  // boundary cells of this pair (rare)
-        if (cd.x != 0 && cd.x != kFrozen) res.x = sv2.x + copy_rb(cd.x, up.x, dn.x, lf0, rt0);
-        if (cd.y != 0 && cd.y != kFrozen) res.y = sv2.y + copy_rb(cd.y, up.y, dn.y, lf1, rt1);
-      }
-      *reinterpret_cast<float2 *>(ec + i) = res;
     }
     __syncthreads();
   }
