@@ -438,7 +438,67 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
                 "tensor_frac_of_measured_bf16": (flops / fwd_ms / 1e9) / BF16_PEAK,
                 "params": net.parameter_count()},
         "training": train_info,
+        "note": "the reference stop rule runs 2000 sweeps in every step of this workload, so no "
+                "warm start can save sweeps here; see learned_cavity for a converging case",
     }
+
+
+def learned_cavity_block(args):
+    """The warm start where solves converge: n x n lid-driven cavities (Re
+    log-uniform in [50, 2000], strict eps 1e-3 on the mean-free fluid
+    residual).  Two configurations, each trained here on the same snapshots
+    and stepped A/B against the plain mixed solve from identical states on
+    two held-out Reynolds numbers: the residual loss with the initial-residual
+    judge, and the error loss (against the solved pressure) with the judge
+    after judge_sweeps red-black iterations."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import presets, warmstart
+    from stroemung_gb300.unet import UNet
+    n = args.ws_cavity_n
+    fam = warmstart.cavity_family(n)
+    t0 = time.perf_counter()
+    train = warmstart.generate_snapshots(args.ws_snapshots, family=fam, steps_per_problem=32,
+                                         seed=1, targets=True)
+    t_gen = time.perf_counter() - t0
+    out = {"grid": f"{n}x{n}", "snapshots": args.ws_snapshots, "generate_s": t_gen,
+           "stop_rule": "ns < (1e-3)^2, fluid cells, mean removed", "held_out_re": [150.0, 900.0],
+           "steps_per_re": args.ws_cavity_steps}
+    for name, loss, judge in (("residual_loss_initial_judge", "residual", 0),
+                              ("error_loss_smoothed_judge", "error", args.ws_judge_sweeps)):
+        net = UNet(seed=0)
+        tr = warmstart.Trainer(net, n + 2, n + 2, 1.0 / n, 1.0 / n, batch=32, loss=loss)
+        t0 = time.perf_counter()
+        hist = tr.fit(train, epochs=args.ws_cavity_epochs, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        sp = sw = acc = steps = 0
+        t_plain = t_ws = 0.0
+        for re in out["held_out_re"]:
+            plain = warmstart.make_simulation(presets.cavity(n), re, 1.0 / n, delt=1e-3,
+                                              max_iterations=40000)
+            wsim = warmstart.make_simulation(presets.cavity(n), re, 1.0 / n, delt=1e-3,
+                                             max_iterations=40000)
+            ws = warmstart.WarmStartSolver(wsim, net, judge_sweeps=judge)
+            scratch = torch.zeros(n + 2, n + 2, dtype=torch.float64, device="cuda")
+            for _ in range(args.ws_cavity_steps):
+                r = warmstart.compare_step(plain, ws, scratch)
+                sp += r["sweeps_plain"]
+                sw += r["sweeps_ws"]
+                acc += r["accepted"]
+                steps += 1
+                t_plain += r["solve_plain_ms"]
+                t_ws += r["predict_ms"] + r["judge_ms"] + r["solve_ws_ms"]
+            plain.close()
+            wsim.close()
+        out[name] = {"loss": loss, "judge_sweeps": judge, "epochs": args.ws_cavity_epochs,
+                     "train_s": t_train, "loss_first_last": [float(np.mean(hist[:8])),
+                                                             float(np.mean(hist[-8:]))],
+                     "sweeps_plain": sp, "sweeps_learned": sw, "sweeps_saved": 1 - sw / sp,
+                     "accepted": f"{acc}/{steps}", "ms_plain": t_plain,
+                     "ms_learned_incl_predict_and_judge": t_ws,
+                     "time_saved": 1 - t_ws / t_plain}
+    return out
 
 
 def cavity_block(args):
@@ -624,6 +684,10 @@ def main():
     ap.add_argument("--ws-snapshots", type=int, default=1024)
     ap.add_argument("--ws-epochs", type=int, default=8)
     ap.add_argument("--ws-steps", type=int, default=4)
+    ap.add_argument("--ws-cavity-n", type=int, default=128)
+    ap.add_argument("--ws-cavity-epochs", type=int, default=30)
+    ap.add_argument("--ws-cavity-steps", type=int, default=24)
+    ap.add_argument("--ws-judge-sweeps", type=int, default=16)
     ap.add_argument("--cavity", type=int, default=1)
     ap.add_argument("--cavity-n", type=int, default=2048)
     ap.add_argument("--cavity-steps", type=int, default=3)
@@ -806,6 +870,7 @@ def main():
             mixed_ms = out["mixed_precision"].get("ms_per_step")
         if args.learned:
             guarded("learned", lambda: learned_block(args, grid, fp64_ms_step, mixed_ms))
+            guarded("learned_cavity", lambda: learned_cavity_block(args))
         if args.cavity:
             guarded("cavity_mixed", lambda: cavity_block(args))
         if args.batched:

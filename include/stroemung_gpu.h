@@ -218,6 +218,20 @@ int strm_export_planes(strm_sim *sim, float *rhs, float *p, uint8_t *flags);
 int strm_apply_correction(strm_sim *sim, const float *q, double scale);
 int strm_copy_field_device(strm_sim *sim, int field, double *dense, int to_sim);
 
+/* Judge of a predicted pressure correction (p += scale * q on fluid interior
+ * cells, q as for strm_apply_correction), between strm_tick_prepare and
+ * strm_tick_solve.  sweeps = 0: the correction is kept when it lowers the
+ * residual norm of the pressure (after the boundary copy).  sweeps > 0: both
+ * candidates first get `sweeps` FP64 red-black iterations and their norms
+ * are compared then (a prediction that removes smooth error but adds a
+ * little high-frequency error has a larger raw residual, which the first
+ * sweeps remove).  Either way the pressure is left at the chosen candidate
+ * without the judge's sweeps, boundary copy applied; ns_prev / ns_pred
+ * receive the two norms, accepted 1 when the correction was kept (each may
+ * be NULL).  No reference counterpart. */
+int strm_judge_correction(strm_sim *sim, const float *q, double scale, int sweeps,
+                          double *ns_prev, double *ns_pred, int *accepted);
+
 /* n ticks back to back with a single host synchronisation; stats[n] (may be
  * NULL) receives each tick's results. */
 int strm_step_n(strm_sim *sim, int n, strm_step_stats *stats);

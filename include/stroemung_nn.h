@@ -91,6 +91,15 @@ int strm_nn_residual_loss(const float *pprev, const float *q, const uint8_t *fla
 int strm_nn_residual_loss_grad(const float *r, const uint8_t *flags, const float *sum_b2,
                                const float *smax, float dx2, float rdx2, float rdy2,
                                float *gp, float *gq, int batch, int nx, int ny, void *stream);
+/* Error loss against target pressures (converged solutions), full planes
+ * [batch][nx][ny] as for the residual loss, q [batch][nx-2][ny-2]: on fluid
+ * interior cells e = p_prev + s dx^2 q - p_target and d = p_target - p_prev,
+ * each with its fluid mean removed; loss[b] = sum e^2 / sum d^2 (may be
+ * NULL) and gq = gradient of the batch mean with respect to q (may be NULL).
+ * work holds 5 * batch floats. */
+int strm_nn_error_loss(const float *pprev, const float *q, const float *ptarget,
+                       const uint8_t *flags, const float *smax, float dx2, float *work,
+                       float *loss, float *gq, int batch, int nx, int ny, void *stream);
 /* cudaMemsetAsync(p, 0, bytes) on stream. */
 int strm_nn_zero(void *p, long long bytes, void *stream);
 /* Adam on FP32 master weights (step counts from 1); writes a BF16 copy to

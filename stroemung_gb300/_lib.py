@@ -113,6 +113,8 @@ SIGNATURES = {
     "strm_batch_autotune": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
     "strm_apply_correction": [_vp, _vp, ctypes.c_double],
     "strm_copy_field_device": [_vp, ctypes.c_int, _vp, ctypes.c_int],
+    "strm_judge_correction": [_vp, _vp, ctypes.c_double, ctypes.c_int, _dp, _dp,
+                              ctypes.POINTER(ctypes.c_int)],
     "strm_render_rgba": [_vp, ctypes.c_int, _u8p],
     "strm_synchronize": [_vp],
     "strm_norm_squared_noalloc": [_dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -133,6 +135,8 @@ SIGNATURES = {
     "strm_nn_flip_weights": [_vp, _i, _i, _i, _vp, _i, _i, _vp],
     "strm_nn_head": [_vp, _i, _i, _fp, _fp, _fp, ctypes.c_longlong, _vp],
     "strm_nn_zero": [_vp, ctypes.c_longlong, _vp],
+    "strm_nn_error_loss": [_fp, _fp, _fp, _u8d, _fp, ctypes.c_float, _fp, _fp, _fp, _i, _i, _i,
+                           _vp],
     "strm_nn_head_bwd": [_vp, _i, _i, _fp, _fp, _vp, _i, _fp, _fp, ctypes.c_longlong, _vp],
     "strm_nn_prepare_input": [_fp, _u8d, _fp, _fp, _fp, _fp, ctypes.c_float, _vp, _i, _i, _i,
                               _vp],

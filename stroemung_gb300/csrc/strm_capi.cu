@@ -674,6 +674,47 @@ int strm_apply_correction(strm_sim *s, const float *q, double scale) {
   return STRM_OK;
 }
 
+int strm_judge_correction(strm_sim *s, const float *q, double scale, int sweeps,
+                          double *ns_prev, double *ns_pred, int *accepted) {
+  if (!s || !q || sweeps < 0 || sweeps > 4096) return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(s->dev));
+  const size_t bytes = sizeof(double) * (size_t)s->g.nx * s->g.pitch;
+  DevFields &d = s->d;
+  // the judge's sweeps: FP64 red-black with fast arithmetic, the sim's norm
+  RunCfg rj = s->cfg;
+  rj.precision = 0;
+  rj.arith = 1;
+  auto norm_after = [&](double *out) -> int {
+    if (sweeps == 0) {
+      CK(launch_pcopy(d, s->g, s->stream));
+      CK(launch_norm(d, s->cfg, s->stream, 0));
+    } else {
+      for (int k = 0; k < sweeps; ++k) CK(launch_sor_iteration(d, rj, s->stream));
+    }
+    int rc = sync_state(s);
+    if (rc) return rc;
+    *out = s->h_st->aux;
+    return STRM_OK;
+  };
+  CK(cudaMemcpyAsync(d.pw, d.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  double a = 0.0, b = 0.0;
+  CK(launch_apply_correction(d, s->g, q, scale, s->stream));
+  int rc = norm_after(&b);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  rc = norm_after(&a);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  const bool take = b < a;
+  if (take) CK(launch_apply_correction(d, s->g, q, scale, s->stream));
+  CK(launch_pcopy(d, s->g, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (ns_prev) *ns_prev = a;
+  if (ns_pred) *ns_pred = b;
+  if (accepted) *accepted = take ? 1 : 0;
+  return STRM_OK;
+}
+
 int strm_copy_field_device(strm_sim *s, int field, double *dense, int to_sim) {
   if (!s || !dense) return fail(STRM_ERR_INVALID, "invalid arguments");
   double *f = field_ptr(s, field);

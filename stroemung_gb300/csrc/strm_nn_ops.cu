@@ -498,6 +498,72 @@ __global__ void copy_adjoint_to_q(const float *gp, const uint8_t *flags, const f
   }
 }
 
+// Error loss against a target pressure (the converged solution): on fluid
+// interior cells e = p_prev + s dx^2 q - p_target and d = p_target - p_prev,
+// both with their fluid mean removed (the pressure is defined up to a
+// constant); loss_b = sum e^2 / sum d^2.  Pass 1 sums e, d and the cell count
+// per sample, pass 2 the squares, pass 3 the gradient with respect to q.
+__device__ __forceinline__ bool interior_fluid(const uint8_t *flags, long long i, int x, int y,
+                                               int nx, int ny) {
+  return flags[i] == 0 && x > 0 && y > 0 && x < nx - 1 && y < ny - 1;
+}
+
+__device__ __forceinline__ float err_raw(const float *pprev, const float *q, const float *pt,
+                                         const float *smax, float dx2, long long i, int b, int x,
+                                         int y, int nx, int ny) {
+  const float s = smax[b] > 0.0f ? smax[b] : 1.0f;
+  const float qv = q[(long long)b * (nx - 2) * (ny - 2) + (long long)(x - 1) * (ny - 2) + (y - 1)];
+  return pprev[i] + s * dx2 * qv - pt[i];
+}
+
+__global__ void error_sums(const float *pprev, const float *q, const float *pt,
+                           const uint8_t *flags, const float *smax, float dx2, float *work,
+                           int batch, int nx, int ny, int pass) {
+  // work: [0,B) sum e, [B,2B) sum d, [2B,3B) count, [3B,4B) sum e^2, [4B,5B) sum d^2
+  const long long plane = (long long)nx * ny;
+  GRID_STRIDE(i, (long long)batch * plane) {
+    const int b = (int)(i / plane);
+    const int j = (int)(i - (long long)b * plane);
+    const int x = j / ny, y = j % ny;
+    if (!interior_fluid(flags, i, x, y, nx, ny)) continue;
+    const float e = err_raw(pprev, q, pt, smax, dx2, i, b, x, y, nx, ny);
+    const float d = pt[i] - pprev[i];
+    if (pass == 0) {
+      atomicAdd(work + b, e);
+      atomicAdd(work + batch + b, d);
+      atomicAdd(work + 2 * batch + b, 1.0f);
+    } else {
+      const float c = work[2 * batch + b];
+      const float em = e - work[b] / c, dm = d - work[batch + b] / c;
+      atomicAdd(work + 3 * batch + b, em * em);
+      atomicAdd(work + 4 * batch + b, dm * dm);
+    }
+  }
+}
+
+__global__ void error_grad(const float *pprev, const float *q, const float *pt,
+                           const uint8_t *flags, const float *smax, float dx2, const float *work,
+                           float *loss, float *gq, int batch, int nx, int ny) {
+  const int h = nx - 2, w = ny - 2;
+  GRID_STRIDE(k, (long long)batch * h * w) {
+    const int b = (int)(k / ((long long)h * w));
+    const int rem = (int)(k - (long long)b * h * w);
+    const int x = rem / w + 1, y = rem % w + 1;
+    const long long i = (long long)b * nx * ny + (long long)x * ny + y;
+    const float d2 = work[4 * batch + b] > 0.0f ? work[4 * batch + b] : 1.0f;
+    if (rem == 0 && loss) loss[b] = work[3 * batch + b] / d2;
+    if (!gq) continue;
+    float g = 0.0f;
+    if (flags[i] == 0) {
+      const float s = smax[b] > 0.0f ? smax[b] : 1.0f;
+      const float em =
+          err_raw(pprev, q, pt, smax, dx2, i, b, x, y, nx, ny) - work[b] / work[2 * batch + b];
+      g = (2.0f / (float)batch) * em / d2 * s * dx2;
+    }
+    gq[k] = g;
+  }
+}
+
 __global__ void mean_div(const float *sum, const float *cnt, float *out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = cnt[i] > 0.0f ? sum[i] / cnt[i] : 0.0f;
@@ -689,6 +755,24 @@ int strm_nn_residual_loss_grad(const float *r, const uint8_t *flags, const float
   residual_grad_p<<<grid_for(n), 256, 0, s>>>(r, flags, sum_b2, rdx2, rdy2, gp, batch, nx, ny);
   copy_adjoint_to_q<<<grid_for((long long)batch * (nx - 2) * (ny - 2)), 256, 0, s>>>(
       gp, flags, smax, dx2, gq, batch, nx, ny);
+  return done();
+}
+
+int strm_nn_error_loss(const float *pprev, const float *q, const float *ptarget,
+                       const uint8_t *flags, const float *smax, float dx2, float *work,
+                       float *loss, float *gq, int batch, int nx, int ny, void *stream) {
+  if (!pprev || !q || !ptarget || !flags || !smax || !work || nx < 3 || ny < 3 || batch < 1)
+    return STRM_NN_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(work, 0, sizeof(float) * 5 * batch, s) != cudaSuccess)
+    return STRM_NN_ERR_CUDA;
+  const long long n = (long long)batch * nx * ny;
+  error_sums<<<grid_for(n), 256, 0, s>>>(pprev, q, ptarget, flags, smax, dx2, work, batch, nx,
+                                         ny, 0);
+  error_sums<<<grid_for(n), 256, 0, s>>>(pprev, q, ptarget, flags, smax, dx2, work, batch, nx,
+                                         ny, 1);
+  error_grad<<<grid_for((long long)batch * (nx - 2) * (ny - 2)), 256, 0, s>>>(
+      pprev, q, ptarget, flags, smax, dx2, work, loss, gq, batch, nx, ny);
   return done();
 }
 

@@ -1,20 +1,31 @@
 """Learned warm start for the pressure solve: snapshot generation, training
 and the in-the-loop predictor with plain SOR as judge and fallback.
 
-Snapshots come from the solver itself: seeded channel problems (the
-benchmark's placement rules), each stepped with ``tick_prepare`` /
-``tick_solve``; between the two the step's RHS, the previous pressure and
-the flags are exported (FP32 / u8, full [nx][ny] planes) — the network's
-input — and the step then solves as usual.
+Snapshots come from the solver itself: seeded problems (channels with the
+benchmark's obstacle placement rules, or lid-driven cavities), each stepped
+with ``tick_prepare`` / ``tick_solve``; between the two the step's RHS, the
+previous pressure and the flags are exported (FP32 / u8, full [nx][ny]
+planes) — the network's input — and, when targets are asked for, the
+pressure the solve reached afterwards (the training target of the error
+loss).
+
+Two losses: ``residual`` (the relative Poisson residual of the corrected
+pressure, Σr²/Σrhs²) and ``error`` (the relative error against the solved
+pressure, both mean-free on fluid cells).  Measured: the residual loss
+learns to remove the rough part of the error, which the first SOR sweeps
+remove anyway, and saves no sweeps; the error loss learns the smooth part,
+which is what SOR is slow on.
 
 In the loop (``WarmStartSolver.step``): after ``tick_prepare`` the network
-predicts a correction q; the corrected pressure p_prev + s*dx^2*q replaces
-p_prev only if its residual norm (the solver's own norm, after the boundary
-copy) is lower than p_prev's; then ``tick_solve`` runs the unchanged
-pressure solve from there.
+predicts a correction q; ``strm_judge_correction`` keeps p_prev + s*dx^2*q
+only if it beats p_prev on the solver's own norm — right away (judge_sweeps
+0: the initial residual) or after judge_sweeps red-black iterations of both
+(a smooth correction with a little rough error has the larger raw residual)
+— then ``tick_solve`` runs the unchanged solve to the same stop rule.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import time
 
@@ -25,14 +36,17 @@ from .unet import IN_CH, UNet
 
 
 class PlaneBatch:
-    """Device planes for `batch` samples of one grid size."""
+    """Device planes for `batch` samples of one grid size (target: the
+    solved pressure of each sample, allocated on request)."""
 
-    def __init__(self, batch, nx, ny, device="cuda"):
+    def __init__(self, batch, nx, ny, device="cuda", targets=False):
         import torch
         self.batch, self.nx, self.ny = batch, nx, ny
         self.rhs = torch.zeros(batch, nx, ny, dtype=torch.float32, device=device)
         self.p = torch.zeros(batch, nx, ny, dtype=torch.float32, device=device)
         self.flags = torch.zeros(batch, nx, ny, dtype=torch.uint8, device=device)
+        self.target = (torch.zeros(batch, nx, ny, dtype=torch.float32, device=device)
+                       if targets else None)
 
 
 def export_sample(sim, planes: PlaneBatch, i: int):
@@ -41,6 +55,13 @@ def export_sample(sim, planes: PlaneBatch, i: int):
     _lib.check(_lib.load().strm_export_planes(
         sim._h, planes.rhs.data_ptr() + 4 * off, planes.p.data_ptr() + 4 * off,
         planes.flags.data_ptr() + off))
+
+
+def export_target(sim, planes: PlaneBatch, i: int):
+    """Copies sim's pressure (after the solve) into sample i's target."""
+    off = i * planes.nx * planes.ny
+    _lib.check(_lib.load().strm_export_planes(sim._h, None, planes.target.data_ptr() + 4 * off,
+                                              None))
 
 
 def channel_problem(rng, imax, jmax, seed, nrect=None, re=None):
@@ -61,8 +82,8 @@ SOLVER = {"sor_absolute_epsilon": 1e-3, "max_iterations": 2000, "omega": 1.7, "t
 
 
 def make_simulation(grid, re, dx, **solver):
-    """A channel Simulation with the solver settings the warm start uses:
-    mixed precision, strict eps on the mean-free fluid-cell residual."""
+    """A Simulation with the solver settings the warm start uses: mixed
+    precision, strict eps on the mean-free fluid-cell residual."""
     from .simulation import NORM_FLUID_MEAN_FREE, PREC_MIXED, Simulation
     cfg = dict(SOLVER)
     cfg.update(solver)
@@ -71,37 +92,65 @@ def make_simulation(grid, re, dx, **solver):
               "sweep_schedule"):
         if k in cfg:
             mode[k] = cfg.pop(k)
-    return Simulation(grid=grid, cell_size=(dx, dx), delt=0.5 * dx, reynolds=re, **cfg, **mode)
+    delt = cfg.pop("delt", 0.5 * dx)
+    return Simulation(grid=grid, cell_size=(dx, dx), delt=delt, reynolds=re, **cfg, **mode)
+
+
+def channel_family(imax=512, jmax=128, dx=0.01):
+    """Problem family: seeded channels (the benchmark's geometry rules)."""
+    def make(rng, seed, **solver):
+        grid, re = channel_problem(rng, imax, jmax, seed)
+        return make_simulation(grid, re, dx, **solver)
+    return make, (imax + 2, jmax + 2)
+
+
+def cavity_family(n=128, re_range=(50.0, 2000.0)):
+    """Problem family: n x n lid-driven cavities, unit square, Reynolds
+    number log-uniform in re_range."""
+    def make(rng, seed, **solver):
+        re = float(np.exp(rng.uniform(math.log(re_range[0]), math.log(re_range[1]))))
+        cfg = dict(delt=1e-3, max_iterations=40000)
+        cfg.update(solver)
+        return make_simulation(presets.cavity(n), re, 1.0 / n, **cfg)
+    return make, (n + 2, n + 2)
 
 
 def generate_snapshots(n_snapshots, imax=512, jmax=128, dx=0.01, steps_per_problem=25,
-                       seed=0, device="cuda", **solver):
-    """Runs seeded channel problems and returns a PlaneBatch with one sample
-    per step (RHS, previous pressure, flags)."""
-    planes = PlaneBatch(n_snapshots, imax + 2, jmax + 2, device)
+                       seed=0, device="cuda", family=None, targets=False, **solver):
+    """Runs seeded problems (channels of imax x jmax unless `family` is given)
+    and returns a PlaneBatch with one sample per step (RHS, previous
+    pressure, flags, and with targets the solved pressure)."""
+    make, (nx, ny) = family if family is not None else channel_family(imax, jmax, dx)
+    planes = PlaneBatch(n_snapshots, nx, ny, device, targets=targets)
     rng = np.random.default_rng(seed)
     i = 0
     k = 0
     while i < n_snapshots:
-        grid, re = channel_problem(rng, imax, jmax, seed * 100003 + k)
+        sim = make(rng, seed * 100003 + k, **solver)
         k += 1
-        sim = make_simulation(grid, re, dx, **solver)
         for _ in range(steps_per_problem):
             if i >= n_snapshots:
                 break
             sim.tick_prepare()
             export_sample(sim, planes, i)
-            i += 1
             sim.tick_solve()
+            if targets:
+                export_target(sim, planes, i)
+            i += 1
         sim.close()
     return planes
 
 
 class Trainer:
-    """Adam on the relative Poisson residual of the corrected pressure."""
+    """Adam on the relative Poisson residual of the corrected pressure
+    (loss="residual") or on its relative error against the solved pressure
+    (loss="error", planes with targets)."""
 
-    def __init__(self, net: UNet, nx, ny, dx, dy, batch=32):
+    def __init__(self, net: UNet, nx, ny, dx, dy, batch=32, loss="residual"):
         import torch
+        if loss not in ("residual", "error"):
+            raise ValueError(loss)
+        self.kind = loss
         self.net, self.nx, self.ny, self.batch = net, nx, ny, batch
         self.dx2 = dx * dx
         self.rdx2, self.rdy2 = 1.0 / (dx * dx), 1.0 / (dy * dy)
@@ -117,15 +166,18 @@ class Trainer:
         self.gq = torch.zeros(batch, h, w, dtype=torch.float32, device=dev)
         self.sum_r2 = torch.zeros(batch, dtype=torch.float32, device=dev)
         self.sum_b2 = torch.zeros(batch, dtype=torch.float32, device=dev)
+        self.work5 = torch.zeros(5 * batch, dtype=torch.float32, device=dev)
+        self.per = torch.zeros(batch, dtype=torch.float32, device=dev)
 
     def _planes(self, planes: PlaneBatch, start):
         off = start * self.nx * self.ny
         return (planes.rhs.data_ptr() + 4 * off, planes.flags.data_ptr() + off,
                 planes.p.data_ptr() + 4 * off)
 
-    def loss(self, planes: PlaneBatch, start, batch=None, forward=True):
-        """Mean relative residual of samples [start, start+batch) after the
-        network's correction (forward) and the per-sample values."""
+    def loss(self, planes: PlaneBatch, start, batch=None, grad=False):
+        """Mean loss of samples [start, start+batch) after the network's
+        correction and the per-sample values (grad: also the gradient with
+        respect to q into self.gq)."""
         b = self.batch if batch is None else batch
         L = self.net.L
         rhs, flags, pprev = self._planes(planes, start)
@@ -135,27 +187,32 @@ class Trainer:
                                                 self.dx2, self.xin.data_ptr(), b, self.nx,
                                                 self.ny, None), "prepare")
         q = self.net.forward(self.xin, b, h, w)
+        if self.kind == "error":
+            off = start * self.nx * self.ny
+            self.net._check(L.strm_nn_error_loss(
+                pprev, q.data_ptr(), planes.target.data_ptr() + 4 * off, flags,
+                self.smax.data_ptr(), self.dx2, self.work5.data_ptr(), self.per.data_ptr(),
+                self.gq.data_ptr() if grad else None, b, self.nx, self.ny, None), "error loss")
+            per = self.per[:b].detach().cpu().numpy()
+            return float(per.mean()), per
         self.net._check(L.strm_nn_residual_loss(pprev, q.data_ptr(), flags, rhs,
                                                 self.smax.data_ptr(), self.dx2, self.rdx2,
                                                 self.rdy2, self.pfull.data_ptr(),
                                                 self.r.data_ptr(), self.sum_r2.data_ptr(),
                                                 self.sum_b2.data_ptr(), b, self.nx, self.ny,
                                                 None), "loss")
+        if grad:
+            self.net._check(L.strm_nn_residual_loss_grad(
+                self.r.data_ptr(), flags, self.sum_b2.data_ptr(), self.smax.data_ptr(),
+                self.dx2, self.rdx2, self.rdy2, self.gp.data_ptr(), self.gq.data_ptr(), b,
+                self.nx, self.ny, None), "loss grad")
         per = (self.sum_r2[:b] / self.sum_b2[:b].clamp_min(1e-30)).detach().cpu().numpy()
         return float(per.mean()), per
 
     def train_step(self, planes: PlaneBatch, start, lr=1e-3):
-        L = self.net.L
         b = self.batch
-        rhs, flags, pprev = self._planes(planes, start)
-        loss, _ = self.loss(planes, start)
+        loss, _ = self.loss(planes, start, grad=True)
         self.net.zero_grad()
-        self.net._check(L.strm_nn_residual_loss_grad(self.r.data_ptr(), flags,
-                                                     self.sum_b2.data_ptr(),
-                                                     self.smax.data_ptr(), self.dx2, self.rdx2,
-                                                     self.rdy2, self.gp.data_ptr(),
-                                                     self.gq.data_ptr(), b, self.nx, self.ny,
-                                                     None), "loss grad")
         self.net.backward(self.gq, b, self.nx - 2, self.ny - 2)
         self.net.adam(lr=lr)
         return loss
@@ -185,13 +242,13 @@ class WarmStartSolver:
     previous pressure is restored (plain SOR is judge and fallback); then
     tick_solve runs the unchanged solve from there."""
 
-    def __init__(self, sim, net: UNet):
+    def __init__(self, sim, net: UNet, judge_sweeps: int = 0):
         import torch
         self.sim, self.net = sim, net
+        self.judge_sweeps = int(judge_sweeps)
         nx, ny = sim.size
         self.planes = PlaneBatch(1, nx, ny, net.device)
         self.trainer = Trainer(net, nx, ny, sim.cell_size[0], sim.cell_size[1], batch=1)
-        self.backup = torch.zeros(nx, ny, dtype=torch.float64, device=net.device)
         self.accepted = 0
         self.rejected = 0
         self.last = {}
@@ -213,22 +270,25 @@ class WarmStartSolver:
         return q, float(tr.smax[0].item()) * tr.dx2
 
     def judge(self, q, scale):
-        """Applies the correction if it lowers the residual norm; returns
-        (accepted, norm before, norm with the correction)."""
-        sim, L = self.sim, _lib.load()
-        sim.copy_pressure_to_boundaries()
-        ns_prev = sim.calculate_norm_squared()
-        _lib.check(L.strm_copy_field_device(sim._h, _lib.FIELD_P, self.backup.data_ptr(), 0))
-        _lib.check(L.strm_apply_correction(sim._h, q.data_ptr(), scale))
-        sim.copy_pressure_to_boundaries()
-        ns_pred = sim.calculate_norm_squared()
-        accepted = ns_pred < ns_prev
-        if accepted:
+        """Keeps the correction if it beats the previous pressure on the
+        solver's norm (after judge_sweeps red-black iterations of both;
+        judge_sweeps < 0 takes it unjudged); returns (accepted, norm
+        without, norm with the correction)."""
+        if self.judge_sweeps < 0:  # no judge: always take the prediction
+            _lib.check(_lib.load().strm_apply_correction(self.sim._h, q.data_ptr(), scale))
+            self.sim.copy_pressure_to_boundaries()
+            self.accepted += 1
+            return True, float("nan"), float("nan")
+        a, b = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        acc = ctypes.c_int(0)
+        _lib.check(_lib.load().strm_judge_correction(
+            self.sim._h, q.data_ptr(), scale, self.judge_sweeps, ctypes.byref(a),
+            ctypes.byref(b), ctypes.byref(acc)))
+        if acc.value:
             self.accepted += 1
         else:
             self.rejected += 1
-            _lib.check(L.strm_copy_field_device(sim._h, _lib.FIELD_P, self.backup.data_ptr(), 1))
-        return accepted, ns_prev, ns_pred
+        return bool(acc.value), a.value, b.value
 
     def step(self):
         t0 = time.perf_counter()
@@ -275,8 +335,11 @@ def compare_step(plain, ws: WarmStartSolver, scratch):
     accepted, ns_prev, ns_pred = ws.judge(q, scale)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    t3 = time.perf_counter()
     it_p, ns_p = plain.tick_solve()
+    t4 = time.perf_counter()
     it_w, ns_w = ws.sim.tick_solve()
+    t5 = time.perf_counter()
     hp, hw = plain.residual_history(), ws.sim.residual_history()
     sync_state(ws.sim, plain, scratch)
     return {"sweeps_plain": it_p, "sweeps_ws": it_w, "ns_plain": ns_p, "ns_ws": ns_w,
@@ -284,4 +347,5 @@ def compare_step(plain, ws: WarmStartSolver, scratch):
             "ns_prev": ns_prev, "ns_pred": ns_pred,
             "ws_sweeps_to_plain_final": sweeps_to_reach(hw, ns_p),
             "predict_ms": (t1 - t0) * 1e3, "judge_ms": (t2 - t1) * 1e3,
+            "solve_plain_ms": (t4 - t3) * 1e3, "solve_ws_ms": (t5 - t4) * 1e3,
             "hist_plain": hp, "hist_ws": hw}

@@ -207,3 +207,88 @@ def test_training_lowers_the_loss():
     tr.fit(train, epochs=40, lr=1e-3)
     after, _ = tr.loss(held, 0)
     assert after < 0.8 * before, (before, after)
+
+
+def test_error_loss_and_gradient_match_numpy():
+    """strm_nn_error_loss: relative mean-free error of the corrected pressure
+    against a target on fluid interior cells, and its gradient with respect
+    to q, against a float64 numpy restatement."""
+    import torch
+    from stroemung_gb300 import _lib
+    L = _lib.load()
+    b, nx, ny, dx2 = 3, 20, 14, 1e-4
+    rng = np.random.default_rng(7)
+    pprev = rng.normal(size=(b, nx, ny)).astype(np.float32)
+    pt = (pprev + 0.1 * rng.normal(size=(b, nx, ny))).astype(np.float32)
+    q = rng.normal(size=(b, nx - 2, ny - 2)).astype(np.float32)
+    flags = np.zeros((b, nx, ny), np.uint8)
+    flags[:, 0, :] = flags[:, -1, :] = flags[:, :, 0] = flags[:, :, -1] = 1
+    flags[:, 6:9, 4:7] = 1 | (2 << 3)
+    smax = np.array([50.0, 0.0, 3.0], np.float32)  # a zero scale counts as 1
+    dev = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    t_pp, t_pt, t_q, t_fl, t_s = dev(pprev), dev(pt), dev(q), dev(flags), dev(smax)
+    work = torch.zeros(5 * b, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(b, dtype=torch.float32, device="cuda")
+    gq = torch.zeros_like(t_q)
+    assert L.strm_nn_error_loss(t_pp.data_ptr(), t_q.data_ptr(), t_pt.data_ptr(), t_fl.data_ptr(),
+                                t_s.data_ptr(), dx2, work.data_ptr(), loss.data_ptr(),
+                                gq.data_ptr(), b, nx, ny, None) == 0
+    torch.cuda.synchronize()
+    s = np.where(smax > 0, smax, 1.0).astype(np.float64)
+    fl = flags[:, 1:-1, 1:-1] == 0
+    want_loss = np.zeros(b)
+    want_g = np.zeros((b, nx - 2, ny - 2))
+    for k in range(b):
+        e = pprev[k, 1:-1, 1:-1] + s[k] * dx2 * q[k] - pt[k, 1:-1, 1:-1]
+        d = pt[k, 1:-1, 1:-1] - pprev[k, 1:-1, 1:-1]
+        em = e[fl[k]] - e[fl[k]].mean()
+        dm = d[fl[k]] - d[fl[k]].mean()
+        want_loss[k] = (em ** 2).sum() / (dm ** 2).sum()
+        want_g[k][fl[k]] = 2.0 / b * em / (dm ** 2).sum() * s[k] * dx2
+    np.testing.assert_allclose(loss.cpu().numpy(), want_loss, rtol=1e-4)
+    np.testing.assert_allclose(gq.cpu().numpy(), want_g, rtol=1e-3,
+                               atol=1e-4 * np.abs(want_g).max())
+    # the gradient is the derivative of the batch-mean loss: a finite
+    # difference along it agrees
+    h = 0.1
+    qs = (q + h * want_g / np.abs(want_g).max()).astype(np.float32)
+    t_q.copy_(dev(qs))
+    assert L.strm_nn_error_loss(t_pp.data_ptr(), t_q.data_ptr(), t_pt.data_ptr(), t_fl.data_ptr(),
+                                t_s.data_ptr(), dx2, work.data_ptr(), loss.data_ptr(), None,
+                                b, nx, ny, None) == 0
+    torch.cuda.synchronize()
+    dl = loss.cpu().numpy().mean() - want_loss.mean()
+    pred = h * (want_g ** 2).sum() / np.abs(want_g).max()
+    assert abs(dl - pred) <= 0.05 * abs(pred), (dl, pred)
+
+
+def test_learned_warm_start_saves_sweeps_on_cavities():
+    """Trained on solved pressures of 64 x 64 lid-driven cavities (error
+    loss) and judged after 16 red-black iterations, the network's correction
+    brings a held-out cavity to the strict stop rule in fewer sweeps than the
+    plain solve from the previous pressure, stepped A/B from identical
+    states; the fields stay those of the plain run."""
+    import torch
+    from stroemung_gb300 import presets, warmstart
+    from stroemung_gb300.unet import UNet
+    n = 64
+    fam = warmstart.cavity_family(n)
+    train = warmstart.generate_snapshots(512, family=fam, steps_per_problem=32, seed=1,
+                                         targets=True)
+    net = UNet(seed=0)
+    tr = warmstart.Trainer(net, n + 2, n + 2, 1.0 / n, 1.0 / n, batch=32, loss="error")
+    tr.fit(train, epochs=25, lr=1e-3)
+    cfg = dict(delt=1e-3, max_iterations=40000)
+    plain = warmstart.make_simulation(presets.cavity(n), 400.0, 1.0 / n, **cfg)
+    wsim = warmstart.make_simulation(presets.cavity(n), 400.0, 1.0 / n, **cfg)
+    ws = warmstart.WarmStartSolver(wsim, net, judge_sweeps=16)
+    scratch = torch.zeros(n + 2, n + 2, dtype=torch.float64, device="cuda")
+    sp = sw = 0
+    for _ in range(16):
+        r = warmstart.compare_step(plain, ws, scratch)
+        assert r["ns_plain"] < 1e-6 and r["ns_ws"] < 1e-6
+        sp += r["sweeps_plain"]
+        sw += r["sweeps_ws"]
+    plain.close()
+    wsim.close()
+    assert sw <= 0.95 * sp, (sp, sw)
