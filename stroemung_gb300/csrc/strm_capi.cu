@@ -68,7 +68,7 @@ struct strm_sim {
   cudaGraphExec_t exec_pre = nullptr, exec_post = nullptr;
   StepState *h_st = nullptr;   // pinned
   StepLog *h_log = nullptr;    // pinned
-  int bc_cap = 0, pcopy_cap = 0;
+  int bc_cap = 0, pcopy_cap = 0, edge_cap = 0;
   void *rgba = nullptr;        // colour-map image, allocated on first use
 };
 
@@ -205,6 +205,33 @@ int classify_and_compile(strm_sim *s, long long *bad_out) {
     s->pcopy_cap = (int)pc.size() + 1024;
     CK(cudaMalloc(&s->d.pcopy, sizeof(PCopy) * s->pcopy_cap));
   }
+  // solver classes and the edge list of the FAST red-black solve
+  std::vector<uint8_t> cls(flags.size(), 2);
+  std::vector<unsigned int> elist;
+  for (int x = 1; x + 1 < g.nx; ++x)
+    for (int y = 1; y + 1 < g.ny; ++y) {
+      const size_t i = (size_t)x * g.ny + y;
+      const unsigned int off = (unsigned int)((size_t)x * g.pitch + y);
+      if (flags[i] != 0) {
+        elist.push_back(off);
+        continue;
+      }
+      const bool edge = flags[i - g.ny] || flags[i + g.ny] || flags[i - 1] || flags[i + 1];
+      cls[i] = edge ? 1 : 0;
+      if (edge && ((x + y) & 1) == 0) elist.push_back(off);
+    }
+  if ((int)elist.size() > s->edge_cap) {
+    if (s->d.edge_list) cudaFree(s->d.edge_list);
+    s->d.edge_list = nullptr;
+    s->edge_cap = (int)elist.size() + 1024;
+    CK(cudaMalloc(&s->d.edge_list, sizeof(unsigned int) * s->edge_cap));
+  }
+  s->d.n_edge = (int)elist.size();
+  if (!elist.empty())
+    CK(cudaMemcpyAsync(s->d.edge_list, elist.data(), sizeof(unsigned int) * elist.size(),
+                       cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpy2DAsync(s->d.cls, g.pitch, cls.data(), g.ny, g.ny, g.nx, cudaMemcpyHostToDevice,
+                       s->stream));
   s->d.n_bc = (int)prog.size();
   s->d.n_pcopy = (int)pc.size();
   if (!prog.empty())
@@ -226,6 +253,7 @@ void free_sim(strm_sim *s) {
   if (s->d.bc) cudaFree(s->d.bc);
   if (s->d.bc_val) cudaFree(s->d.bc_val);
   if (s->d.pcopy) cudaFree(s->d.pcopy);
+  if (s->d.edge_list) cudaFree(s->d.edge_list);
   if (s->rgba) cudaFree(s->rgba);
   if (s->h_st) cudaFreeHost(s->h_st);
   if (s->h_log) cudaFreeHost(s->h_log);
@@ -269,6 +297,10 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   *out = nullptr;
   if (!params || !kinds || !u || !v || !p || nx < 1 || ny < 1)
     return fail(STRM_ERR_INVALID, "invalid arguments");
+  // cell offsets of the solver's lists are 32-bit (a grid this large would
+  // not fit in device memory anyway)
+  if ((unsigned long long)nx * align_up((size_t)ny, 16) >= (1ULL << 32))
+    return fail(STRM_ERR_INVALID, "grid of %d x %d cells is too large", nx, ny);
   const size_t ncell = (size_t)nx * ny;
   for (size_t i = 0; i < ncell; ++i)
     if (kinds[i] > STRM_MOVING_WALL)
@@ -319,6 +351,9 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   const size_t o_st = take(sizeof(StepState));
   const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
   const size_t o_partb = take(sizeof(double) * 2 * (size_t)black_pass_blocks(s->g));
+  const size_t o_partr = take(sizeof(double) * 2 * (size_t)black_pass_blocks(s->g));
+  const size_t o_parte = take(sizeof(double) * 2 * (size_t)kEdgeBlocksMax);
+  const size_t o_cls = take(nfield);
   const size_t o_log = take(sizeof(StepLog) * kLogCap);
   const size_t o_bad = take(8), o_fc = take(8);
   const size_t o_hist = take(sizeof(double) * 2 * kHistCap);
@@ -342,6 +377,9 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   d.partials = (double *)(base + o_part);
   d.n_partials = 4 * nb;
   d.partials_b = (double *)(base + o_partb);
+  d.partials_r = (double *)(base + o_partr);
+  d.partials_e = (double *)(base + o_parte);
+  d.cls = (uint8_t *)(base + o_cls);
   d.log = (StepLog *)(base + o_log);
   d.first_bad = (long long *)(base + o_bad);
   d.fluid_count = (unsigned long long *)(base + o_fc);

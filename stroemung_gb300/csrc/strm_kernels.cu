@@ -421,32 +421,74 @@ __global__ void __launch_bounds__(256)
   p[o] = sor_update<EXACT>(pc, pw, pe, pn, ps, rhs[o], c);
 }
 
+// The colour passes of the FAST red-black solve stride over the virtual
+// blocks of the colour-pass layout (gx x gy blocks of kRedBlock threads, a
+// thread per cell pair, as sor_color_kernel) with a fixed number of resident
+// blocks, each reducing once.  A thread takes kPassUnroll virtual blocks at
+// a time and issues every load of those cells (class byte, the five
+// pressures, rhs) before it uses one: the pressure loads do not wait for the
+// class byte, and several cells' loads are in flight.  The FP64 pipe is the
+// bound; memory latency is what keeps it idle.
+constexpr int kPassUnroll = 2;
+
+struct PassCells {
+  size_t o[kPassUnroll];
+  bool ok[kPassUnroll];
+};
+
+// The cells of colour `color` a thread owns in virtual blocks vb0,
+// vb0 + stride, ...; cells outside the interior get a harmless address (an
+// interior cell) and ok = false.
+__device__ __forceinline__ PassCells pass_cells(int vb0, int stride, int nvb, int gx, int color,
+                                                const Geom &g) {
+  PassCells pc;
+#pragma unroll
+  for (int u = 0; u < kPassUnroll; ++u) {
+    const int vb = vb0 + u * stride;
+    const int x = 1 + (vb / gx) * blockDim.y + threadIdx.y;
+    const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + ((x + color) & 1);
+    pc.ok[u] = vb < nvb && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2;
+    pc.o[u] = pc.ok[u] ? OFF(x, y) : OFF(1, 1);
+  }
+  return pc;
+}
+
 // The black pass of a FAST red-black iteration fused with the residual of the
 // black fluid cells: once they are updated their four (red) neighbours are
 // final, so r = t - 2(1/dx^2+1/dy^2) p_new with t from the update (the same
-// p_new as sor_color_kernel<false>).  The grid strides over the colour
-// pass's blocks (gx x gy of them, the layout of sor_color_kernel) so that a
-// block reduces once: its sums of r^2 (and r when mean-free) go to
-// partials_b[blockIdx.x]; residual_kernel adds the other cells.
+// p_new as sor_color_kernel<false>).  Its sums of r^2 (and r when mean-free)
+// go to partials_b[blockIdx.x].
 __global__ void __launch_bounds__(256)
     sor_black_res_kernel(double *__restrict__ p, const double *__restrict__ rhs,
                          const uint8_t *__restrict__ flags, Geom g, Consts c,
                          double *__restrict__ partials_b, int mean_free, int gx, int nvb) {
   double acc = 0.0, acc1 = 0.0;
-  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-    const int x = 1 + (vb / gx) * blockDim.y + threadIdx.y;
-    const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + ((x + 1) & 1);
-    if (x > g.nx - 2 || y < 1 || y > g.ny - 2) continue;
-    const size_t o = OFF(x, y);
-    if (flags[o] != 0) continue;
-    const double pc = p[o];
-    const double t = fma(p[o + g.pitch] + p[o - g.pitch], c.r_dx2,
-                         fma(p[o + 1] + p[o - 1], c.r_dy2, -rhs[o]));
-    const double pn = fma(c.one_minus_w, pc, c.middle * t);
-    p[o] = pn;
-    const double r = fma(-c.two_r_sum, pn, t);
-    acc = fma(r, r, acc);
-    if (mean_free) acc1 += r;
+  for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
+    const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 1, g);
+    unsigned int f[kPassUnroll];
+    double pc[kPassUnroll], pe[kPassUnroll], pw[kPassUnroll], pn[kPassUnroll], ps[kPassUnroll],
+        rh[kPassUnroll];
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      const size_t o = cells.o[u];
+      f[u] = flags[o];
+      pc[u] = p[o];
+      pe[u] = p[o + g.pitch];
+      pw[u] = p[o - g.pitch];
+      ps[u] = p[o + 1];
+      pn[u] = p[o - 1];
+      rh[u] = rhs[o];
+    }
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      if (!cells.ok[u] || f[u] != 0) continue;
+      const double t = fma(pe[u] + pw[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
+      const double pnew = fma(c.one_minus_w, pc[u], c.middle * t);
+      p[cells.o[u]] = pnew;
+      const double r = fma(-c.two_r_sum, pnew, t);
+      acc = fma(r, r, acc);
+      if (mean_free) acc1 += r;
+    }
   }
   const double bsum = block_reduce(acc, OpAdd(), 0.0);
   if (mean_free) {
@@ -497,6 +539,39 @@ __device__ __forceinline__ double finish_norm2(const double *pa, int na, const d
   const double s1 = reduce_partials(pa, na, 2, 1, OpAdd(), 0.0) +
                     reduce_partials(pb, nb, 2, 1, OpAdd(), 0.0);
   return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
+
+// Bookkeeping of one pressure iteration once its norm is known
+// (src/simulation.rs:272-281): counts it, records the norm, applies the stop
+// rule and ends the graph's WHILE loop at the stop or at itermax.
+template <bool IN_GRAPH>
+__device__ __forceinline__ void solve_iteration_done(StepState *st, double ns, const Consts &c,
+                                                     int strict, unsigned int itermax,
+                                                     cudaGraphConditionalHandle h) {
+  const unsigned int it = st->sor_iters + 1;
+  st->sor_iters = it;
+  st->ns = ns;
+  hist_push(st, it, ns);
+  st->nonfinite = !isfinite(ns);
+  const bool done = stop_rule(ns, c, st, strict);
+  if (done) st->converged = 1;
+  else if (it >= itermax) st->exhausted = 1;
+  if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
+}
+
+// Independent bound on a WHILE loop: the stop test ends it at iteration
+// itermax at the latest; should that bookkeeping ever fail, this ends it two
+// launches later and flags the step.
+template <bool IN_GRAPH>
+__device__ __forceinline__ void loop_guard(StepState *st, unsigned int itermax,
+                                           cudaGraphConditionalHandle h) {
+  if (IN_GRAPH && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
+    if (launches >= itermax + 2) {
+      st->overrun = 1;
+      cudaGraphSetConditional(h, 0);
+    }
+  }
 }
 
 // This thread's share of the residual sums over the block's tiles: sum r^2
@@ -574,16 +649,7 @@ __global__ void __launch_bounds__(256)
   } else if (threadIdx.x == 0 && threadIdx.y == 0) {
     partials[blockIdx.x] = bsum;
   }
-  if (IN_GRAPH && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-    // Independent bound on the WHILE loop: the normal stop below ends it at
-    // iteration itermax at the latest; should that bookkeeping ever fail,
-    // this ends it two launches later and flags the step.
-    const unsigned int launches = atomicAdd(&st->body_count, 1u) + 1;
-    if (launches >= itermax + 2) {
-      st->overrun = 1;
-      cudaGraphSetConditional(h, 0);
-    }
-  }
+  loop_guard<IN_GRAPH>(st, itermax, h);
   if (!last_block_done(&st->counter)) return;
   const double ns = partials_b ? finish_norm2(partials, gridDim.x, partials_b, nbb, mean_free,
                                               st->fluid_cells)
@@ -598,17 +664,184 @@ __global__ void __launch_bounds__(256)
     } else if (mode == RES_NORM) {
       st->aux = ns;
     } else {
-      const unsigned int it = st->sor_iters + 1;
-      st->sor_iters = it;
-      st->ns = ns;
-      hist_push(st, it, ns);
-      st->nonfinite = !isfinite(ns);
-      const bool done = stop_rule(ns, c, st, strict);
-      if (done) st->converged = 1;
-      else if (it >= itermax) st->exhausted = 1;
-      if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
+      solve_iteration_done<IN_GRAPH>(st, ns, c, strict, itermax, h);
     }
   }
+}
+
+// ------------------------------------------------------------------------
+// FAST red-black solve with the red residual taken from the next red pass.
+//
+// Iteration k ends with the norm of the residual after its black pass.  For
+// a red fluid cell whose four neighbours are fluid, that residual is
+// t - 2(1/dx^2+1/dy^2) p with t = (pe+pw)/dx^2 + (ps+pn)/dy^2 - rhs, read
+// from the black values of iteration k and the red value p of iteration k:
+// exactly what the red pass of iteration k+1 reads before it updates p to
+// p + omega r / (2(1/dx^2+1/dy^2)) (the reference update, src/simulation.rs:
+// 260-271, rearranged).  So the red pass of iteration k+1 sums iteration k's
+// red residual and applies the stop test of k; the separate residual pass
+// over the red cells disappears (its FP64 operations and its reads of p and
+// rhs).  What that pass cannot see:
+//   * red fluid cells next to a non-fluid cell (class 1) and the non-fluid
+//     interior cells read boundary values, which the copy before iteration
+//     k+1 changes (src/grid/mod.rs:343-412; the norm of iteration k uses the
+//     stale ones).  edge_res_kernel sums those cells from a list, after the
+//     black pass of k and before that copy;
+//   * the stop itself: when iteration k stops the solve, the red pass and
+//     the boundary copy of k+1 have run.  Both saved the values they
+//     overwrote (in pw), and sor_rollback_kernel puts them back, so the
+//     solve ends on iteration k's pressure, boundary values included.
+// Iteration k+1's red pass and copy run only when k < itermax.
+// Per iteration: black pass (+ its residual), edge list, copy, red pass (+
+// the stop test), instead of copy, red, black, residual.
+// ------------------------------------------------------------------------
+
+// Solver class of a cell (per cell, pitch layout): 0 fluid interior cell with
+// four fluid neighbours, 1 fluid interior cell next to a non-fluid cell,
+// 2 anything else.
+enum : uint8_t { CLS_FLUID = 0, CLS_FLUID_EDGE = 1, CLS_OTHER = 2 };
+
+template <bool MEAN_FREE>
+__device__ __forceinline__ void store_sums(double acc, double acc1, double *partials) {
+  const double bsum = block_reduce(acc, OpAdd(), 0.0);
+  if (MEAN_FREE) {
+    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      partials[2 * blockIdx.x] = bsum;
+      partials[2 * blockIdx.x + 1] = bsum1;
+    }
+  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
+    partials[blockIdx.x] = bsum;
+  }
+}
+
+// The norm from three partial arrays (black pass, edge list, red pass), in
+// that fixed order.
+__device__ __forceinline__ double finish_norm3(const double *pa, int na, const double *pb, int nb,
+                                               const double *pc, int nc, bool mean_free,
+                                               double fluid_cells) {
+  const int st = mean_free ? 2 : 1;
+  const double s2 = reduce_partials(pa, na, st, 0, OpAdd(), 0.0) +
+                    reduce_partials(pb, nb, st, 0, OpAdd(), 0.0) +
+                    reduce_partials(pc, nc, st, 0, OpAdd(), 0.0);
+  if (!mean_free) return s2 / fluid_cells;
+  const double s1 = reduce_partials(pa, na, 2, 1, OpAdd(), 0.0) +
+                    reduce_partials(pb, nb, 2, 1, OpAdd(), 0.0) +
+                    reduce_partials(pc, nc, 2, 1, OpAdd(), 0.0);
+  return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
+
+// Residual sums of the listed cells (offsets, x-major): the non-fluid
+// interior cells (skipped by the fluid norms) and the red class-1 cells.
+template <bool FLUID, bool MEAN_FREE>
+__global__ void __launch_bounds__(256)
+    edge_res_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
+                    const uint8_t *__restrict__ flags, const unsigned int *__restrict__ list,
+                    int n, Geom g, Consts c, double *__restrict__ partials_e) {
+  double acc = 0.0, acc1 = 0.0;
+  const int nt = blockDim.x * blockDim.y;
+  for (int i = blockIdx.x * nt + threadIdx.x + threadIdx.y * blockDim.x; i < n;
+       i += gridDim.x * nt) {
+    const size_t o = list[i];
+    if (FLUID && flags[o] != 0) continue;
+    const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
+                                        rhs[o], c);
+    acc = fma(r, r, acc);
+    if (MEAN_FREE) acc1 += r;
+  }
+  store_sums<MEAN_FREE>(acc, acc1, partials_e);
+}
+
+// The boundary copy before iteration k+1 (only when k < itermax), saving the
+// values it overwrites into pw.
+__global__ void pcopy_save_kernel(double *p, double *pw, const PCopy *pc, int n, int pitch,
+                                  const StepState *st, unsigned int itermax) {
+  if (st->sor_iters + 1 >= itermax) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    pw[pc[k].off] = p[pc[k].off];
+    pcopy_one(p, pc[k], pitch);
+  }
+}
+
+// Red pass.  mode 0: update only (the first red pass of a solve, and the
+// phase entry points).  mode 1: sum the residual of iteration k over the
+// class-0 red cells, update (saving the old value into pw) only when k <
+// itermax; the last block adds the black pass's and the edge list's sums
+// and applies the stop test of iteration k.  The update is the same in both
+// modes.
+template <bool IN_GRAPH, bool MEAN_FREE>
+__global__ void __launch_bounds__(256)
+    sor_red_res_kernel(double *__restrict__ p, double *__restrict__ pw,
+                       const double *__restrict__ rhs, const uint8_t *__restrict__ cls, Geom g,
+                       Consts c, StepState *st, double *__restrict__ partials_r,
+                       const double *partials_b, int nbb, const double *partials_e, int nbe,
+                       int gx, int nvb, unsigned int itermax, int strict, int mode,
+                       cudaGraphConditionalHandle h) {
+  const bool sum = mode == 1;
+  const bool write = !sum || st->sor_iters + 1 < itermax;
+  double acc = 0.0, acc1 = 0.0;
+  for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
+    const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 0, g);
+    unsigned int k[kPassUnroll];
+    double pc[kPassUnroll], pe[kPassUnroll], pwv[kPassUnroll], pn[kPassUnroll],
+        ps[kPassUnroll], rh[kPassUnroll];
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      const size_t o = cells.o[u];
+      k[u] = cls[o];
+      pc[u] = p[o];
+      pe[u] = p[o + g.pitch];
+      pwv[u] = p[o - g.pitch];
+      ps[u] = p[o + 1];
+      pn[u] = p[o - 1];
+      rh[u] = rhs[o];
+    }
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      if (!cells.ok[u] || k[u] >= CLS_OTHER) continue;
+      const double t = fma(pe[u] + pwv[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
+      const double r = fma(-c.two_r_sum, pc[u], t);
+      if (sum && k[u] == CLS_FLUID) {
+        acc = fma(r, r, acc);
+        if (MEAN_FREE) acc1 += r;
+      }
+      if (write) {
+        if (sum) pw[cells.o[u]] = pc[u];
+        p[cells.o[u]] = fma(c.middle, r, pc[u]);
+      }
+    }
+  }
+  if (!sum) return;
+  store_sums<MEAN_FREE>(acc, acc1, partials_r);
+  loop_guard<IN_GRAPH>(st, itermax, h);
+  if (!last_block_done(&st->counter)) return;
+  const double ns = finish_norm3(partials_b, nbb, partials_e, nbe, partials_r, gridDim.x,
+                                 MEAN_FREE, st->fluid_cells);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->counter = 0;
+    solve_iteration_done<IN_GRAPH>(st, ns, c, strict, itermax, h);
+  }
+}
+
+// After the solve: when it stopped at iteration k < itermax, undo the red
+// pass and the boundary copy of iteration k+1.
+__global__ void __launch_bounds__(256)
+    sor_rollback_kernel(double *__restrict__ p, const double *__restrict__ pw,
+                        const uint8_t *__restrict__ cls, const PCopy *__restrict__ pc, int npc,
+                        Geom g, const StepState *st, unsigned int itermax, int gx, int nvb) {
+  if (!(st->converged && st->sor_iters < itermax)) return;
+  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    const int x = 1 + (vb / gx) * blockDim.y + threadIdx.y;
+    const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + (x & 1);
+    if (x > g.nx - 2 || y < 1 || y > g.ny - 2) continue;
+    const size_t o = OFF(x, y);
+    if (cls[o] < CLS_OTHER) p[o] = pw[o];
+  }
+  const int nt = blockDim.x * blockDim.y;
+  for (int k = blockIdx.x * nt + threadIdx.x + threadIdx.y * blockDim.x; k < npc;
+       k += gridDim.x * nt)
+    p[pc[k].off] = pw[pc[k].off];
 }
 
 // Lexicographic Gauss-Seidel SOR in one CTA, bit-identical to the reference
@@ -1447,6 +1680,33 @@ int black_pass_blocks(const Geom &g) {
   return n < 1 ? 1 : (int)n;
 }
 
+int edge_blocks(int n) {
+  int b = (n + 255) / 256;
+  if (b > kEdgeBlocksMax) b = kEdgeBlocksMax;
+  return b < 1 ? 1 : b;
+}
+
+// Kernel choices of the FAST red-black solve for a stop-rule setting.
+struct FastSolveKernels {
+  const void *red_graph, *red_eager, *edge;
+  int mean_free;
+};
+
+static FastSolveKernels fast_solve_kernels(int strict) {
+  const bool fluid = (strict & STOP_FLUID_NORM) != 0;
+  const bool mf = fluid && (strict & STOP_MEAN_FREE) != 0;
+  FastSolveKernels k;
+  k.mean_free = mf ? 1 : 0;
+  k.red_graph = mf ? (const void *)sor_red_res_kernel<true, true>
+                   : (const void *)sor_red_res_kernel<true, false>;
+  k.red_eager = mf ? (const void *)sor_red_res_kernel<false, true>
+                   : (const void *)sor_red_res_kernel<false, false>;
+  k.edge = !fluid ? (const void *)edge_res_kernel<false, false>
+           : mf   ? (const void *)edge_res_kernel<true, true>
+                  : (const void *)edge_res_kernel<true, false>;
+  return k;
+}
+
 // The sweep schedules: 0 is one launch per colour pass; the others are
 // temporal-blocking tile shapes, `sweeps` red-black sweeps per launch.
 struct TbShape {
@@ -1675,11 +1935,14 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
   if (r.arith) {
     // as in the solve: the black pass also sums the black fluid cells' residual
     const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
-    sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, 0);
+    // the red pass of the solve (its update formula), without its sums
     const int bb = black_pass_blocks(r.g);
+    const int nvb = (int)(sgrid.x * sgrid.y);
+    sor_red_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
+        d.p, d.pw, d.rhs, d.cls, r.g, r.c, d.st, d.partials_r, d.partials_b, bb, d.partials_e, 1,
+        (int)sgrid.x, nvb, r.itermax, r.strict_eps, 0, 0);
     sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.partials_b,
-                                                  mean_free, (int)sgrid.x,
-                                                  (int)(sgrid.x * sgrid.y));
+                                                  mean_free, (int)sgrid.x, nvb);
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
                                                            r.strict_eps, RES_NORM, d.partials_b,
@@ -1795,7 +2058,6 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
                (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
     const int nbb = (int)(sgrid.x * sgrid.y);
-    const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
     if (r.strict_eps & STOP_RELATIVE) {
       // the norm the solve starts from (relative stop rule)
       if (r.arith)
@@ -1809,19 +2071,55 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
                                                               r.itermax, r.strict_eps, RES_START,
                                                               nullptr, 0);
     }
+    if (r.arith) {
+      // fast arithmetic: the red pass of iteration k+1 finishes iteration k's
+      // norm (see sor_red_res_kernel); the same launches as the graph
+      const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
+      const int bb = black_pass_blocks(g);
+      const int nbe = edge_blocks(d.n_edge);
+      int gx = (int)sgrid.x;
+      unsigned int itermax = r.itermax;
+      int strict = r.strict_eps, mode = 0;
+      cudaGraphConditionalHandle h0 = 0;
+      double *p = d.p, *pw = d.pw, *prt_r = d.partials_r;
+      const double *rhs = d.rhs, *prt_b = d.partials_b, *prt_e = d.partials_e;
+      const uint8_t *cls = d.cls;
+      StepState *st = d.st;
+      Geom gg = g;
+      Consts cc = c;
+      int nbb_b = bb, nbe_e = nbe, nvb = nbb;
+      void *red_args[] = {&p, &pw, &rhs, &cls, &gg, &cc, &st, &prt_r, &prt_b, &nbb_b, &prt_e,
+                          &nbe_e, &gx, &nvb, &itermax, &strict, &mode, &h0};
+      if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
+      if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
+          cudaSuccess)
+        return e;
+      mode = 1;
+      const unsigned int *list = d.edge_list;
+      const uint8_t *flags = d.flags;
+      int n_edge = d.n_edge;
+      void *edge_args[] = {&p, &rhs, &flags, &list, &n_edge, &gg, &cc, &prt_e};
+      while (!done) {
+        sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
+                                                      fk.mean_free, gx, nbb);
+        if ((e = cudaLaunchKernel(fk.edge, dim3(nbe), kRedBlock, edge_args, 0, s)) !=
+            cudaSuccess)
+          return e;
+        if (d.n_pcopy > 0)
+          pcopy_save_kernel<<<(d.n_pcopy + 255) / 256, 256, 0, s>>>(d.p, d.pw, d.pcopy,
+                                                                    d.n_pcopy, g.pitch, d.st,
+                                                                    r.itermax);
+        if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
+            cudaSuccess)
+          return e;
+        if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
+      }
+      sor_rollback_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.pw, d.cls, d.pcopy, d.n_pcopy, g, d.st,
+                                                   r.itermax, gx, nbb);
+    }
     while (!done) {
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
-      if (r.arith) {
-        // fast arithmetic: the black pass also sums the black fluid cells' residual
-        sor_color_kernel<false><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, 0);
-        const int bb = black_pass_blocks(g);
-        sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
-                                                      mean_free, (int)sgrid.x, nbb);
-        residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
-                                                               ty_int, nt_int, 0, r.itermax,
-                                                               r.strict_eps, RES_SOLVE,
-                                                               d.partials_b, bb);
-      } else {
+      {
         for (int color = 0; color < 2; ++color)
           sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
         residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
@@ -2056,6 +2354,22 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                    ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_START,
                    (const double *)nullptr, 0);
     }
+    dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
+               (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
+    const int nbb = (int)(sgrid.x * sgrid.y);
+    const int bb = black_pass_blocks(g);
+    const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
+    if (r.arith) {
+      // fast arithmetic: first copy and red pass outside the loop; the red
+      // pass of iteration k+1 finishes iteration k's norm (sor_red_res_kernel)
+      if (d.n_pcopy > 0)
+        n = b.kernel(b.graph, n, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
+                     dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+      n = b.kernel(b.graph, n, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
+                   (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
+                   (const double *)d.partials_b, bb, (const double *)d.partials_e,
+                   edge_blocks(d.n_edge), (int)sgrid.x, nbb, r.itermax, r.strict_eps, 0, h);
+    }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
@@ -2067,30 +2381,29 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     if (b.err == cudaSuccess) {
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
-      if (d.n_pcopy > 0)
-        bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
-                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
-      dim3 sgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
-                 (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
-      const void *kc = r.arith ? (const void *)sor_color_kernel<false>
-                               : (const void *)sor_color_kernel<true>;
-      const void *kr = r.arith ? (const void *)residual_kernel<false, true>
-                               : (const void *)residual_kernel<true, true>;
-      const int nbb = (int)(sgrid.x * sgrid.y);
-      const int mean_free = (r.strict_eps & STOP_FLUID_NORM) && (r.strict_eps & STOP_MEAN_FREE);
       if (r.arith) {
-        // fast arithmetic: the black pass also sums the black fluid cells' residual
-        bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
-                      (const uint8_t *)d.flags, g, c, 0);
-        const int bb = black_pass_blocks(g);
-        bn = b.kernel(body, bn, (const void *)sor_black_res_kernel, dim3(bb), kRedBlock, d.p,
+        const int nbe = edge_blocks(d.n_edge);
+        bn = b.kernel(body, nullptr, (const void *)sor_black_res_kernel, dim3(bb), kRedBlock, d.p,
                       (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
-                      mean_free, (int)sgrid.x, nbb);
-        bn = b.kernel(body, bn, kr, dim3(nb), kRedBlock, (const double *)d.p,
-                      (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.st, d.partials,
-                      ty_int, nt_int, h, r.itermax, r.strict_eps, (int)RES_SOLVE,
-                      (const double *)d.partials_b, bb);
+                      fk.mean_free, (int)sgrid.x, nbb);
+        bn = b.kernel(body, bn, fk.edge, dim3(nbe), kRedBlock, (const double *)d.p,
+                      (const double *)d.rhs, (const uint8_t *)d.flags,
+                      (const unsigned int *)d.edge_list, d.n_edge, g, c, d.partials_e);
+        if (d.n_pcopy > 0)
+          bn = b.kernel(body, bn, (const void *)pcopy_save_kernel,
+                        dim3((d.n_pcopy + 255) / 256), dim3(256), d.p, d.pw,
+                        (const PCopy *)d.pcopy, d.n_pcopy, g.pitch, (const StepState *)d.st,
+                        r.itermax);
+        bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
+                      (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
+                      (const double *)d.partials_b, bb, (const double *)d.partials_e, nbe,
+                      (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
       } else {
+        if (d.n_pcopy > 0)
+          bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
+                        dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
+        const void *kc = (const void *)sor_color_kernel<true>;
+        const void *kr = (const void *)residual_kernel<true, true>;
         for (int color = 0; color < 2; ++color)
           bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
                         (const uint8_t *)d.flags, g, c, color);
@@ -2101,6 +2414,10 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       }
     }
     n = wnode;
+    if (r.arith)
+      n = b.kernel(b.graph, n, (const void *)sor_rollback_kernel, dim3(bb), kRedBlock, d.p,
+                   (const double *)d.pw, (const uint8_t *)d.cls, (const PCopy *)d.pcopy,
+                   d.n_pcopy, g, (const StepState *)d.st, r.itermax, (int)sgrid.x, nbb);
   }
   if (part != 1) {
     n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock,

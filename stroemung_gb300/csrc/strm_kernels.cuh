@@ -29,6 +29,15 @@ struct DevFields {
   int n_bc;
   PCopy *pcopy;
   int n_pcopy;
+  // FAST red-black solve: solver class per cell (0 fluid with fluid
+  // neighbours, 1 fluid next to a non-fluid cell, 2 other), the cells whose
+  // residual the edge pass sums (offsets, x-major), and the partial sums of
+  // the red pass and of the edge pass
+  uint8_t *cls;
+  unsigned int *edge_list;
+  int n_edge;
+  double *partials_r;
+  double *partials_e;
   long long *first_bad;   // classification: first thin-wall cell (x*ny+y)
   unsigned long long *fluid_count;
 };
@@ -65,6 +74,10 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
 // (the inner iteration of the mixed solve), by the configured schedule.
 cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_t s, int n);
 int num_sweep_schedules();
+// Blocks of the edge-list residual pass for n listed cells (at most
+// kEdgeBlocksMax).
+constexpr int kEdgeBlocksMax = 256;
+int edge_blocks(int n);
 
 // Colour map into a device RGBA8 image [ny][nx] (0 pressure, 1 speed).
 cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, void *rgba,
