@@ -3,10 +3,20 @@
 // Step graph (red-black solve):
 //   bc_kernel        cluster of 8 CTAs: step bookkeeping + compiled boundary program
 //   fg_rhs_kernel    tiled F, G (+ their boundary restore) and RHS, one pass
-//   WHILE(solve not done):
+//   fg_rhs32_kernel  the same with the stencil in FP32 (mixed precision)
+//   WHILE(solve not done), exact arithmetic:
 //     pcopy_kernel     boundary pressure copy
 //     sor_color_kernel red cells, then black cells
 //     residual_kernel  residual norm, stop test, sets the WHILE condition
+//   fast arithmetic: pcopy_kernel, sor_red_res_kernel (first red pass), then
+//   WHILE(solve not done):
+//     sor_black_res_kernel  black pass + the black cells' residual
+//     edge_res_kernel       residual of the cells next to boundary values
+//     pcopy_save_kernel     boundary copy of the next iteration (saved)
+//     sor_red_res_kernel    red pass of the next iteration + this one's red
+//                           residual, norm, stop test
+//   sor_rollback_kernel  undoes the next iteration's copy and red pass
+//   mixed precision: FP32 sweeps with FP64 refinement (see the mixed solve)
 //   prange_kernel    pressure range when the solve ran out of iterations
 //   velocity_kernel  velocity update + restore + max|u|,|v| + speed range + time
 //
@@ -351,6 +361,192 @@ __global__ void __launch_bounds__(FG_THREADS)
       rhs[OFF(x, y)] = xdiv(a + b, dt, s_rdt);
     }
   }
+}
+
+// F/G/RHS of the mixed-precision step: the tiles, boundary rules and
+// restore of fg_rhs_kernel with the advection-diffusion stencil in FP32.
+// Each u, v value of the tile is held as a pair of floats (hi = u rounded,
+// lo = u - hi rounded), about 48 significant bits.  The stencil takes first
+// and second differences of the hi parts first (exact for neighbouring
+// values) and adds those of the lo parts, and forms the convective
+// differences of products as (A - B) C + B (C - D), so that no FP32
+// operation cancels a large value: the FP32 rounding is relative to the
+// terms of the increment dt (lap/Re - d(u^2)/dx - d(uv)/dy), not to u.
+// F = u + increment is formed in FP64; boundary values (F = u, G = v) are
+// exact copies; the RHS takes FP64 differences of F and G (reciprocal
+// multiplications).  The terms are the reference's (src/math.rs:19-174),
+// rearranged.
+struct Consts32F {
+  float gamma, r_dx2, r_dy2, r_four_dx, r_four_dy, r_re;
+};
+
+struct HL {
+  float h, l;
+};
+
+__device__ __forceinline__ HL hl_of(double x) {
+  HL r;
+  r.h = __double2float_rn(x);
+  r.l = __double2float_rn(x - (double)r.h);
+  return r;
+}
+// a - b
+__device__ __forceinline__ float hl_dif(HL a, HL b) { return (a.h - b.h) + (a.l - b.l); }
+// a + b
+__device__ __forceinline__ float hl_sum(HL a, HL b) { return (a.h + b.h) + (a.l + b.l); }
+// e - 2c + w
+__device__ __forceinline__ float hl_d2(HL e, HL c, HL w) {
+  return ((e.h - c.h) - (c.h - w.h)) + ((e.l - c.l) - (c.l - w.l));
+}
+
+// d(u^2)/dx (src/math.rs:19-33): a^2 - b^2 as (a - b)(a + b), a - b = u(i+1) - u(i-1)
+__device__ __forceinline__ float f_du2dx(HL um1, HL u, HL up1, const Consts32F &k) {
+  const float a = hl_sum(u, up1), b = hl_sum(um1, u);
+  return (hl_dif(up1, um1) * (a + b) +
+          k.gamma * (fabsf(a) * hl_dif(u, up1) - fabsf(b) * hl_dif(um1, u))) *
+         k.r_four_dx;
+}
+
+// d(v^2)/dy (src/math.rs:136-150)
+__device__ __forceinline__ float f_dv2dy(HL vm1, HL v, HL vp1, const Consts32F &k) {
+  const float a = hl_sum(v, vp1), b = hl_sum(vm1, v);
+  return (hl_dif(vp1, vm1) * (a + b) +
+          k.gamma * (fabsf(a) * hl_dif(v, vp1) - fabsf(b) * hl_dif(vm1, v))) *
+         k.r_four_dy;
+}
+
+// d(uv)/dy (src/math.rs:97-120): A C - B D as (A - B) C + B (C - D)
+__device__ __forceinline__ float f_duvdy(HL u_ij, HL u_ijm1, HL u_ijp1, HL v_ij, HL v_ijm1,
+                                         HL v_ip1j, HL v_ip1jm1, const Consts32F &k) {
+  const float A = hl_sum(v_ij, v_ip1j), B = hl_sum(v_ijm1, v_ip1jm1);
+  const float C = hl_sum(u_ij, u_ijp1);
+  const float AmB = hl_dif(v_ij, v_ijm1) + hl_dif(v_ip1j, v_ip1jm1);
+  const float CmD = hl_dif(u_ijp1, u_ijm1);
+  return (AmB * C + B * CmD +
+          k.gamma * (fabsf(A) * hl_dif(u_ij, u_ijp1) - fabsf(B) * hl_dif(u_ijm1, u_ij))) *
+         k.r_four_dy;
+}
+
+// d(uv)/dx (src/math.rs:53-77)
+__device__ __forceinline__ float f_duvdx(HL u_ij, HL u_ijp1, HL u_im1j, HL u_im1jp1, HL v_ij,
+                                         HL v_ip1j, HL v_im1j, const Consts32F &k) {
+  const float A = hl_sum(u_ij, u_ijp1), B = hl_sum(u_im1j, u_im1jp1);
+  const float C = hl_sum(v_ij, v_ip1j);
+  const float AmB = hl_dif(u_ij, u_im1j) + hl_dif(u_ijp1, u_im1jp1);
+  const float CmD = hl_dif(v_ip1j, v_im1j);
+  return (AmB * C + B * CmD +
+          k.gamma * (fabsf(A) * hl_dif(v_ij, v_ip1j) - fabsf(B) * hl_dif(v_im1j, v_ij))) *
+         k.r_four_dx;
+}
+
+// laplacian (src/math.rs:162-174)
+__device__ __forceinline__ float f_laplacian(HL e, HL e_jm1, HL e_jp1, HL e_im1, HL e_ip1,
+                                             const Consts32F &k) {
+  return hl_d2(e_ip1, e, e_im1) * k.r_dx2 + hl_d2(e_jp1, e, e_jm1) * k.r_dy2;
+}
+
+__global__ void __launch_bounds__(FG_THREADS)
+    fg_rhs32_kernel(const double *__restrict__ u, const double *__restrict__ v, double *f,
+                    double *gg, double *__restrict__ rhs, const uint8_t *__restrict__ flags,
+                    Geom g, Consts c, Consts32F k, const StepState *st) {
+  __shared__ HL su[FG_TX + 3][FG_TY + 3];
+  __shared__ HL sv[FG_TX + 3][FG_TY + 3];
+  __shared__ double sF[FG_TX + 1][FG_TY + 1];
+  __shared__ double sG[FG_TX + 1][FG_TY + 1];
+  __shared__ uint8_t sfl[FG_TX + 2][FG_TY + 2];
+
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * FG_TY;
+  const int x0 = blockIdx.y * FG_TX;
+  const double dt = st->dt;
+  const double rdt = 1.0 / dt;
+  const float dt32 = (float)dt;
+  const HL zero = {0.f, 0.f};
+  for (int q = tid; q < (FG_TX + 3) * (FG_TY + 3); q += FG_THREADS) {
+    const int i = q / (FG_TY + 3), j = q % (FG_TY + 3);
+    const int x = x0 - 2 + i, y = y0 - 2 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    su[i][j] = in ? hl_of(u[OFF(x, y)]) : zero;
+    sv[i][j] = in ? hl_of(v[OFF(x, y)]) : zero;
+  }
+  for (int q = tid; q < (FG_TX + 2) * (FG_TY + 2); q += FG_THREADS) {
+    const int i = q / (FG_TY + 2), j = q % (FG_TY + 2);
+    const int x = x0 - 1 + i, y = y0 - 1 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    sfl[i][j] = in ? flags[OFF(x, y)] : (uint8_t)0;
+  }
+  __syncthreads();
+
+  for (int q = tid; q < (FG_TX + 1) * (FG_TY + 1); q += FG_THREADS) {
+    const int i = q / (FG_TY + 1), j = q % (FG_TY + 1);
+    const int x = x0 - 1 + i, y = y0 - 1 + j;
+    double Fv = 0.0, Gv = 0.0;
+    if (x >= 0 && y >= 0 && x < g.nx && y < g.ny) {
+      const size_t o = OFF(x, y);
+      const uint8_t fc = sfl[i][j];
+      const bool bc = is_bnd(fc);
+      const bool keepF = bc || (x + 1 < g.nx && is_bnd(sfl[i + 1][j]));
+      const bool keepG = bc || (y + 1 < g.ny && is_bnd(sfl[i][j + 1]));
+      const bool interior = x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+      const int si = i + 1, sj = j + 1;
+      if (keepF) {
+        Fv = u[o];
+      } else if (interior) {
+        const HL u01 = su[si - 1][sj], u10 = su[si][sj - 1], u11 = su[si][sj];
+        const HL u12 = su[si][sj + 1], u21 = su[si + 1][sj];
+        const HL v10 = sv[si][sj - 1], v11 = sv[si][sj], v20 = sv[si + 1][sj - 1];
+        const HL v21 = sv[si + 1][sj];
+        const float inc = dt32 * (f_laplacian(u11, u10, u12, u01, u21, k) * k.r_re -
+                                  f_du2dx(u01, u11, u21, k) -
+                                  f_duvdy(u11, u10, u12, v11, v10, v21, v20, k));
+        Fv = u[o] + (double)inc;
+      } else {
+        Fv = f[o];
+      }
+      if (keepG) {
+        Gv = v[o];
+      } else if (interior) {
+        const HL u01 = su[si - 1][sj], u02 = su[si - 1][sj + 1], u11 = su[si][sj];
+        const HL u12 = su[si][sj + 1];
+        const HL v01 = sv[si - 1][sj], v10 = sv[si][sj - 1], v11 = sv[si][sj];
+        const HL v12 = sv[si][sj + 1], v21 = sv[si + 1][sj];
+        const float inc = dt32 * (f_laplacian(v11, v10, v12, v01, v21, k) * k.r_re -
+                                  f_duvdx(u11, u12, u01, u02, v11, v21, v01, k) -
+                                  f_dv2dy(v10, v11, v12, k));
+        Gv = v[o] + (double)inc;
+      } else {
+        Gv = gg[o];
+      }
+      if (i >= 1 && j >= 1) {
+        if (keepF || interior) f[o] = Fv;
+        if (keepG || interior) gg[o] = Gv;
+      }
+    }
+    sF[i][j] = Fv;
+    sG[i][j] = Gv;
+  }
+  __syncthreads();
+
+  for (int q = tid; q < FG_TX * FG_TY; q += FG_THREADS) {
+    const int i = q / FG_TY, j = q % FG_TY;
+    const int x = x0 + i, y = y0 + j;
+    if (x >= 1 && y >= 1 && x < g.nx && y < g.ny) {
+      const double a = sF[i + 1][j + 1] - sF[i][j + 1];
+      const double b = sG[i + 1][j + 1] - sG[i + 1][j];
+      rhs[OFF(x, y)] = fma(a, c.r_dx, b * c.r_dy) * rdt;
+    }
+  }
+}
+
+static Consts32F consts32f_of(const Consts &c) {
+  Consts32F k;
+  k.gamma = (float)c.gamma;
+  k.r_dx2 = (float)c.r_dx2;
+  k.r_dy2 = (float)c.r_dy2;
+  k.r_four_dx = (float)c.r_four_dx;
+  k.r_four_dy = (float)c.r_four_dy;
+  k.r_re = (float)c.r_re;
+  return k;
 }
 
 // ------------------------------------------------------------------------
@@ -1840,7 +2036,11 @@ cudaError_t launch_bc(const DevFields &d, cudaStream_t s) {
 
 cudaError_t launch_fg_rhs(const DevFields &d, const RunCfg &r, cudaStream_t s) {
   dim3 grd((r.g.ny + FG_TY - 1) / FG_TY, (r.g.nx + FG_TX - 1) / FG_TX);
-  fg_rhs_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c, d.st);
+  if (r.precision == 1)
+    fg_rhs32_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c,
+                                               consts32f_of(r.c), d.st);
+  else
+    fg_rhs_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c, d.st);
   return cudaGetLastError();
 }
 
@@ -2213,9 +2413,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                  d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc, d.bc_val, d.n_bc, d.st, c, r.tau,
                  r.delt, r.itermax, 1);
     dim3 fg_grid((g.ny + FG_TY - 1) / FG_TY, (g.nx + FG_TX - 1) / FG_TX);
-    n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
-                 (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
-                 (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
+    if (r.precision == 1)
+      n = b.kernel(b.graph, n, (const void *)fg_rhs32_kernel, fg_grid, dim3(FG_THREADS),
+                   (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
+                   (const uint8_t *)d.flags, g, c, consts32f_of(c), (const StepState *)d.st);
+    else
+      n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
+                   (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
+                   (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
   }
   if (part == 1 || part == 3) {
     // the first half of a step ends after the RHS; part 3 is the second
