@@ -608,6 +608,8 @@ def batched_block(args):
     batch.close()
     for s in sims:
         s.close()
+    learned = guarded_value(lambda: batched_learned(args, specs, cfg, best, st, t_batch)) \
+        if args.batch_learned else None
     # the same instances one after another on the plain FP64 path (a sample,
     # scaled by cells)
     sample = list(range(0, len(specs), max(1, len(specs) // args.batch_seq_sample)))
@@ -635,7 +637,72 @@ def batched_block(args):
         "sor_iterations_mean": float(np.mean(st["sor_iterations"])),
         "solver": "mixed precision (FP32 sweeps, FP64 norm/refinement), reference stop rule, "
                   "eps 1e-3, max_iterations 2000; one graph per step",
+        "learned": learned,
     }
+
+
+def guarded_value(fn):
+    try:
+        return fn()
+    except Exception as exc:  # reported in the JSON line, not fatal
+        return {"error": f"{type(exc).__name__}: {exc}"}
+
+
+def batched_learned(args, specs, cfg, sched, st_plain, t_plain):
+    """The same members with the learned warm start: a U-Net trained here on
+    channel snapshots against their solved pressures (error loss), each
+    member's prediction judged after 16 red-black iterations between the
+    batch's halves; stepped from the state the plain batch's timed steps
+    started from, so sweeps compare step by step."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import warmstart
+    from stroemung_gb300.batch import Batch
+    from stroemung_gb300.simulation import PREC_MIXED, Simulation
+    from stroemung_gb300.unet import UNet
+    t0 = time.perf_counter()
+    train = warmstart.generate_snapshots(args.batch_ws_snapshots, imax=512, jmax=128, dx=0.01,
+                                         steps_per_problem=16, seed=11, targets=True)
+    net = UNet(seed=0)
+    tr = warmstart.Trainer(net, 514, 130, 0.01, 0.01, batch=32, loss="error")
+    hist = tr.fit(train, epochs=args.batch_ws_epochs, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del train
+    sims = [Simulation(grid=g, reynolds=re, precision=PREC_MIXED, inner_sweeps=16, **cfg)
+            for g, re, _ in specs]
+    batch = Batch(sims)
+    batch.set_schedule(sched)
+    batch.step(1)
+    bws = warmstart.BatchWarmStart(batch, net, judge_sweeps=args.ws_judge_sweeps)
+    sweeps, acc = [], 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    t_pj = 0.0
+    for _ in range(args.batch_steps):
+        rec = bws.step()
+        sweeps.append(rec["sor_iterations"].astype(np.int64))
+        acc += sum(bws.last["accepted"])
+        t_pj += bws.last["predict_judge_s"]
+    torch.cuda.synchronize()
+    t_learned = (time.perf_counter() - t0) / args.batch_steps
+    batch.close()
+    for s in sims:
+        s.close()
+    plain = int(st_plain["sor_iterations"].astype(np.int64).sum())
+    learned = int(np.sum(sweeps))
+    return {"training": {"snapshots": args.batch_ws_snapshots, "grid": "512x128",
+                         "epochs": args.batch_ws_epochs, "loss": "error",
+                         "loss_first_last": [float(np.mean(hist[:8])),
+                                             float(np.mean(hist[-8:]))],
+                         "generate_and_train_s": t_train},
+            "judge_sweeps": args.ws_judge_sweeps,
+            "accepted": f"{acc}/{len(specs) * args.batch_steps}",
+            "sweeps_plain": plain, "sweeps_learned": learned,
+            "sweeps_saved": 1 - learned / plain,
+            "ms_per_batch_step": t_learned * 1e3,
+            "predict_and_judge_ms_per_batch_step": t_pj / args.batch_steps * 1e3,
+            "time_vs_plain_batch": t_learned / t_plain}
 
 
 def profile_target(what: str, steps: int) -> None:
@@ -704,6 +771,10 @@ def main():
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-seq-sample", type=int, default=16)
+    ap.add_argument("--batch-learned", type=int, default=1,
+                    help="also step the batch with the learned warm start")
+    ap.add_argument("--batch-ws-snapshots", type=int, default=512)
+    ap.add_argument("--batch-ws-epochs", type=int, default=20)
     ap.add_argument("--profile", default="", choices=["", "fp64", "mixed", "sweeps", "conv"],
                     help="run a small workload for ncu instead of the benchmark")
     args = ap.parse_args()

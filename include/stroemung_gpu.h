@@ -292,6 +292,14 @@ int strm_batch_destroy(strm_batch *batch);
 /* n steps of every member, one host synchronisation; stats (may be NULL)
  * receives n entries per member, member-major. */
 int strm_batch_step(strm_batch *batch, int n, strm_step_stats *stats);
+/* One batch step in two halves, as strm_tick_prepare / strm_tick_solve for a
+ * single simulation: prepare runs every member's boundary pass, time step,
+ * F/G and RHS; between the halves the members' pressures may be changed
+ * (strm_judge_correction, strm_upload); solve runs the pressure solves and
+ * the second halves, and stats (may be NULL) receives one entry per member.
+ * prepare followed by solve gives exactly the fields of strm_batch_step. */
+int strm_batch_prepare(strm_batch *batch);
+int strm_batch_solve(strm_batch *batch, strm_step_stats *stats);
 /* Blocked sweep schedule of the batch (2..STRM_SWEEPS_COUNT-1). */
 int strm_batch_set_schedule(strm_batch *batch, int schedule);
 /* Times `reps` whole batch steps under each blocked schedule (members'

@@ -109,6 +109,8 @@ SIGNATURES = {
                           ctypes.POINTER(ctypes.c_void_p)],
     "strm_batch_destroy": [_vp],
     "strm_batch_step": [_vp, ctypes.c_int, _vp],
+    "strm_batch_prepare": [_vp],
+    "strm_batch_solve": [_vp, _vp],
     "strm_batch_set_schedule": [_vp, ctypes.c_int],
     "strm_batch_autotune": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
     "strm_apply_correction": [_vp, _vp, ctypes.c_double],

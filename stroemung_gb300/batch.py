@@ -36,6 +36,26 @@ class Batch:
                 out[k, i] = (s.sor_iterations, s.norm_squared, s.delt, s.converged)
         return out
 
+    def prepare(self) -> None:
+        """First half of a batch step: every member's boundary pass, time
+        step, F/G and RHS (the members' pressures may be changed before
+        solve)."""
+        _lib.check(_lib.load().strm_batch_prepare(self._h))
+
+    def solve(self) -> np.ndarray:
+        """Second half: the pressure solves and velocity updates; returns
+        one record per member (as step(1)[:, 0])."""
+        m = len(self.sims)
+        buf = (_lib.StepStats * m)()
+        _lib.check(_lib.load().strm_batch_solve(self._h, ctypes.cast(buf, ctypes.c_void_p)))
+        dt = np.dtype([("sor_iterations", np.uint32), ("norm_squared", np.float64),
+                       ("delt", np.float64), ("converged", np.uint32)])
+        out = np.zeros(m, dt)
+        for k in range(m):
+            s = buf[k]
+            out[k] = (s.sor_iterations, s.norm_squared, s.delt, s.converged)
+        return out
+
     def set_schedule(self, schedule: int) -> None:
         _lib.check(_lib.load().strm_batch_set_schedule(self._h, int(schedule)))
 

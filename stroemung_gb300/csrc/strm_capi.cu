@@ -784,13 +784,21 @@ struct strm_batch {
   int inner = 16;
   BatchPlan plan{};
   cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec_pre = nullptr, exec_solve = nullptr;
 };
 
 namespace {
 
+void batch_destroy_execs(strm_batch *b) {
+  cudaGraphExec_t *ex[3] = {&b->exec, &b->exec_pre, &b->exec_solve};
+  for (cudaGraphExec_t *e : ex) {
+    if (*e) cudaGraphExecDestroy(*e);
+    *e = nullptr;
+  }
+}
+
 int batch_rebuild(strm_batch *b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  b->exec = nullptr;
+  batch_destroy_execs(b);
   free_batch(&b->plan);
   std::vector<BatchMember> mem;
   for (strm_sim *s : b->sims) mem.push_back(BatchMember{s->d, s->cfg});
@@ -799,6 +807,50 @@ int batch_rebuild(strm_batch *b) {
     return fail(STRM_ERR_INVALID, "a batch member has max_iterations below the inner sweeps");
   CK(e);
   CK(cudaGraphInstantiate(&b->exec, b->plan.graph, 0));
+  CK(cudaGraphInstantiate(&b->exec_pre, b->plan.graph_pre, 0));
+  CK(cudaGraphInstantiate(&b->exec_solve, b->plan.graph_solve, 0));
+  return STRM_OK;
+}
+
+// Copies each member's state and the last n log entries to the host and
+// fills stats[member * n + i].
+int batch_collect(strm_batch *b, int n, strm_step_stats *stats) {
+  unsigned int overrun = 0;
+  CK(cudaMemcpyAsync(&overrun, (char *)b->plan.state + kBatchOverrunOffset, sizeof overrun,
+                     cudaMemcpyDeviceToHost, b->stream));
+  const int ns = (int)b->sims.size();
+  for (int k = 0; k < ns; ++k) {
+    strm_sim *s = b->sims[k];
+    CK(cudaMemcpyAsync(s->h_st, s->d.st, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    if (stats && n > 0)
+      CK(cudaMemcpyAsync(s->h_log, s->d.log, sizeof(StepLog) * n, cudaMemcpyDeviceToHost,
+                         b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (stats)
+      for (int i = 0; i < n; ++i) {
+        strm_step_stats &o = stats[(size_t)k * n + i];
+        o.sor_iterations = s->h_log[i].sor_iters;
+        o.converged = s->h_log[i].converged;
+        o.norm_squared = s->h_log[i].ns;
+        o.delt = s->h_log[i].dt;
+      }
+  }
+  if (overrun) return fail(STRM_ERR_TIMEOUT, "batch pressure loop passed its bound");
+  for (strm_sim *s : b->sims)
+    if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return STRM_OK;
+}
+
+// Orders the batch stream after the members' own streams and resets their
+// step logs and the loop-overrun flag.
+int batch_begin(strm_batch *b) {
+  const unsigned int zero = 0;
+  for (strm_sim *s : b->sims) {
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  }
+  CK(cudaMemsetAsync((char *)b->plan.state + kBatchOverrunOffset, 0, sizeof(unsigned int),
+                     b->stream));
   return STRM_OK;
 }
 
@@ -840,7 +892,7 @@ int strm_batch_destroy(strm_batch *b) {
   if (!b) return STRM_OK;
   cudaSetDevice(b->dev);
   if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
+  batch_destroy_execs(b);
   free_batch(&b->plan);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -861,39 +913,30 @@ int strm_batch_step(strm_batch *b, int n, strm_step_stats *stats) {
   if (!b || n < 0) return fail(STRM_ERR_INVALID, "invalid arguments");
   if (n > kLogCap) return fail(STRM_ERR_INVALID, "at most %d steps per call", kLogCap);
   CK(cudaSetDevice(b->dev));
-  const unsigned int zero = 0;
   // the members' own streams may hold work (uploads, edits): order after it
-  for (strm_sim *s : b->sims) {
-    CK(cudaStreamSynchronize(s->stream));
-    CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
-  }
-  CK(cudaMemsetAsync((char *)b->plan.state + kBatchOverrunOffset, 0, sizeof(unsigned int),
-                     b->stream));
+  int rc = batch_begin(b);
+  if (rc) return rc;
   for (int i = 0; i < n; ++i) CK(cudaGraphLaunch(b->exec, b->stream));
-  unsigned int overrun = 0;
-  CK(cudaMemcpyAsync(&overrun, (char *)b->plan.state + kBatchOverrunOffset, sizeof overrun,
-                     cudaMemcpyDeviceToHost, b->stream));
-  const int ns = (int)b->sims.size();
-  for (int k = 0; k < ns; ++k) {
-    strm_sim *s = b->sims[k];
-    CK(cudaMemcpyAsync(s->h_st, s->d.st, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
-    if (stats && n > 0)
-      CK(cudaMemcpyAsync(s->h_log, s->d.log, sizeof(StepLog) * n, cudaMemcpyDeviceToHost,
-                         b->stream));
-    CK(cudaStreamSynchronize(b->stream));
-    if (stats)
-      for (int i = 0; i < n; ++i) {
-        strm_step_stats &o = stats[(size_t)k * n + i];
-        o.sor_iterations = s->h_log[i].sor_iters;
-        o.converged = s->h_log[i].converged;
-        o.norm_squared = s->h_log[i].ns;
-        o.delt = s->h_log[i].dt;
-      }
-  }
-  if (overrun) return fail(STRM_ERR_TIMEOUT, "batch pressure loop passed its bound");
-  for (strm_sim *s : b->sims)
-    if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
+  return batch_collect(b, n, stats);
+}
+
+int strm_batch_prepare(strm_batch *b) {
+  if (!b) return fail(STRM_ERR_INVALID, "batch is NULL");
+  CK(cudaSetDevice(b->dev));
+  int rc = batch_begin(b);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(b->exec_pre, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
   return STRM_OK;
+}
+
+int strm_batch_solve(strm_batch *b, strm_step_stats *stats) {
+  if (!b) return fail(STRM_ERR_INVALID, "batch is NULL");
+  CK(cudaSetDevice(b->dev));
+  // work queued on the members' streams between the halves (corrections)
+  for (strm_sim *s : b->sims) CK(cudaStreamSynchronize(s->stream));
+  CK(cudaGraphLaunch(b->exec_solve, b->stream));
+  return batch_collect(b, 1, stats);
 }
 
 int strm_batch_autotune(strm_batch *b, int reps, int *best, double *ms_per_step) {

@@ -2842,8 +2842,12 @@ static const void *batch_tb_fn(int sched) {
 
 void free_batch(BatchPlan *bp) {
   if (bp->graph) cudaGraphDestroy(bp->graph);
+  if (bp->graph_pre) cudaGraphDestroy(bp->graph_pre);
+  if (bp->graph_solve) cudaGraphDestroy(bp->graph_solve);
   if (bp->dev) cudaFree(bp->dev);
   bp->graph = nullptr;
+  bp->graph_pre = nullptr;
+  bp->graph_solve = nullptr;
   bp->dev = nullptr;
   bp->state = nullptr;
 }
@@ -2931,15 +2935,16 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     return e;
   }
 
+  // part 0: the whole step; 1: the members' first halves (boundary pass,
+  // F/G, RHS); 2: the pressure solves and the second halves
+  auto assemble = [&](int part, cudaGraph_t *out) -> cudaError_t {
   GraphBuilder b;
-  if ((e = cudaGraphCreate(&b.graph, 0)) != cudaSuccess) {
-    free_batch(bp);
-    return e;
-  }
+  cudaError_t e2 = cudaGraphCreate(&b.graph, 0);
+  if (e2 != cudaSuccess) return e2;
   b.store.reserve(64);
   // per-instance first halves, in parallel
   std::vector<cudaGraphNode_t> pre(n, nullptr);
-  for (int i = 0; i < n && b.err == cudaSuccess; ++i) {
+  for (int i = 0; i < n && b.err == cudaSuccess && part != 2; ++i) {
     cudaGraph_t child = nullptr;
     b.err = build_step_graph(mem[i].d, mem[i].r, &child, 1);
     if (b.err == cudaSuccess) {
@@ -2947,9 +2952,18 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
       cudaGraphDestroy(child);
     }
   }
+  if (part == 1) {
+    if (b.err != cudaSuccess) {
+      cudaGraphDestroy(b.graph);
+      return b.err;
+    }
+    *out = b.graph;
+    return cudaSuccess;
+  }
   cudaGraphNode_t nd = nullptr;
   if (b.err == cudaSuccess)
-    b.err = cudaGraphAddEmptyNode(&nd, b.graph, pre.data(), (size_t)n);
+    b.err = cudaGraphAddEmptyNode(&nd, b.graph, part == 2 ? nullptr : pre.data(),
+                                  part == 2 ? 0 : (size_t)n);
   const int nres = (int)t_res.size(), nref = (int)t_ref.size(), ndel = (int)t_del.size();
   const int ntb = (int)t_tb.size();
   cudaGraphConditionalHandle h{};
@@ -3059,11 +3073,16 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   }
   if (b.err != cudaSuccess) {
     cudaGraphDestroy(b.graph);
-    free_batch(bp);
     return b.err;
   }
-  bp->graph = b.graph;
+  *out = b.graph;
   return cudaSuccess;
+  };
+  e = assemble(0, &bp->graph);
+  if (e == cudaSuccess) e = assemble(1, &bp->graph_pre);
+  if (e == cudaSuccess) e = assemble(2, &bp->graph_solve);
+  if (e != cudaSuccess) free_batch(bp);
+  return e;
 }
 
 cudaError_t batch_sweeps(const std::vector<BatchMember> &mem, int sched, int m,

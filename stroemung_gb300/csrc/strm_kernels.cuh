@@ -122,7 +122,9 @@ struct BatchState;
 struct BatchPlan {
   void *dev = nullptr;          // device tables (one allocation)
   BatchState *state = nullptr;  // in dev: loop counters and the overrun flag
-  cudaGraph_t graph = nullptr;
+  cudaGraph_t graph = nullptr;        // the whole step
+  cudaGraph_t graph_pre = nullptr;    // the members' boundary pass, F/G, RHS
+  cudaGraph_t graph_solve = nullptr;  // the pressure solves and the second halves
 };
 // sched: internal blocked schedule (1..num_sweep_schedules()-1); m: sweeps
 // per refinement (every member needs max_iterations >= m).

@@ -339,11 +339,15 @@ __global__ void assemble_input(const float *rhs, const uint8_t *flags, const flo
 }
 
 // Per-sample mean of p_prev over fluid cells (sum and count by atomics).
-__global__ void sample_mean(const float *p, const uint8_t *flags, float *sum, float *cnt,
-                            int plane) {
+// Sum and count of p over each sample's non-boundary cells, one block per
+// sample with a fixed reduction order, so the network input (and with it
+// the prediction) is the same bits run after run.
+__global__ void __launch_bounds__(1024)
+    sample_mean(const float *p, const uint8_t *flags, float *sum, float *cnt, int plane) {
+  __shared__ float ss[32], sc[32];
   const int b = blockIdx.y;
   float s = 0.0f, c = 0.0f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x)
+  for (int i = threadIdx.x; i < plane; i += blockDim.x)
     if (!is_bnd(flags[(size_t)b * plane + i])) {
       s += p[(size_t)b * plane + i];
       c += 1.0f;
@@ -352,9 +356,23 @@ __global__ void sample_mean(const float *p, const uint8_t *flags, float *sum, fl
     s += __shfl_xor_sync(0xffffffffu, s, o);
     c += __shfl_xor_sync(0xffffffffu, c, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(sum + b, s);
-    atomicAdd(cnt + b, c);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    ss[w] = s;
+    sc[w] = c;
+  }
+  __syncthreads();
+  if (w == 0) {
+    s = lane < nw ? ss[lane] : 0.0f;
+    c = lane < nw ? sc[lane] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) {
+      sum[b] = s;
+      cnt[b] = c;
+    }
   }
 }
 
@@ -721,7 +739,7 @@ int strm_nn_prepare_input(const float *rhs, const uint8_t *flags, const float *p
     return STRM_NN_ERR_CUDA;
   dim3 g2((plane + 255) / 256 < 64 ? (plane + 255) / 256 : 64, batch);
   sample_absmax<<<g2, 256, 0, s>>>(rhs, flags, smax, plane);
-  sample_mean<<<g2, 256, 0, s>>>(pprev, flags, work2, work2 + batch, plane);
+  sample_mean<<<dim3(1, batch), 1024, 0, s>>>(pprev, flags, work2, work2 + batch, plane);
   mean_div<<<(batch + 255) / 256, 256, 0, s>>>(work2, work2 + batch, pmean, batch);
   assemble_input<<<grid_for((long long)batch * (nx - 2) * (ny - 2)), 256, 0, s>>>(
       rhs, flags, pprev, smax, pmean, dx2, (bf16 *)xin, batch, nx, ny);

@@ -175,16 +175,51 @@ class UNet:
         self._bufs[key] = B
         return B
 
+    def _forward_buffers(self, b, h, w):
+        """The forward pass's buffers as views of one shared, zero-filled pool
+        (no gradients): for predictions over many grid shapes, which would
+        otherwise each keep a full set.  Valid until the next such call."""
+        import torch
+        if h % 8 or w % 8:
+            raise ValueError("the network needs sizes divisible by 8")
+        c0, c1, c2, c3 = CHANNELS
+        spec = [("a0", h, w, c0), ("cat0", h, w, c1 + c0), ("p0", h // 2, w // 2, c0),
+                ("a1", h // 2, w // 2, c1), ("cat1", h // 2, w // 2, c2 + c1),
+                ("p1", h // 4, w // 4, c1), ("a2", h // 4, w // 4, c2),
+                ("cat2", h // 4, w // 4, c3 + c2), ("p2", h // 8, w // 8, c2),
+                ("b1", h // 8, w // 8, c3), ("b2", h // 8, w // 8, c3),
+                ("d2a", h // 4, w // 4, c2), ("d2", h // 4, w // 4, c2),
+                ("d1a", h // 2, w // 2, c1), ("d1", h // 2, w // 2, c1),
+                ("d0a", h, w, c0), ("d0", h, w, c0)]
+        offs, total = [], 0
+        for _, hh, ww, c in spec:
+            offs.append(total)
+            total += (2 * b * hh * ww * c + 255) // 256 * 256
+        q_off = total
+        total += 4 * b * h * w
+        pool = getattr(self, "_pool", None)
+        if pool is None or pool.numel() < total:
+            pool = self._pool = torch.empty(total, dtype=torch.uint8, device=self.device)
+        pool[:total].zero_()
+        B = {}
+        for (name, hh, ww, c), o in zip(spec, offs):
+            n = 2 * b * hh * ww * c
+            B[name] = pool[o:o + n].view(torch.bfloat16).view(b, hh, ww, c)
+        B["q"] = pool[q_off:q_off + 4 * b * h * w].view(torch.float32).view(b, h, w)
+        return B
+
     # ---- forward ---------------------------------------------------------------
     def _conv(self, layer, x, cs_in, y, cs_out, b, h, w, relu=1):
         self._check(self.L.strm_nn_conv3x3(
             x, cs_in, layer.cin_p, self._wbf(layer), layer.kp, self._ptr(layer.b), y,
             None, cs_out, layer.cout, b, h, w, relu, None), "conv3x3")
 
-    def forward(self, xin, b, h, w):
+    def forward(self, xin, b, h, w, keep: bool = True):
         """xin: BF16 [b][h][w][8] device tensor (see strm_nn_prepare_input).
-        Returns the FP32 correction q [b][h][w]."""
-        B = self._buffers(b, h, w)
+        Returns the FP32 correction q [b][h][w].  keep=False (prediction
+        only, no backward to follow) runs in the shared forward pool: q is
+        then valid until the next such call."""
+        B = self._buffers(b, h, w) if keep else self._forward_buffers(b, h, w)
         B["x_in_ptr"] = xin.data_ptr()
         L = self.L
         c0, c1, c2, c3 = CHANNELS

@@ -265,7 +265,7 @@ class WarmStartSolver:
                                                 tr.pmean.data_ptr(), tr.work2.data_ptr(),
                                                 tr.dx2, tr.xin.data_ptr(), 1, tr.nx, tr.ny,
                                                 None), "prepare")
-        q = self.net.forward(tr.xin, 1, tr.nx - 2, tr.ny - 2)
+        q = self.net.forward(tr.xin, 1, tr.nx - 2, tr.ny - 2, keep=False)
         torch.cuda.synchronize()
         return q, float(tr.smax[0].item()) * tr.dx2
 
@@ -302,6 +302,36 @@ class WarmStartSolver:
                      "predict_s": t1 - t0, "judge_s": t2 - t1,
                      "solve_s": time.perf_counter() - t2}
         return it, ns
+
+
+class BatchWarmStart:
+    """The learned warm start for a Batch: between the batch's two halves
+    every member's pressure is predicted and judged as WarmStartSolver does
+    for one simulation; then the members' pressure solves run together in
+    the batch's WHILE loop.  Each member ends exactly where its own
+    WarmStartSolver steps would end."""
+
+    def __init__(self, batch, net: UNet, judge_sweeps: int = 16):
+        self.batch = batch
+        self.members = [WarmStartSolver(s, net, judge_sweeps) for s in batch.sims]
+        self.last = {}
+
+    def step(self):
+        """One batch step; returns the per-member records of Batch.solve and
+        keeps the accepted flags and the predictor/judge time in self.last."""
+        import torch
+        self.batch.prepare()
+        t0 = time.perf_counter()
+        accepted = []
+        for w in self.members:
+            q, scale = w.predict()
+            accepted.append(w.judge(q, scale)[0])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        out = self.batch.solve()
+        self.last = {"accepted": accepted, "predict_judge_s": t1 - t0,
+                     "solve_s": time.perf_counter() - t1}
+        return out
 
 
 def sync_state(dst, src, scratch):

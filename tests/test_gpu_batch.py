@@ -104,3 +104,73 @@ def test_batch_rejects_unsuitable_members():
         Batch([short])
     fp64.close()
     short.close()
+
+
+def test_batch_halves_equal_batch_steps():
+    """prepare + solve, three times, gives the fields and records of
+    step(3)."""
+    members = _members()
+    a = [_make(g, kw, 3) for g, kw in members]
+    b = [_make(g, kw, 3) for g, kw in members]
+    with Batch(a) as ba, Batch(b) as bb:
+        st = ba.step(3)
+        for i in range(3):
+            bb.prepare()
+            rec = bb.solve()
+            for k in range(len(b)):
+                assert rec[k]["sor_iterations"] == st[k, i]["sor_iterations"]
+                assert rec[k]["norm_squared"] == st[k, i]["norm_squared"]
+                assert rec[k]["delt"] == st[k, i]["delt"]
+    for sa, sb in zip(a, b):
+        for n in ("u", "v", "p"):
+            np.testing.assert_array_equal(sb.download(n), sa.download(n), err_msg=n)
+        sa.close()
+        sb.close()
+
+
+def _net_with_random_head(seed=3):
+    import torch
+    from stroemung_gb300.unet import UNet
+    net = UNet(seed=seed)
+    th = net.theta.detach().cpu().numpy().copy()
+    th[-33:] = np.random.default_rng(seed).normal(0.0, 0.3, 33).astype(np.float32)
+    net.load_state_dict({"theta": th, "step": 0})
+    torch.cuda.synchronize()
+    return net
+
+
+@pytest.mark.parametrize("judge_sweeps", [-1, 4])
+def test_batch_warm_start_matches_members_stepped_alone(judge_sweeps):
+    """A batch stepped with the learned warm start (prediction and judge per
+    member between the batch's halves) ends bit-identical to each member
+    stepped alone by WarmStartSolver; judge -1 applies every prediction."""
+    from stroemung_gb300 import warmstart
+    net = _net_with_random_head()
+    members = _members()
+    steps = 3
+    alone = []
+    for grid, kw in members:
+        sim = _make(grid, kw, 3)
+        ws = warmstart.WarmStartSolver(sim, net, judge_sweeps=judge_sweeps)
+        recs = []
+        for _ in range(steps):
+            it, ns = ws.step()
+            recs.append((it, ns, ws.last["accepted"]))
+        alone.append((recs, {n: sim.download(n) for n in ("u", "v", "p")}))
+        sim.close()
+    sims = [_make(grid, kw, 3) for grid, kw in members]
+    with Batch(sims) as batch:
+        bws = warmstart.BatchWarmStart(batch, net, judge_sweeps=judge_sweeps)
+        for i in range(steps):
+            rec = bws.step()
+            for k in range(len(sims)):
+                it, ns, acc = alone[k][0][i]
+                assert rec[k]["sor_iterations"] == it, (k, i)
+                assert rec[k]["norm_squared"] == ns, (k, i)
+                assert bws.last["accepted"][k] == acc, (k, i)
+    if judge_sweeps < 0:
+        assert all(a for recs, _ in alone for (_, _, a) in recs)
+    for k, sim in enumerate(sims):
+        for n in ("u", "v", "p"):
+            np.testing.assert_array_equal(sim.download(n), alone[k][1][n], err_msg=n)
+        sim.close()
