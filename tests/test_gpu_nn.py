@@ -52,9 +52,12 @@ def _nhwc(x, cin_p):
     return out.contiguous()
 
 
+# the odd sizes leave partial pixel tiles and image rows
 @pytest.mark.parametrize("cin,cout,h,w,relu", [(3, 32, 16, 128, 1), (32, 64, 8, 64, 1),
                                                 (96, 32, 16, 32, 0), (128, 256, 4, 64, 1),
-                                                (64, 16, 8, 16, 1)])
+                                                (64, 16, 8, 16, 1), (32, 32, 7, 200, 1),
+                                                (64, 64, 5, 300, 0), (8, 32, 3, 130, 1),
+                                                (48, 32, 9, 140, 1), (96, 32, 4, 256, 1)])
 def test_conv3x3_forward_matches_torch(cin, cout, h, w, relu):
     import torch
     import torch.nn.functional as F
