@@ -19,9 +19,20 @@ enum {
     STRM_NN_ERR_TIMEOUT = 4
 };
 
+/* The three tensor-core contractions (strm_nn_gemm_bf16, strm_nn_conv3x3,
+ * strm_nn_conv3x3_wgrad) wait for their kernel and return STRM_NN_ERR_TIMEOUT
+ * when a bounded wait inside it gave up.  strm_nn_set_sync(0) makes them
+ * return right after the launch (process-wide; 1 restores waiting); a
+ * timeout is then reported by strm_nn_status, which waits for `stream` and
+ * returns STRM_NN_ERR_TIMEOUT once any such wait on this device has given
+ * up (the flag stays set). */
+int strm_nn_set_sync(int sync);
+int strm_nn_status(void *stream);
+
 /* d[m x n] (FP32, row-major) = a[m x k] * b[n x k]^T with a, b BF16 row-major
  * device arrays; m, n multiples of 128, k a multiple of 64.  tcgen05.mma with
- * TMEM accumulators; synchronous on `stream` (a cudaStream_t). */
+ * TMEM accumulators, on `stream` (a cudaStream_t); waits for the kernel
+ * unless strm_nn_set_sync(0). */
 int strm_nn_gemm_bf16(const void *a, const void *b, float *d, int m, int n, int k,
                       void *stream);
 
@@ -35,8 +46,8 @@ int strm_nn_gemm_bf16(const void *a, const void *b, float *d, int m, int n, int 
  * [cout][kp] with K = tap*cin_p + channel (tap = (dy+1)*3 + (dx+1)), kp =
  * roundup(9*cin_p, 64), zero padded; cout in {16, 32, 64, 128, 256}; bias
  * FP32 [cout] or NULL; relu 0/1; output BF16 at y (pixel stride cs_out), or
- * FP32 at y32 when y32 is not NULL.  Synchronous (returns TIMEOUT if a bounded
- * wait gave up). */
+ * FP32 at y32 when y32 is not NULL.  Waits for the kernel unless
+ * strm_nn_set_sync(0) (see above). */
 int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *w, int kp,
                     const float *bias, void *y, float *y32, int cs_out, int cout, int batch,
                     int h, int width, int relu, void *stream);
@@ -44,7 +55,8 @@ int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *w, int kp,
 /* Weight gradient of that convolution, accumulated (+=) into FP32
  * dw[cout][kp]: dw += sum_q g[q] (x) im2col(x)[q], with g = dy masked by the
  * forward ReLU output yact (y > 0) when yact is not NULL (yact uses the
- * forward pixel stride cs_out).  Synchronous. */
+ * forward pixel stride cs_out).  Waits for the kernel unless
+ * strm_nn_set_sync(0). */
 int strm_nn_conv3x3_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy,
                           int cs_dy, const void *yact, int cs_out, float *dw, int cout,
                           int batch, int h, int width, void *stream);

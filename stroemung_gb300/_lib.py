@@ -125,6 +125,8 @@ SIGNATURES = {
     "strm_host_boundary_pass": [ctypes.c_int, ctypes.c_int, _u8p, _dp, _dp, _dp, _dp, _dp],
     "strm_last_error": [ctypes.c_char_p, ctypes.c_size_t],
     # include/stroemung_nn.h
+    "strm_nn_set_sync": [_i],
+    "strm_nn_status": [_vp],
     "strm_nn_gemm_bf16": [_vp, _vp, _fp, _i, _i, _i, _vp],
     "strm_nn_conv3x3": [_vp, _i, _i, _vp, _i, _fp, _vp, _fp, _i, _i, _i, _i, _i, _i, _vp],
     "strm_nn_conv3x3_wgrad": [_vp, _i, _i, _i, _vp, _i, _vp, _i, _fp, _i, _i, _i, _i, _vp],

@@ -4,6 +4,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "../../include/stroemung_nn.h"
@@ -421,6 +422,17 @@ cudaError_t error_flag(unsigned int **out) {
   *out = g_err[dev];
   return cudaSuccess;
 }
+
+// 1: the contractions wait for their kernel and report its timeout flag
+std::atomic<int> g_sync{1};
+
+int read_flag(unsigned int *err, cudaStream_t s) {
+  unsigned int h = 0;
+  if (cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return STRM_NN_ERR_CUDA;
+  return h ? STRM_NN_ERR_TIMEOUT : STRM_NN_OK;
+}
 }  // namespace
 
 }  // namespace strm_nn
@@ -438,11 +450,7 @@ extern "C" int strm_nn_gemm_bf16(const void *a, const void *b, float *d, int m, 
   gemm_bf16_kernel<<<dim3(n / GN, m / GM), 128, smem, s>>>(
       (const __nv_bfloat16 *)a, (const __nv_bfloat16 *)b, d, m, n, k, err);
   if (cudaGetLastError() != cudaSuccess) return STRM_NN_ERR_CUDA;
-  unsigned int h = 0;
-  if (cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return STRM_NN_ERR_CUDA;
-  return h ? STRM_NN_ERR_TIMEOUT : STRM_NN_OK;
+  return g_sync.load() ? read_flag(err, s) : STRM_NN_OK;
 }
 
 namespace {
@@ -497,12 +505,8 @@ int launch_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy, in
 }
 
 int finish(unsigned int *err, cudaStream_t s, int rc) {
-  if (rc != STRM_NN_OK) return rc;
-  unsigned int h = 0;
-  if (cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return STRM_NN_ERR_CUDA;
-  return h ? STRM_NN_ERR_TIMEOUT : STRM_NN_OK;
+  if (rc != STRM_NN_OK || !g_sync.load()) return rc;
+  return read_flag(err, s);
 }
 
 bool conv_args_ok(int cs_in, int cin_p, int kp, int cs_out, int cout) {
@@ -512,6 +516,17 @@ bool conv_args_ok(int cs_in, int cin_p, int kp, int cs_out, int cout) {
 }
 
 }  // namespace
+
+extern "C" int strm_nn_set_sync(int sync) {
+  g_sync.store(sync ? 1 : 0);
+  return STRM_NN_OK;
+}
+
+extern "C" int strm_nn_status(void *stream) {
+  unsigned int *err = nullptr;
+  if (error_flag(&err) != cudaSuccess) return STRM_NN_ERR_CUDA;
+  return read_flag(err, (cudaStream_t)stream);
+}
 
 extern "C" int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *w, int kp,
                                const float *bias, void *y, float *y32, int cs_out, int cout,

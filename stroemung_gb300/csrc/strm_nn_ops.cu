@@ -339,19 +339,15 @@ __global__ void assemble_input(const float *rhs, const uint8_t *flags, const flo
 }
 
 // Per-sample mean of p_prev over fluid cells (sum and count by atomics).
-// Sum and count of p over each sample's non-boundary cells, one block per
-// sample with a fixed reduction order, so the network input (and with it
-// the prediction) is the same bits run after run.
-__global__ void __launch_bounds__(1024)
-    sample_mean(const float *p, const uint8_t *flags, float *sum, float *cnt, int plane) {
+// Sum and count of p over each sample's non-boundary cells in a fixed order,
+// so the network input (and with it the prediction) is the same bits run
+// after run: kMeanBlocks blocks per sample reduce strided shares with a fixed
+// shuffle tree into partials (sum, count) [batch][kMeanBlocks][2], then one
+// warp per sample adds those in order.
+constexpr int kMeanBlocks = 64;
+
+__device__ __forceinline__ void block_sum2(float &s, float &c) {
   __shared__ float ss[32], sc[32];
-  const int b = blockIdx.y;
-  float s = 0.0f, c = 0.0f;
-  for (int i = threadIdx.x; i < plane; i += blockDim.x)
-    if (!is_bnd(flags[(size_t)b * plane + i])) {
-      s += p[(size_t)b * plane + i];
-      c += 1.0f;
-    }
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_xor_sync(0xffffffffu, s, o);
     c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -369,10 +365,39 @@ __global__ void __launch_bounds__(1024)
       s += __shfl_xor_sync(0xffffffffu, s, o);
       c += __shfl_xor_sync(0xffffffffu, c, o);
     }
-    if (lane == 0) {
-      sum[b] = s;
-      cnt[b] = c;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    sample_mean_partial(const float *p, const uint8_t *flags, float *part, int plane) {
+  const int b = blockIdx.y;
+  float s = 0.0f, c = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x)
+    if (!is_bnd(flags[(size_t)b * plane + i])) {
+      s += p[(size_t)b * plane + i];
+      c += 1.0f;
     }
+  block_sum2(s, c);
+  if (threadIdx.x == 0) {
+    part[((size_t)b * gridDim.x + blockIdx.x) * 2] = s;
+    part[((size_t)b * gridDim.x + blockIdx.x) * 2 + 1] = c;
+  }
+}
+
+__global__ void sample_mean_final(const float *part, int nblocks, float *sum, float *cnt) {
+  const int b = blockIdx.x, lane = threadIdx.x;
+  float s = 0.0f, c = 0.0f;
+  for (int k = lane; k < nblocks; k += 32) {
+    s += part[((size_t)b * nblocks + k) * 2];
+    c += part[((size_t)b * nblocks + k) * 2 + 1];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if (lane == 0) {
+    sum[b] = s;
+    cnt[b] = c;
   }
 }
 
@@ -739,7 +764,14 @@ int strm_nn_prepare_input(const float *rhs, const uint8_t *flags, const float *p
     return STRM_NN_ERR_CUDA;
   dim3 g2((plane + 255) / 256 < 64 ? (plane + 255) / 256 : 64, batch);
   sample_absmax<<<g2, 256, 0, s>>>(rhs, flags, smax, plane);
-  sample_mean<<<dim3(1, batch), 1024, 0, s>>>(pprev, flags, work2, work2 + batch, plane);
+  // the per-block partial sums borrow the start of xin, which
+  // assemble_input then overwrites (16 bytes per interior cell; at most
+  // 2 partials of 8 bytes per interior cell are used)
+  float *part = static_cast<float *>(xin);
+  const long long room = (long long)(nx - 2) * (ny - 2) * 2;  // 8-byte partials per sample
+  const int nmb = room < kMeanBlocks ? (int)room : kMeanBlocks;
+  sample_mean_partial<<<dim3(nmb, batch), 256, 0, s>>>(pprev, flags, part, plane);
+  sample_mean_final<<<batch, 32, 0, s>>>(part, nmb, work2, work2 + batch);
   mean_div<<<(batch + 255) / 256, 256, 0, s>>>(work2, work2 + batch, pmean, batch);
   assemble_input<<<grid_for((long long)batch * (nx - 2) * (ny - 2)), 256, 0, s>>>(
       rhs, flags, pprev, smax, pmean, dx2, (bf16 *)xin, batch, nx, ny);

@@ -20,6 +20,8 @@ boundary copy, averaged over the batch.
 """
 from __future__ import annotations
 
+import contextlib
+
 import math
 
 import numpy as np
@@ -114,6 +116,17 @@ class UNet:
     def _check(self, rc, what):
         if rc != 0:
             raise RuntimeError(f"{what} failed with status {rc}")
+
+    @contextlib.contextmanager
+    def _deferred(self):
+        """The tensor-core kernels of one pass run without a host wait each;
+        their timeout flag is checked once at the end."""
+        self.L.strm_nn_set_sync(0)
+        try:
+            yield
+        finally:
+            self.L.strm_nn_set_sync(1)
+        self._check(self.L.strm_nn_status(None), "tensor-core kernels")
 
     def _wbf(self, layer):
         return self.theta_bf.data_ptr() + 2 * int(self._offsets[layer.w])
@@ -219,6 +232,10 @@ class UNet:
         Returns the FP32 correction q [b][h][w].  keep=False (prediction
         only, no backward to follow) runs in the shared forward pool: q is
         then valid until the next such call."""
+        with self._deferred():
+            return self._forward(xin, b, h, w, keep)
+
+    def _forward(self, xin, b, h, w, keep):
         B = self._buffers(b, h, w) if keep else self._forward_buffers(b, h, w)
         B["x_in_ptr"] = xin.data_ptr()
         L = self.L
@@ -289,6 +306,10 @@ class UNet:
     def backward(self, gq, b, h, w):
         """gq: FP32 [b][h][w] gradient of the loss with respect to the output.
         Accumulates every parameter gradient into self.grad."""
+        with self._deferred():
+            self._backward(gq, b, h, w)
+
+    def _backward(self, gq, b, h, w):
         B = self._buffers(b, h, w)
         L = self.L
         c0, c1, c2, c3 = CHANNELS

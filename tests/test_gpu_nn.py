@@ -129,3 +129,30 @@ def test_conv3x3_weight_and_data_gradients_match_torch(cin, cout, h, w):
     ref_x = xr.grad.permute(0, 2, 3, 1)
     err = (dx.float() - ref_x).abs().max().item()
     assert err <= 1e-2 * max(1.0, ref_x.abs().max().item()), err
+
+
+def test_deferred_waits_give_the_same_result():
+    """strm_nn_set_sync(0): the convolution returns after its launch, the
+    result equals the waiting call's, and strm_nn_status reports no
+    timeout."""
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    cin, cout, h, w = 32, 64, 16, 96
+    x = _bf(torch.randn(1, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.2)
+    wp, kp = _pack_weights(wt, cin)
+    xn = _nhwc(x, cin)
+    y1 = torch.empty(1, h, w, cout, device="cuda", dtype=torch.bfloat16)
+    y2 = torch.empty_like(y1)
+    torch.cuda.synchronize()
+    assert L.strm_nn_conv3x3(xn.data_ptr(), cin, cin, wp.data_ptr(), kp, None, y1.data_ptr(),
+                             None, cout, cout, 1, h, w, 1, None) == 0
+    assert L.strm_nn_set_sync(0) == 0
+    try:
+        assert L.strm_nn_conv3x3(xn.data_ptr(), cin, cin, wp.data_ptr(), kp, None,
+                                 y2.data_ptr(), None, cout, cout, 1, h, w, 1, None) == 0
+    finally:
+        L.strm_nn_set_sync(1)
+    assert L.strm_nn_status(None) == 0
+    assert torch.equal(y1, y2)
