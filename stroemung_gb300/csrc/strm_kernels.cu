@@ -573,17 +573,13 @@ __global__ void pcopy_kernel(double *p, const PCopy *pc, int n, int pitch) {
   if (k < n) pcopy_one(p, pc[k], pitch);
 }
 
-// SOR update of one fluid cell (src/simulation.rs:260-271).
-template <bool EXACT>
+// SOR update of one fluid cell in the reference's operation order
+// (src/simulation.rs:260-271).  The fast-arithmetic passes form it from the
+// residual instead (sor_red_res_kernel, sor_black_res_kernel).
 __device__ __forceinline__ double sor_update(double p, double pw, double pe, double pn, double ps,
                                              double r, const Consts &c) {
-  if (EXACT) {
-    return (c.one_minus_w * p) +
-           c.middle * (xdiv(pe + pw, c.dx2, c.r_dx2) + xdiv(ps + pn, c.dy2, c.r_dy2) - r);
-  } else {
-    const double t = fma(pe + pw, c.r_dx2, fma(ps + pn, c.r_dy2, -r));
-    return fma(c.one_minus_w, p, c.middle * t);
-  }
+  return (c.one_minus_w * p) +
+         c.middle * (xdiv(pe + pw, c.dx2, c.r_dx2) + xdiv(ps + pn, c.dy2, c.r_dy2) - r);
 }
 
 // Residual of one interior cell (src/math.rs:176-186).
@@ -600,10 +596,9 @@ __device__ __forceinline__ double residual_of(double p, double pw, double pe, do
   }
 }
 
-// One colour of a red-black sweep: cells with (x + y) % 2 == color.  Thread
-// (tx, ty) owns the cell pair y = 2*(y-pair), x = row; it updates the member
-// of the pair that has the colour.
-template <bool EXACT>
+// One colour of an exact-arithmetic red-black sweep: cells with
+// (x + y) % 2 == color.  Thread (tx, ty) owns the cell pair y = 2*(y-pair),
+// x = row; it updates the member of the pair that has the colour.
 __global__ void __launch_bounds__(256)
     sor_color_kernel(double *__restrict__ p, const double *__restrict__ rhs,
                      const uint8_t *__restrict__ flags, Geom g, Consts c, int color) {
@@ -614,7 +609,7 @@ __global__ void __launch_bounds__(256)
   if (flags[o] != 0) return;
   const double pc = p[o], pw = p[o - g.pitch], pe = p[o + g.pitch];
   const double pn = p[o - 1], ps = p[o + 1];
-  p[o] = sor_update<EXACT>(pc, pw, pe, pn, ps, rhs[o], c);
+  p[o] = sor_update(pc, pw, pe, pn, ps, rhs[o], c);
 }
 
 // The colour passes of the FAST red-black solve stride over the virtual
@@ -650,10 +645,10 @@ __device__ __forceinline__ PassCells pass_cells(int vb0, int stride, int nvb, in
 }
 
 // The black pass of a FAST red-black iteration fused with the residual of the
-// black fluid cells: once they are updated their four (red) neighbours are
-// final, so r = t - 2(1/dx^2+1/dy^2) p_new with t from the update (the same
-// p_new as sor_color_kernel<false>).  Its sums of r^2 (and r when mean-free)
-// go to partials_b[blockIdx.x].
+// black fluid cells: with t = (pe+pw)/dx^2 + (ps+pn)/dy^2 - rhs from the red
+// values, p_new = (1-omega) p + omega t / (2/dx^2+2/dy^2), and since the four
+// (red) neighbours are final the cell's residual is r = t - 2(1/dx^2+1/dy^2)
+// p_new.  Its sums of r^2 (and r when mean-free) go to partials_b[blockIdx.x].
 __global__ void __launch_bounds__(256)
     sor_black_res_kernel(double *__restrict__ p, const double *__restrict__ rhs,
                          const uint8_t *__restrict__ flags, Geom g, Consts c,
@@ -952,12 +947,12 @@ __global__ void __launch_bounds__(256)
 // values it overwrites into pw.
 __global__ void pcopy_save_kernel(double *p, double *pw, const PCopy *pc, int n, int pitch,
                                   const StepState *st, unsigned int itermax) {
-  if (st->sor_iters + 1 >= itermax) return;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) {
-    pw[pc[k].off] = p[pc[k].off];
-    pcopy_one(p, pc[k], pitch);
-  }
+  if (k >= n) return;
+  const PCopy c = pc[k];  // loaded together with the iteration count
+  if (st->sor_iters + 1 >= itermax) return;
+  pw[c.off] = p[c.off];
+  pcopy_one(p, c, pitch);
 }
 
 // Red pass.  mode 0: update only (the first red pass of a solve, and the
@@ -1064,7 +1059,7 @@ __global__ void __launch_bounds__(1024)
         const int y = d - x;
         const size_t o = OFF(x, y);
         if (flags[o] == 0)
-          p[o] = sor_update<true>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
+          p[o] = sor_update(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
                                   rhs[o], c);
       }
       __syncthreads();
@@ -2149,7 +2144,7 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
                                                            bb);
   } else {
     for (int color = 0; color < 2; ++color)
-      sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
+      sor_color_kernel<<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
     residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                           d.partials, ty, nt, 0, r.itermax,
                                                           r.strict_eps, RES_NORM, nullptr, 0);
@@ -2321,7 +2316,7 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
       {
         for (int color = 0; color < 2; ++color)
-          sor_color_kernel<true><<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
+          sor_color_kernel<<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, color);
         residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.st, d.partials,
                                                               ty_int, nt_int, 0, r.itermax,
                                                               r.strict_eps, RES_SOLVE, nullptr, 0);
@@ -2607,7 +2602,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         if (d.n_pcopy > 0)
           bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
                         dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
-        const void *kc = (const void *)sor_color_kernel<true>;
+        const void *kc = (const void *)sor_color_kernel;
         const void *kr = (const void *)residual_kernel<true, true>;
         for (int color = 0; color < 2; ++color)
           bn = b.kernel(body, bn, kc, sgrid, kRedBlock, d.p, (const double *)d.rhs,
