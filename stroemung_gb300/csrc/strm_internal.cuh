@@ -120,6 +120,75 @@ __host__ __device__ __forceinline__ double xdiv(double a, double b, double rb) {
 #endif
 }
 
+// Conversions between FP32 and FP64 in integer arithmetic.  On this part
+// the conversion instructions run on the narrow FP64 pipe; the mixed-precision
+// kernels convert every cell, so they use these instead (bit manipulation on
+// the integer pipe).  Both flush magnitudes below 2^-126 (the FP32 normal
+// range) to zero of the same sign; infinities and NaNs map to themselves.
+__host__ __device__ __forceinline__ uint64_t f64_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double f64_of(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ float f32_of(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+
+// float -> double, exact (FP32 denormals flushed).
+__host__ __device__ __forceinline__ double widen(float f) {
+  const uint32_t u = f32_bits(f);
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  if (e == 0) return f64_of(sign);
+  if (e == 0xFF) return f64_of(sign | 0x7FF0000000000000ull | ((uint64_t)m << 29));
+  return f64_of(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29));
+}
+
+// double -> float, rounded to nearest (ties to even).
+__host__ __device__ __forceinline__ float narrow(double x) {
+  const uint64_t b = f64_bits(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7FFu);
+  const uint64_t M = b & 0xFFFFFFFFFFFFFull;
+  if (E == 0x7FF) return f32_of(sign | 0x7F800000u | (M ? 0x400000u : 0u));
+  const int e = E - 896;  // FP32 biased exponent
+  if (e >= 255) return f32_of(sign | 0x7F800000u);
+  if (e <= 0) return f32_of(sign);
+  const uint32_t m = (uint32_t)(M >> 29);
+  const uint32_t rem = (uint32_t)(M & 0x1FFFFFFFu), half = 0x10000000u;
+  uint32_t r = ((uint32_t)e << 23) | m;
+  if (rem > half || (rem == half && (m & 1u))) ++r;  // a carry moves into the exponent
+  return f32_of(sign | r);
+}
+
 // Order-preserving map of a double onto uint64 (for atomicMin/atomicMax).
 __host__ __device__ __forceinline__ unsigned long long ord_enc(double d) {
 #ifdef __CUDA_ARCH__

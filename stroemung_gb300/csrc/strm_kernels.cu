@@ -386,8 +386,8 @@ struct HL {
 
 __device__ __forceinline__ HL hl_of(double x) {
   HL r;
-  r.h = __double2float_rn(x);
-  r.l = __double2float_rn(x - (double)r.h);
+  r.h = narrow(x);
+  r.l = narrow(x - widen(r.h));
   return r;
 }
 // a - b
@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(FG_THREADS)
         const float inc = dt32 * (f_laplacian(u11, u10, u12, u01, u21, k) * k.r_re -
                                   f_du2dx(u01, u11, u21, k) -
                                   f_duvdy(u11, u10, u12, v11, v10, v21, v20, k));
-        Fv = u[o] + (double)inc;
+        Fv = u[o] + widen(inc);
       } else {
         Fv = f[o];
       }
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(FG_THREADS)
         const float inc = dt32 * (f_laplacian(v11, v10, v12, v01, v21, k) * k.r_re -
                                   f_duvdx(u11, u12, u01, u02, v11, v21, v01, k) -
                                   f_dv2dy(v10, v11, v12, k));
-        Gv = v[o] + (double)inc;
+        Gv = v[o] + widen(inc);
       } else {
         Gv = gg[o];
       }
@@ -1513,7 +1513,7 @@ __device__ __forceinline__ void refine_cells(double *__restrict__ p, const float
     const bool fluid_in = fl == 0 && x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
     if (save) save[o] = p[o];
     if (apply && (fluid_in || (is_bnd(fl) && edge_of(fl) != E_NONE)))
-      p[o] = p[o] + (double)e[o];
+      p[o] = p[o] + widen(e[o]);
     ez[o] = 0.0f;
   }
 }
@@ -1559,6 +1559,9 @@ __device__ __forceinline__ void mixed_residual_sum(
     const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
     int tiles_y, int ntiles, int bid, int nblocks, double *acc_out, double *acc1_out) {
   double acc = 0.0, acc1 = 0.0;
+  // the defect is rounded to FP32 before the scaling (integer conversion,
+  // FP32 multiply): no FP64 operation beyond the residual and its sums
+  const float mid32 = narrow(c.middle);
   for (int t = bid; t < ntiles; t += nblocks) {
     const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
     if (x > g.nx - 2) continue;
@@ -1575,7 +1578,7 @@ __device__ __forceinline__ void mixed_residual_sum(
           acc = fma(r, r, acc);
           if (MEAN_FREE) acc1 += r;
         }
-        if (fluid) s[o] = (float)(c.middle * r);
+        if (fluid) s[o] = narrow(r) * mid32;
       }
     }
   }

@@ -189,8 +189,8 @@ class UNet:
         return B
 
     def _forward_buffers(self, b, h, w):
-        """The forward pass's buffers as views of one shared, zero-filled pool
-        (no gradients): for predictions over many grid shapes, which would
+        """The forward pass's buffers as views of one shared pool (no
+        gradients): for predictions over many grid shapes, which would
         otherwise each keep a full set.  Valid until the next such call."""
         import torch
         if h % 8 or w % 8:
@@ -212,8 +212,9 @@ class UNet:
         total += 4 * b * h * w
         pool = getattr(self, "_pool", None)
         if pool is None or pool.numel() < total:
-            pool = self._pool = torch.empty(total, dtype=torch.uint8, device=self.device)
-        pool[:total].zero_()
+            # zeroed once: the forward writes every buffer in full before it
+            # reads it, so views of an earlier shape's data need no clearing
+            pool = self._pool = torch.zeros(total, dtype=torch.uint8, device=self.device)
         B = {}
         for (name, hh, ww, c), o in zip(spec, offs):
             n = 2 * b * hh * ww * c
