@@ -1345,7 +1345,9 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
                                               const float *__restrict__ s,
                                               const uint8_t *__restrict__ flags, const Geom &g,
                                               const Consts32 &k, int tile, int tiles_y, int n,
-                                              int skip_last_copy, unsigned char *smem_raw) {
+                                              int skip_last_copy, unsigned char *smem_raw,
+                                              double *__restrict__ pf = nullptr,
+                                              double *__restrict__ pw = nullptr) {
   static_assert(H % 4 == 0 && TX % 2 == 0 && TY % 4 == 0, "tile origins must be multiples of 4");
   static_assert(TY + 2 * H == 128, "extended rows are 128 cells");
   constexpr int EX = TX + 2 * H, EY = 128, W = EY / 2, NC = EX * W;
@@ -1462,7 +1464,53 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
   }
   // write the interior back: lane takes cells 4*lane .. 4*lane+3 of a row
   const int ly0 = 4 * lane;
-  if (ly0 >= H && ly0 < H + TY) {
+  if (pf && ly0 >= H && ly0 < H + TY) {
+    // the outer iteration's last launch ends it here (as refine_cells):
+    // p += e on the cells the sweeps update (fluid interior, boundary cells
+    // with an edge), the previous p saved in pw, and eout cleared for the
+    // next outer iteration's sweeps
+    for (int lx = H + warp; lx < H + TX; lx += WARPS) {
+      const int x = gx0 + lx;
+      if (x >= g.nx) break;
+      const int c0 = lx & 1;
+      const int ia = c0 * NC + lx * W + j0, ib = (1 - c0) * NC + lx * W + j0;
+      const float2 a = *reinterpret_cast<const float2 *>(se + ia);
+      const float2 b = *reinterpret_cast<const float2 *>(se + ib);
+      const uchar2 ca = *reinterpret_cast<const uchar2 *>(sc + ia);
+      const uchar2 cb = *reinterpret_cast<const uchar2 *>(sc + ib);
+      const float ev[4] = {a.x, b.x, a.y, b.y};
+      const uint8_t cv[4] = {ca.x, cb.x, ca.y, cb.y};
+      const int y0 = gy0 + ly0;
+      const size_t o = OFF(x, y0);
+      if (y0 + 3 < g.ny) {
+        // four consecutive cells: 32-byte aligned (y0 and the pitch are
+        // multiples of 4), two 16-byte accesses per FP64 field
+        double2 *p2 = reinterpret_cast<double2 *>(pf + o);
+        const double2 lo = p2[0], hi = p2[1];
+        if (pw) {
+          double2 *w2 = reinterpret_cast<double2 *>(pw + o);
+          w2[0] = lo;
+          w2[1] = hi;
+        }
+        const double pv[4] = {lo.x, lo.y, hi.x, hi.y};
+        double nv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) nv[q] = cv[q] != kFrozen ? pv[q] + widen(ev[q]) : pv[q];
+        p2[0] = make_double2(nv[0], nv[1]);
+        p2[1] = make_double2(nv[2], nv[3]);
+        *reinterpret_cast<float4 *>(eout + o) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (y0 + q >= g.ny) break;
+          const double p0 = pf[o + q];
+          if (pw) pw[o + q] = p0;
+          if (cv[q] != kFrozen) pf[o + q] = p0 + widen(ev[q]);
+          eout[o + q] = 0.0f;
+        }
+      }
+    }
+  } else if (ly0 >= H && ly0 < H + TY) {
     for (int lx = H + warp; lx < H + TX; lx += WARPS) {
       const int x = gx0 + lx;
       if (x >= g.nx) break;
@@ -1486,10 +1534,11 @@ template <int H, int TX, int TY>
 __global__ void __launch_bounds__(512)
     sor32_tb_kernel(const float *__restrict__ ein, float *__restrict__ eout,
                     const float *__restrict__ s, const uint8_t *__restrict__ flags, Geom g,
-                    Consts32 k, int tiles_y, int n, int skip_last_copy) {
+                    Consts32 k, int tiles_y, int n, int skip_last_copy, double *pf,
+                    double *pw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   sor32_tb_tile<H, TX, TY>(ein, eout, s, flags, g, k, (int)blockIdx.x, tiles_y, n,
-                           skip_last_copy, smem_raw);
+                           skip_last_copy, smem_raw, pf, pw);
 }
 
 // p += e on fluid interior cells and boundary cells with an edge (apply != 0),
@@ -1935,12 +1984,17 @@ struct SweepLaunch {
   float *eout;
   int tiles_y, n, skip_last_copy;
   int color, copy;  // schedule 0
+  double *pf, *pw;  // blocked: the launch also applies the correction to p
 };
 
 // The launches of m inner sweeps (colour passes or blocked tiles) starting
-// from correction buffer a; *final receives the buffer holding the result.
+// from correction buffer e32; *final receives the buffer holding the result.
+// refine (blocked schedules with an even number of launches): the last
+// launch also does the refinement (p += e, p saved in `save` when not NULL,
+// its output buffer, e32, cleared) and *final is NULL.
 static std::vector<SweepLaunch> sweep_plan(const DevFields &d, const Geom &g, int m, int sched,
-                                           float **final) {
+                                           float **final, bool refine = false,
+                                           double *save = nullptr) {
   std::vector<SweepLaunch> v;
   if (sched <= 0 || sched >= kNumSchedules) {
     dim3 pgrid((g.ny / 2 + 1 + kRedBlock.x - 1) / kRedBlock.x,
@@ -1979,6 +2033,11 @@ static std::vector<SweepLaunch> sweep_plan(const DevFields &d, const Geom &g, in
     cur ^= 1;
   }
   *final = bufs[cur];
+  if (refine && cur == 0) {
+    v.back().pf = d.p;
+    v.back().pw = save;
+    *final = nullptr;
+  }
   return v;
 }
 
@@ -2005,8 +2064,9 @@ static cudaError_t issue_sweep(const SweepLaunch &l, const float *s, const uint8
   if (l.smem == 0) {
     sor32_color_kernel<<<l.grid, l.block, 0, st>>>(l.eout, s, flags, g, k32, l.color, l.copy);
   } else {
-    void *args[] = {(void *)&l.ein, (void *)&l.eout, (void *)&s, (void *)&flags, (void *)&g,
-                    (void *)&k32, (void *)&l.tiles_y, (void *)&l.n, (void *)&l.skip_last_copy};
+    void *args[] = {(void *)&l.ein, (void *)&l.eout, (void *)&s, (void *)&flags,
+                    (void *)&g, (void *)&k32, (void *)&l.tiles_y, (void *)&l.n,
+                    (void *)&l.skip_last_copy, (void *)&l.pf, (void *)&l.pw};
     return cudaLaunchKernel(l.fn, l.grid, l.block, args, l.smem, st);
   }
   return cudaGetLastError();
@@ -2203,8 +2263,9 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
                (g.nx + kRedBlock.y - 1) / kRedBlock.y);
     if ((e = tb_prepare()) != cudaSuccess) return e;
     float *final = nullptr;
-    const std::vector<SweepLaunch> plan = sweep_plan(d, g, m, r.sweep_schedule, &final);
     const int coarse = m > 1 ? 1 : 0;
+    const std::vector<SweepLaunch> plan =
+        sweep_plan(d, g, m, r.sweep_schedule, &final, true, coarse ? d.pw : nullptr);
     refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0, nullptr);
     launch_delta(d, g, s);
     mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
@@ -2213,8 +2274,9 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     while (!done) {
       for (const SweepLaunch &l : plan)
         if ((e = issue_sweep(l, d.r32, d.flags, g, k32, s)) != cudaSuccess) return e;
-      refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1,
-                                                coarse ? d.pw : nullptr);
+      if (final)  // else the last blocked launch refined
+        refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1,
+                                                  coarse ? d.pw : nullptr);
       launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
@@ -2434,7 +2496,9 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                (g.nx + kRedBlock.y - 1) / kRedBlock.y);
     if (b.err == cudaSuccess) b.err = tb_prepare();
     float *final = nullptr;
-    const std::vector<SweepLaunch> plan = sweep_plan(d, g, m, r.sweep_schedule, &final);
+    const int coarse_g = m > 1 ? 1 : 0;
+    const std::vector<SweepLaunch> plan =
+        sweep_plan(d, g, m, r.sweep_schedule, &final, true, coarse_g ? d.pw : nullptr);
     cudaGraphConditionalHandle h;
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
@@ -2470,12 +2534,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         else
           bn = b.kernel_smem(body, bn, l.fn, l.grid, l.block, l.smem, l.ein, l.eout,
                              (const float *)d.r32, (const uint8_t *)d.flags, g, k32, l.tiles_y,
-                             l.n, l.skip_last_copy);
+                             l.n, l.skip_last_copy, l.pf, l.pw);
       }
-      // the refinement also keeps p before this outer iteration (for a redo)
-      bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
-                    (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1,
-                    coarse ? d.pw : (double *)nullptr);
+      // the refinement also keeps p before this outer iteration (for a redo);
+      // the last blocked launch did it when final is NULL
+      if (final)
+        bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
+                      (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1,
+                      coarse ? d.pw : (double *)nullptr);
       if (d.n_pcopy > 0)
         bn = b.kernel(body, bn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
                       dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
