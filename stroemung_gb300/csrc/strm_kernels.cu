@@ -1594,13 +1594,6 @@ __device__ __forceinline__ void delta_entry(const double *__restrict__ p, float 
   e[o] = d;
 }
 
-__global__ void delta_kernel(const double *__restrict__ p, float *__restrict__ s,
-                             float *__restrict__ e, const PCopy *__restrict__ pc, int n,
-                             int pitch) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  delta_entry(p, s, e, pc[k], pitch);
-}
 
 template <bool FLUID, bool MEAN_FREE>
 __device__ __forceinline__ void mixed_residual_sum(
@@ -1711,6 +1704,9 @@ __device__ __forceinline__ unsigned int replay_of(int status, const StepState *s
 // 2 the defect only (no norm, no state change).  coarse: the loop checks
 // every `sweeps` > 1 sweeps; when it stops, st->replay says how the solve
 // finishes (and, in a graph, h_replay opens the finishing pass).
+// The kernel also writes the boundary entries the next sweeps start from
+// (delta_entry for the npc listed boundary cells: s and e there, disjoint
+// from the fluid cells' defect).
 template <bool IN_GRAPH>
 __global__ void __launch_bounds__(256)
     mixed_residual_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
@@ -1718,7 +1714,14 @@ __global__ void __launch_bounds__(256)
                           Consts c, StepState *st, double *partials, int tiles_y, int ntiles,
                           cudaGraphConditionalHandle h, unsigned int itermax, int strict,
                           int sweeps, int check, cudaGraphConditionalHandle h_replay,
-                          int coarse) {
+                          int coarse, const PCopy *__restrict__ pc, int npc,
+                          float *__restrict__ e) {
+  {
+    const int nt = blockDim.x * blockDim.y;
+    for (int k = blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x; k < npc;
+         k += gridDim.x * nt)
+      delta_entry(p, s, e, pc[k], g.pitch);
+  }
   mixed_residual_partial(p, rhs, flags, s, g, c, partials, tiles_y, ntiles, strict, blockIdx.x,
                          gridDim.x);
   if (check == 2) return;
@@ -2215,11 +2218,6 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
   return cudaGetLastError();
 }
 
-static void launch_delta(const DevFields &d, const Geom &g, cudaStream_t s) {
-  if (d.n_pcopy > 0)
-    delta_kernel<<<(d.n_pcopy + 255) / 256, 256, 0, s>>>(d.p, d.r32, d.e32, d.pcopy, d.n_pcopy,
-                                                        g.pitch);
-}
 
 cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s) {
   sor_lex_kernel<<<1, 1024, 0, s>>>(d.p, d.rhs, d.flags, d.pcopy, d.n_pcopy, r.g, r.c, d.st,
@@ -2267,21 +2265,20 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     const std::vector<SweepLaunch> plan =
         sweep_plan(d, g, m, r.sweep_schedule, &final, true, coarse ? d.pw : nullptr);
     refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0, nullptr);
-    launch_delta(d, g, s);
     mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c, d.st,
                                                           d.partials, ty_int, nt_int, 0,
-                                                          r.itermax, r.strict_eps, m, 0, 0, coarse);
+                                                          r.itermax, r.strict_eps, m, 0, 0, coarse,
+                                                          d.pcopy, d.n_pcopy, d.e32);
     while (!done) {
       for (const SweepLaunch &l : plan)
         if ((e = issue_sweep(l, d.r32, d.flags, g, k32, s)) != cudaSuccess) return e;
       if (final)  // else the last blocked launch refined
         refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, final, d.e32, d.flags, g, 1,
                                                   coarse ? d.pw : nullptr);
-      launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
                                                             r.itermax, r.strict_eps, m, 1, 0,
-                                                            coarse);
+                                                            coarse, d.pcopy, d.n_pcopy, d.e32);
       if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
     }
     unsigned int replay = 0;
@@ -2296,21 +2293,20 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       // finish sweep by sweep so that the solve stops where a per-sweep test would
       restore_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.pw, g, d.st, m);
       refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 0, nullptr);
-      launch_delta(d, g, s);
       mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                             d.st, d.partials, ty_int, nt_int, 0,
-                                                            r.itermax, r.strict_eps, 1, 2, 0, 0);
+                                                            r.itermax, r.strict_eps, 1, 2, 0, 0,
+                                                            d.pcopy, d.n_pcopy, d.e32);
       done = false;
       while (!done) {
         for (int color = 0; color < 2; ++color)
           sor32_color_kernel<<<pgrid, kRedBlock, 0, s>>>(d.e32, d.r32, d.flags, g, k32, color,
                                                          color == 0 ? 1 : 0);
         refine_kernel<<<pgrid, kRedBlock, 0, s>>>(d.p, d.e32, d.e32, d.flags, g, 1, nullptr);
-        launch_delta(d, g, s);
         mixed_residual_kernel<false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, d.r32, g, c,
                                                               d.st, d.partials, ty_int, nt_int,
                                                               0, r.itermax, r.strict_eps, 1, 1, 0,
-                                                              0);
+                                                              0, d.pcopy, d.n_pcopy, d.e32);
         if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
       }
     }
@@ -2504,10 +2500,6 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
     n = b.kernel(b.graph, n, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
                  (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0, (double *)nullptr);
-    if (d.n_pcopy > 0)
-      n = b.kernel(b.graph, n, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
-                   dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
-                   d.n_pcopy, g.pitch);
     const int coarse = m > 1 ? 1 : 0;
     cudaGraphConditionalHandle h_rep{};
     if (b.err == cudaSuccess)
@@ -2515,7 +2507,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     n = b.kernel(b.graph, n, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                  (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32, g,
                  c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 0, h_rep,
-                 coarse);
+                 coarse, (const PCopy *)d.pcopy, d.n_pcopy, d.e32);
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
@@ -2542,14 +2534,10 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         bn = b.kernel(body, bn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
                       (const float *)final, d.e32, (const uint8_t *)d.flags, g, 1,
                       coarse ? d.pw : (double *)nullptr);
-      if (d.n_pcopy > 0)
-        bn = b.kernel(body, bn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
-                      dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
-                      d.n_pcopy, g.pitch);
       bn = b.kernel(body, bn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                     (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags, d.r32,
                     g, c, d.st, d.partials, ty_int, nt_int, h, r.itermax, r.strict_eps, m, 1,
-                    h_rep, coarse);
+                    h_rep, coarse, (const PCopy *)d.pcopy, d.n_pcopy, d.e32);
     }
     n = wnode;
     if (coarse) {
@@ -2570,17 +2558,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
         fn = b.kernel(ib, fn, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
                       (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 0,
                       (double *)nullptr);
-        if (d.n_pcopy > 0)
-          fn = b.kernel(ib, fn, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
-                        dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
-                        d.n_pcopy, g.pitch);
         cudaGraphConditionalHandle h_fine{};
         if (b.err == cudaSuccess)
           b.err = cudaGraphConditionalHandleCreate(&h_fine, ib, 1, cudaGraphCondAssignDefault);
         fn = b.kernel(ib, fn, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                       (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags,
                       d.r32, g, c, d.st, d.partials, ty_int, nt_int, h_fine, r.itermax,
-                      r.strict_eps, 1, 2, h_fine, 0);
+                      r.strict_eps, 1, 2, h_fine, 0, (const PCopy *)d.pcopy, d.n_pcopy,
+                      d.e32);
         cudaGraphNodeParams fp = {};
         fp.type = cudaGraphNodeTypeConditional;
         fp.conditional.handle = h_fine;
@@ -2598,14 +2583,11 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
           x = b.kernel(fb, x, (const void *)refine_kernel, pgrid, kRedBlock, d.p,
                        (const float *)d.e32, d.e32, (const uint8_t *)d.flags, g, 1,
                        (double *)nullptr);
-          if (d.n_pcopy > 0)
-            x = b.kernel(fb, x, (const void *)delta_kernel, dim3((d.n_pcopy + 255) / 256),
-                         dim3(256), (const double *)d.p, d.r32, d.e32, (const PCopy *)d.pcopy,
-                         d.n_pcopy, g.pitch);
           x = b.kernel(fb, x, (const void *)mixed_residual_kernel<true>, dim3(nb), kRedBlock,
                        (const double *)d.p, (const double *)d.rhs, (const uint8_t *)d.flags,
                        d.r32, g, c, d.st, d.partials, ty_int, nt_int, h_fine, r.itermax,
-                       r.strict_eps, 1, 1, h_fine, 0);
+                       r.strict_eps, 1, 1, h_fine, 0, (const PCopy *)d.pcopy, d.n_pcopy,
+                       d.e32);
         }
       }
       n = inode;
