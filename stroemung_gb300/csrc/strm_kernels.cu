@@ -2707,6 +2707,7 @@ struct BInst {
   StepState *st;
   double *partials;
   const PCopy *pcopy;
+  int npc;               // boundary cells of the copy (pcopy entries)
   Geom g;
   Consts c;
   Consts32 k32;
@@ -2748,26 +2749,19 @@ __global__ void __launch_bounds__(256)
                e.y / b.pgx, (apply && !fine && save) ? b.pw : nullptr);
 }
 
-__global__ void batch_delta_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab,
-                                   int n, int check, int fine) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const int2 e = tab[k];
-  const BInst &b = I[e.x];
-  if (!in_phase(b, fine) || (check && inst_stopped(b.st))) return;
-  delta_entry(b.p, b.r32, b.e32, b.pcopy[e.y], b.g.pitch);
-}
-
 template <int H, int TX, int TY>
 __global__ void __launch_bounds__(512)
     batch_tb_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int n,
-                    int skip_last_copy, int src_b) {
+                    int skip_last_copy, int src_b, int finish, int save) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 e = tab[blockIdx.x];
   const BInst &b = I[e.x];
   if (!b.solve || inst_stopped(b.st)) return;
+  // finish: the outer iteration's last launch also refines (as for one
+  // simulation, see sweep_plan)
   sor32_tb_tile<H, TX, TY>(src_b ? b.e32b : b.e32, src_b ? b.e32 : b.e32b, b.r32, b.flags, b.g,
-                           b.k32, e.y, b.tb_tiles_y, n, skip_last_copy, smem_raw);
+                           b.k32, e.y, b.tb_tiles_y, n, skip_last_copy, smem_raw,
+                           finish ? b.p : nullptr, (finish && save) ? b.pw : nullptr);
 }
 
 __global__ void __launch_bounds__(256)
@@ -2811,6 +2805,11 @@ __global__ void __launch_bounds__(256)
   const int2 e = tab[blockIdx.x];
   const BInst &b = I[e.x];
   if (!in_phase(b, fine) || (check == 1 && inst_stopped(b.st))) return;
+  // the member's boundary deltas, block-strided over its nb blocks (as
+  // mixed_residual_kernel does for one simulation)
+  const int nt = blockDim.x * blockDim.y;
+  for (int k = e.y * nt + threadIdx.y * blockDim.x + threadIdx.x; k < b.npc; k += b.nb * nt)
+    delta_entry(b.p, b.r32, b.e32, b.pcopy[k], b.g.pitch);
   mixed_residual_partial(b.p, b.rhs, b.flags, b.r32, b.g, b.c, b.partials, b.ty_int, b.nt_int,
                          b.strict, e.y, b.nb);
 }
@@ -2911,7 +2910,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   }
   const TbShape &shape = kTbShapes[sched];
   std::vector<BInst> inst(n);
-  std::vector<int2> t_res, t_ref, t_del, t_tb;
+  std::vector<int2> t_res, t_ref, t_tb;
   unsigned int itermax_all = 0;
   for (int i = 0; i < n; ++i) {
     const DevFields &d = mem[i].d;
@@ -2927,6 +2926,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     b.st = d.st;
     b.partials = d.partials;
     b.pcopy = d.pcopy;
+    b.npc = d.n_pcopy;
     b.g = r.g;
     b.c = r.c;
     b.k32 = consts32_of(r.c);
@@ -2947,15 +2947,13 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     if (r.itermax > itermax_all) itermax_all = r.itermax;
     for (int k = 0; k < b.nb; ++k) t_res.push_back(make_int2(i, k));
     for (int k = 0; k < b.pgx * pgy; ++k) t_ref.push_back(make_int2(i, k));
-    for (int k = 0; k < d.n_pcopy; ++k) t_del.push_back(make_int2(i, k));
     for (int k = 0; k < b.tb_tiles_y * tb_tiles_x; ++k) t_tb.push_back(make_int2(i, k));
   }
-  // device tables: instances, the four block tables, the batch state
+  // device tables: instances, the three block tables, the batch state
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_inst = 0, o_res = o_inst + al(sizeof(BInst) * n);
   const size_t o_ref = o_res + al(sizeof(int2) * (t_res.size() + 1));
-  const size_t o_del = o_ref + al(sizeof(int2) * (t_ref.size() + 1));
-  const size_t o_tb = o_del + al(sizeof(int2) * (t_del.size() + 1));
+  const size_t o_tb = o_ref + al(sizeof(int2) * (t_ref.size() + 1));
   const size_t o_bs = o_tb + al(sizeof(int2) * (t_tb.size() + 1));
   const size_t total = o_bs + al(sizeof(BatchState));
   char *dev = nullptr;
@@ -2963,7 +2961,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   bp->dev = dev;
   const BInst *d_inst = (const BInst *)(dev + o_inst);
   const int2 *d_res = (const int2 *)(dev + o_res), *d_ref = (const int2 *)(dev + o_ref);
-  const int2 *d_del = (const int2 *)(dev + o_del), *d_tb = (const int2 *)(dev + o_tb);
+  const int2 *d_tb = (const int2 *)(dev + o_tb);
   BatchState *d_bs = (BatchState *)(dev + o_bs);
   bp->state = d_bs;
   e = cudaMemset(dev, 0, total);
@@ -2972,8 +2970,6 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     e = cudaMemcpy(dev + o_res, t_res.data(), sizeof(int2) * t_res.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !t_ref.empty())
     e = cudaMemcpy(dev + o_ref, t_ref.data(), sizeof(int2) * t_ref.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && !t_del.empty())
-    e = cudaMemcpy(dev + o_del, t_del.data(), sizeof(int2) * t_del.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !t_tb.empty())
     e = cudaMemcpy(dev + o_tb, t_tb.data(), sizeof(int2) * t_tb.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -3010,7 +3006,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   if (b.err == cudaSuccess)
     b.err = cudaGraphAddEmptyNode(&nd, b.graph, part == 2 ? nullptr : pre.data(),
                                   part == 2 ? 0 : (size_t)n);
-  const int nres = (int)t_res.size(), nref = (int)t_ref.size(), ndel = (int)t_del.size();
+  const int nres = (int)t_res.size(), nref = (int)t_ref.size();
   const int ntb = (int)t_tb.size();
   cudaGraphConditionalHandle h{};
   if (b.err == cudaSuccess)
@@ -3019,12 +3015,8 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     cudaGraphConditionalHandle h_rep{};
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h_rep, b.graph, 0, cudaGraphCondAssignDefault);
-    const dim3 g_del((ndel + 255) / 256);
     nd = b.kernel(b.graph, nd, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
                   d_ref, 0, 0, 0, 0);
-    if (ndel > 0)
-      nd = b.kernel(b.graph, nd, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
-                    d_del, ndel, 0, 0);
     nd = b.kernel(b.graph, nd, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
                   d_inst, d_res, 0, 0);
     nd = b.kernel(b.graph, nd, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
@@ -3040,16 +3032,19 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
       int launches = 0;
+      // an even number of launches ends in the start buffer: the last one
+      // refines (as sweep_plan for one simulation)
+      const bool fused = ((m + shape.sweeps - 1) / shape.sweeps) % 2 == 0;
       for (int done = 0; done < m; done += shape.sweeps, ++launches) {
         const int cnt = m - done < shape.sweeps ? m - done : shape.sweeps;
+        const int last = done + cnt >= m ? 1 : 0;
         bn = b.kernel_smem(body, bn, batch_tb_fn(sched), dim3(ntb), dim3(512), tb_smem(shape),
-                           d_inst, d_tb, cnt, done + cnt >= m ? 1 : 0, launches & 1);
+                           d_inst, d_tb, cnt, last, launches & 1, (last && fused) ? 1 : 0,
+                           m > 1 ? 1 : 0);
       }
-      bn = b.kernel(body, bn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
-                    d_ref, 1, launches & 1, 0, m > 1 ? 1 : 0);
-      if (ndel > 0)
-        bn = b.kernel(body, bn, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
-                      d_del, ndel, 1, 0);
+      if (!fused)
+        bn = b.kernel(body, bn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock,
+                      d_inst, d_ref, 1, launches & 1, 0, m > 1 ? 1 : 0);
       bn = b.kernel(body, bn, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
                     d_inst, d_res, 1, 0);
       bn = b.kernel(body, bn, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
@@ -3072,9 +3067,6 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
                       d_ref, m);
         fn = b.kernel(ib, fn, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
                       d_ref, 0, 0, 1, 0);
-        if (ndel > 0)
-          fn = b.kernel(ib, fn, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
-                        d_del, ndel, 0, 1);
         fn = b.kernel(ib, fn, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
                       d_inst, d_res, 2, 1);
         cudaGraphConditionalHandle h_fine{};
@@ -3095,9 +3087,6 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
                          d_ref, color, color == 0 ? 1 : 0);
           x = b.kernel(fb, x, (const void *)batch_refine_kernel, dim3(nref), kRedBlock, d_inst,
                        d_ref, 1, 0, 1, 0);
-          if (ndel > 0)
-            x = b.kernel(fb, x, (const void *)batch_delta_kernel, g_del, dim3(256), d_inst,
-                         d_del, ndel, 1, 1);
           x = b.kernel(fb, x, (const void *)batch_residual_kernel, dim3(nres), kRedBlock,
                        d_inst, d_res, 1, 1);
           x = b.kernel(fb, x, (const void *)batch_finish_kernel, dim3(n), kRedBlock, d_inst, n,
