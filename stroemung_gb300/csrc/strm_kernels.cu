@@ -1336,6 +1336,59 @@ __device__ __forceinline__ uint8_t tb_code(uint8_t fl, int x, int y, const Geom 
   return edge_of(fl) != E_NONE ? edge_of(fl) : kFrozen;
 }
 
+// One row of a colour pass in the blocked sweeps: the lane's two compacted
+// cells at index i of colour row `ec`, with the other colour's rows above
+// (up), at (mid) and below (loaded here) rolling through registers.  P is
+// the row's parity (lx + c) & 1: a cell's neighbours along y in the other
+// colour are (j-1+P, j+P).
+template <int P, int W>
+__device__ __forceinline__ void tb_row(float *__restrict__ ec, const float *__restrict__ eo,
+                                       const float *__restrict__ svc,
+                                       const uint8_t *__restrict__ cc, int i, float2 &up,
+                                       float2 &mid, const Consts32 &k, bool copy) {
+  const float2 dn = *reinterpret_cast<const float2 *>(eo + i + W);
+  const unsigned int cd2 = *reinterpret_cast<const uint16_t *>(cc + i);  // both cells' codes
+  const float2 cur = *reinterpret_cast<const float2 *>(ec + i);
+  const float2 sv2 = *reinterpret_cast<const float2 *>(svc + i);
+  float lf0, rt0, lf1, rt1;
+  if (P) {
+    lf0 = mid.x;
+    rt0 = mid.y;
+    lf1 = mid.y;
+    rt1 = eo[i + 2];
+  } else {
+    lf0 = eo[i - 1];
+    rt0 = mid.x;
+    lf1 = mid.x;
+    rt1 = mid.y;
+  }
+  const float s0 = fmaf(k.omw, cur.x, fmaf(k.a, up.x + dn.x, fmaf(k.b, lf0 + rt0, sv2.x)));
+  const float s1 = fmaf(k.omw, cur.y, fmaf(k.a, up.y + dn.y, fmaf(k.b, lf1 + rt1, sv2.y)));
+  float2 res = make_float2(s0, s1);
+  if (cd2 != 0) {  // a boundary or frozen cell in the pair (rare)
+    const unsigned int cx = cd2 & 0xFFu, cy = cd2 >> 8;
+    res.x = cx == 0 ? s0 : (copy && cx != kFrozen ? sv2.x + copy_rb(cx, up.x, dn.x, lf0, rt0)
+                                                  : cur.x);
+    res.y = cy == 0 ? s1 : (copy && cy != kFrozen ? sv2.y + copy_rb(cy, up.y, dn.y, lf1, rt1)
+                                                  : cur.y);
+  }
+  *reinterpret_cast<float2 *>(ec + i) = res;
+  up = mid;
+  mid = dn;
+}
+
+// A warp's strip of up to S consecutive rows (nrows of them inside the
+// pass's region), starting with parity P0.
+template <int P0, int S, int W>
+__device__ __forceinline__ void tb_strip(float *ec, const float *eo, const float *svc,
+                                         const uint8_t *cc, int i0, int nrows, float2 &up,
+                                         float2 &mid, const Consts32 &k, bool copy) {
+  tb_row<P0, W>(ec, eo, svc, cc, i0, up, mid, k, copy);
+  if constexpr (S > 1) {
+    if (nrows > 1) tb_strip<P0 ^ 1, S - 1, W>(ec, eo, svc, cc, i0 + W, nrows - 1, up, mid, k, copy);
+  }
+}
+
 // One tile.  Extended rows are EY = 128 cells wide, so each colour row is 64
 // words and every lane owns two neighbouring compacted cells (j, j+1): the
 // four cells y = 4*lane .. 4*lane+3 of a row land as one pair per colour.
@@ -1425,40 +1478,13 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
     if (first <= hix) {
       float2 up = *reinterpret_cast<const float2 *>(eo + (first - 1) * W + j0);
       float2 mid = *reinterpret_cast<const float2 *>(eo + first * W + j0);
-#pragma unroll
-      for (int r = 0; r < STRIP; ++r) {
-        const int lx = first + r;
-        if (lx > hix) break;
-        const int p = (lx + c) & 1;
-        const int i = lx * W + j0;
-        const float2 dn = *reinterpret_cast<const float2 *>(eo + i + W);
-        const uchar2 cd = *reinterpret_cast<const uchar2 *>(cc + i);
-        const float2 cur = *reinterpret_cast<const float2 *>(ec + i);
-        const float2 sv2 = *reinterpret_cast<const float2 *>(svc + i);
-        // neighbours along y of cell j: (j-1+p, j+p) in the other colour
-        float lf0, rt0, lf1, rt1;
-        if (p) {
-          lf0 = mid.x;
-          rt0 = mid.y;
-          lf1 = mid.y;
-          rt1 = eo[i + 2];
-        } else {
-          lf0 = eo[i - 1];
-          rt0 = mid.x;
-          lf1 = mid.x;
-          rt1 = mid.y;
-        }
-        const float s0 = fmaf(k.omw, cur.x, fmaf(k.a, up.x + dn.x, fmaf(k.b, lf0 + rt0, sv2.x)));
-        const float s1 = fmaf(k.omw, cur.y, fmaf(k.a, up.y + dn.y, fmaf(k.b, lf1 + rt1, sv2.y)));
-        float2 res = make_float2(cd.x == 0 ? s0 : cur.x, cd.y == 0 ? s1 : cur.y);
-        if ((cd.x | cd.y) != 0 && copy) {  // boundary cells of this pair (rare)
-          if (cd.x != 0 && cd.x != kFrozen) res.x = sv2.x + copy_rb(cd.x, up.x, dn.x, lf0, rt0);
-          if (cd.y != 0 && cd.y != kFrozen) res.y = sv2.y + copy_rb(cd.y, up.y, dn.y, lf1, rt1);
-        }
-        *reinterpret_cast<float2 *>(ec + i) = res;
-        up = mid;
-        mid = dn;
-      }
+      // row parity alternates along the strip: one warp-uniform branch picks
+      // the variant whose rows know their parity at compile time
+      const int i0 = first * W + j0, nrows = hix - first + 1;
+      if ((first + c) & 1)
+        tb_strip<1, STRIP, W>(ec, eo, svc, cc, i0, nrows, up, mid, k, copy);
+      else
+        tb_strip<0, STRIP, W>(ec, eo, svc, cc, i0, nrows, up, mid, k, copy);
     }
     __syncthreads();
   }
