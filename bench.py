@@ -192,6 +192,12 @@ def run_reference(args):
 
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
 
+# DRAM traffic from the committed ncu captures of this workload (bytes):
+# one FP64 iteration (red 88.5 + 20.2 MB, black 72.1 + 1.0 MB, edge list
+# 2.8 MB) and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
+SOR_ITERATION_TRAFFIC = (88.5 + 20.2 + 72.1 + 1.0 + 2.8) * 1e6
+SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
+
 
 def config_dict(args):
     return {"workload": "channel 4096x1024, 64 rectangles (seed 0), Re 400, tau 0.5, "
@@ -335,7 +341,13 @@ def mixed_block(args, grid, fp64_ms_step, peak):
                     "plain run by rounding only, and both errors grow at the flow's rate"},
         "roofline_fp32_sweep": {"achieved": sw_bytes / t_sw / 1e9, "peak": peak, "unit": "GB/s",
                                 "frac": sw_bytes / t_sw / 1e9 / peak, "us_per_sweep": t_sw * 1e6,
-                                "algorithmic_bytes": sw_bytes},
+                                "algorithmic_bytes": sw_bytes,
+                                "traffic": SWEEP_TRAFFIC,
+                                "traffic_note": "ncu dram__bytes read+write of one blocked "
+                                                "launch (4 sweeps) divided by 4, cold cache "
+                                                "(profiles/sor32_blocked_sweeps_channel_"
+                                                "4096x1024.md): the sweeps read e, s and the "
+                                                "flags once per launch"},
         "dtype": "f32 stencil and sweeps, f64 norm/refinement/dt",
     }
 
@@ -919,7 +931,14 @@ def main():
                      "+ the previous iteration's red residual and stop test)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes": sor_bytes, "traffic": None},
+                     "algorithmic_bytes": sor_bytes,
+                     # DRAM bytes of one iteration's kernels (red, black, edge
+                     # list) in one ncu capture of this workload, cold cache:
+                     # profiles/fp64_sor_kernels_channel_4096x1024.md
+                     "traffic": SOR_ITERATION_TRAFFIC,
+                     "traffic_note": "ncu dram__bytes read+write of one iteration's kernels, "
+                                     "cold cache; each colour pass touches the whole of p and "
+                                     "rhs (the colours interleave within cache lines)"},
         "fp64": {"ops_per_iteration": ops, "achieved_tflops": ops / t_iter / 1e12,
                  "dgemm_tflops_measured": fp64_peak,
                  "note": "FP64 pipe operations (add, mul, fma each 1) of the solve"},
