@@ -119,9 +119,11 @@ struct ConvShape {
 // *err and the CTA still releases its TMEM.
 template <int BN>
 struct ConvPipe {
-  // narrow tiles keep fewer stages so that more CTAs (more gathering warps)
-  // share an SM
-  static constexpr int S = BN <= 32 ? 2 : (BN <= 64 ? 3 : 4);  // stages
+  // stages: the gather is the bound, so fewer stages (more CTAs, more
+  // gathering warps per SM) win except at 64 channels; measured on the
+  // U-Net forward at 4096 x 1024 (2/3/2: 4.33 ms, 2/3/3: 4.63, 2/3/4: 4.89,
+  // 2/2/2-3: 4.75-4.78, 3-4/3-4/4: 5.4-6.2)
+  static constexpr int S = BN <= 32 ? 2 : (BN <= 64 ? 3 : 2);
   static constexpr int LAG = S - 1 < 2 ? S - 1 : 2;            // gathers in flight per thread
   static constexpr int A_BYTES = GM * 128;          // 128 rows x 64 BF16
   static constexpr int B_BYTES = BN * 128;
