@@ -193,9 +193,9 @@ def run_reference(args):
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
 
 # DRAM traffic from the committed ncu captures of this workload (bytes):
-# one FP64 iteration (red 88.5 + 20.2 MB, black 72.1 + 1.0 MB, edge list
+# one FP64 iteration (red 88.4 + 20.1 MB, black 72.1 + 1.0 MB, edge list
 # 2.8 MB) and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
-SOR_ITERATION_TRAFFIC = (88.5 + 20.2 + 72.1 + 1.0 + 2.8) * 1e6
+SOR_ITERATION_TRAFFIC = (88.4 + 20.1 + 72.1 + 1.0 + 2.8) * 1e6
 SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
 
 
@@ -840,8 +840,9 @@ def main():
     iters = [s[0] for s in stats]
     if arith == ARITH_FAST:
         # boundary pass, F/G+RHS; copy + first red pass; per iteration black
-        # pass, edge list, copy, red pass; rollback; pressure range, velocity
-        launches = sum(2 + 2 + 4 * k + 1 + 2 for k in iters)
+        # pass (+ half the next copy), edge list (+ the other half), red
+        # pass; rollback; pressure range, velocity
+        launches = sum(2 + 2 + 3 * k + 1 + 2 for k in iters)
     else:
         # per iteration copy, red, black, residual
         launches = sum(2 + 4 * k + 2 for k in iters)
@@ -865,9 +866,9 @@ def main():
     # FP64 pipe work of one iteration: update on fluid cells + residual on all
     fluid = float((grid["kind"][1:-1, 1:-1] == 0).sum())
     # FAST: red update + the previous iteration's residual 7 and black update
-    # + residual 8 per fluid cell of the colour, the residual of every other
+    # + residual 7 per fluid cell of the colour, the residual of every other
     # interior cell 6 (the red fluid cells next to a wall pay 6 more)
-    ops = (7.5 * fluid + 6 * (interior - fluid)) if arith == ARITH_FAST \
+    ops = (7.0 * fluid + 6 * (interior - fluid)) if arith == ARITH_FAST \
         else (17 * fluid + 20 * interior)
     fp64_peak = None
     try:
@@ -927,8 +928,9 @@ def main():
                     "rule": "reference stop rule; no step reached eps" if not any(
                         s[3] for s in stats) else "reference stop rule"},
         "roofline": {"bound": "hbm", "kernel": "one red-black SOR iteration of the solve graph "
-                     "(black pass + its residual, edge-list residual, pressure copy, red pass "
-                     "+ the previous iteration's red residual and stop test)",
+                     "(black pass + its residual + half the pressure copy, edge-list residual "
+                     "+ the other half, red pass + the previous iteration's red residual and "
+                     "stop test)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": sor_bytes,

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
 #include <vector>
@@ -205,6 +206,15 @@ int classify_and_compile(strm_sim *s, long long *bad_out) {
     s->pcopy_cap = (int)pc.size() + 1024;
     CK(cudaMalloc(&s->d.pcopy, sizeof(PCopy) * s->pcopy_cap));
   }
+  // black-coloured copy targets ((x + y) odd: red sources) first, for the
+  // FAST red-black solve's split copy (the copies are independent: every
+  // source is a fluid cell)
+  const auto black_target = [&](const PCopy &c) {
+    return (((long long)(c.off / g.pitch) + c.off % g.pitch) & 1) != 0;
+  };
+  const int n_pc_b = (int)(std::stable_partition(pc.begin(), pc.end(), black_target) - pc.begin());
+  std::vector<uint8_t> copied((size_t)g.nx * g.pitch, 0);
+  for (const PCopy &c : pc) copied[(size_t)c.off] = 1;
   // solver classes and the edge list of the FAST red-black solve
   std::vector<uint8_t> cls(flags.size(), 2);
   std::vector<unsigned int> elist;
@@ -220,20 +230,35 @@ int classify_and_compile(strm_sim *s, long long *bad_out) {
       cls[i] = edge ? 1 : 0;
       if (edge && ((x + y) & 1) == 0) elist.push_back(off);
     }
+  // which stencil points of each listed cell are copied boundary cells
+  std::vector<uint8_t> emask(elist.size());
+  for (size_t i = 0; i < elist.size(); ++i) {
+    const size_t o = elist[i];
+    emask[i] = (uint8_t)(copied[o] | copied[o - g.pitch] << 1 | copied[o + g.pitch] << 2 |
+                         copied[o - 1] << 3 | copied[o + 1] << 4);
+  }
   if ((int)elist.size() > s->edge_cap) {
     if (s->d.edge_list) cudaFree(s->d.edge_list);
+  if (s->d.edge_mask) cudaFree(s->d.edge_mask);
+    if (s->d.edge_mask) cudaFree(s->d.edge_mask);
     s->d.edge_list = nullptr;
+    s->d.edge_mask = nullptr;
     s->edge_cap = (int)elist.size() + 1024;
     CK(cudaMalloc(&s->d.edge_list, sizeof(unsigned int) * s->edge_cap));
+    CK(cudaMalloc(&s->d.edge_mask, s->edge_cap));
   }
   s->d.n_edge = (int)elist.size();
-  if (!elist.empty())
+  if (!elist.empty()) {
     CK(cudaMemcpyAsync(s->d.edge_list, elist.data(), sizeof(unsigned int) * elist.size(),
                        cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->d.edge_mask, emask.data(), emask.size(), cudaMemcpyHostToDevice,
+                       s->stream));
+  }
   CK(cudaMemcpy2DAsync(s->d.cls, g.pitch, cls.data(), g.ny, g.ny, g.nx, cudaMemcpyHostToDevice,
                        s->stream));
   s->d.n_bc = (int)prog.size();
   s->d.n_pcopy = (int)pc.size();
+  s->d.n_pcopy_b = n_pc_b;
   if (!prog.empty())
     CK(cudaMemcpyAsync(s->d.bc, prog.data(), sizeof(BcEntry) * prog.size(),
                        cudaMemcpyHostToDevice, s->stream));
@@ -254,6 +279,7 @@ void free_sim(strm_sim *s) {
   if (s->d.bc_val) cudaFree(s->d.bc_val);
   if (s->d.pcopy) cudaFree(s->d.pcopy);
   if (s->d.edge_list) cudaFree(s->d.edge_list);
+  if (s->d.edge_mask) cudaFree(s->d.edge_mask);
   if (s->rgba) cudaFree(s->rgba);
   if (s->h_st) cudaFreeHost(s->h_st);
   if (s->h_log) cudaFreeHost(s->h_log);

@@ -10,9 +10,11 @@
 //     residual_kernel  residual norm, stop test, sets the WHILE condition
 //   fast arithmetic: pcopy_kernel, sor_red_res_kernel (first red pass), then
 //   WHILE(solve not done):
-//     sor_black_res_kernel  black pass + the black cells' residual
-//     edge_res_kernel       residual of the cells next to boundary values
-//     pcopy_save_kernel     boundary copy of the next iteration (saved)
+//     sor_black_res_kernel  black pass + the black cells' residual; saves the
+//                           boundary values, copies the black-coloured ones
+//                           for the next iteration
+//     edge_res_kernel       residual of the cells next to boundary values;
+//                           copies the red-coloured boundary cells
 //     sor_red_res_kernel    red pass of the next iteration + this one's red
 //                           residual, norm, stop test
 //   sor_rollback_kernel  undoes the next iteration's copy and red pass
@@ -27,6 +29,7 @@
 #include <cooperative_groups.h>
 #include <float.h>
 
+#include <algorithm>
 #include <initializer_list>
 
 #include "strm_kernels.cuh"
@@ -644,15 +647,74 @@ __device__ __forceinline__ PassCells pass_cells(int vb0, int stride, int nvb, in
   return pc;
 }
 
+// Block sums of the FAST solve passes: the threads' values go to shared
+// memory and warp 0 adds them (nt/32 - 1 additions per lane, then the
+// shuffle tree).  That is 12 FP64 additions by one warp per block of 256
+// threads, where block_reduce's shuffle tree costs 5 in every warp: the
+// passes are bound by the FP64 pipe.  Fixed order (deterministic); at most
+// 256 threads, a multiple of 32; the sums are valid in thread 0.
+template <bool TWO>
+__device__ __forceinline__ void block_sum_pass(double &a, double &b) {
+  __shared__ double sa[256];
+  __shared__ double sb[TWO ? 256 : 1];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nt = blockDim.x * blockDim.y;
+  sa[tid] = a;
+  if (TWO) sb[tid] = b;
+  __syncthreads();
+  if (tid < 32) {
+    double s = sa[tid], s1 = TWO ? sb[tid] : 0.0;
+    for (int k = tid + 32; k < nt; k += 32) {
+      s += sa[k];
+      if (TWO) s1 += sb[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (TWO) s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    a = s;
+    b = s1;
+  }
+}
+
 // The black pass of a FAST red-black iteration fused with the residual of the
-// black fluid cells: with t = (pe+pw)/dx^2 + (ps+pn)/dy^2 - rhs from the red
-// values, p_new = (1-omega) p + omega t / (2/dx^2+2/dy^2), and since the four
-// (red) neighbours are final the cell's residual is r = t - 2(1/dx^2+1/dy^2)
-// p_new.  Its sums of r^2 (and r when mean-free) go to partials_b[blockIdx.x].
+// black fluid cells.  With t = (pe+pw)/dx^2 + (ps+pn)/dy^2 - rhs from the red
+// values and r0 = t - 2(1/dx^2+1/dy^2) p the residual before the update, the
+// update is p_new = p + omega r0 / (2(1/dx^2+1/dy^2)) (the reference update,
+// src/simulation.rs:260-271, rearranged), and since the four (red) neighbours
+// are final the cell's residual afterwards is r = (1-omega) r0.  The pass
+// sums r0^2 (and r0 when MEAN_FREE) and scales the block sums by (1-omega)^2
+// (and 1-omega): 7 FP64 operations per cell.  The sums go to
+// partials_b[blockIdx.x].
+//
+// In the solve the pass also starts the boundary copy of iteration k+1
+// (src/grid/mod.rs:343-412; only when k < itermax, as the copy runs only
+// before another iteration): every copied boundary cell's value of
+// iteration k is saved into pw (the edge pass reads the residual's stale
+// boundary values from there, the rollback restores them), and the
+// black-coloured boundary cells pc[0..npc_b) get their new values here.
+// Their sources are red cells, final since the red pass, and no black
+// cell's stencil contains a black-coloured cell, so nothing in this pass
+// reads what the copy writes.  npc = 0: no copy (the phase entry points).
+template <bool MEAN_FREE>
 __global__ void __launch_bounds__(256)
-    sor_black_res_kernel(double *__restrict__ p, const double *__restrict__ rhs,
-                         const uint8_t *__restrict__ flags, Geom g, Consts c,
-                         double *__restrict__ partials_b, int mean_free, int gx, int nvb) {
+    sor_black_res_kernel(double *__restrict__ p, double *__restrict__ pw,
+                         const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
+                         Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
+                         const PCopy *__restrict__ pc, int npc_b, int npc, const StepState *st,
+                         unsigned int itermax) {
+  {
+    const int nt = blockDim.x * blockDim.y;
+    int k = blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x;
+    if (k < npc) {
+      const bool copy = st->sor_iters + 1 < itermax;
+      for (; k < npc; k += gridDim.x * nt) {
+        const PCopy e = pc[k];
+        pw[e.off] = p[e.off];
+        if (copy && k < npc_b) pcopy_one(p, e, g.pitch);
+      }
+    }
+  }
   double acc = 0.0, acc1 = 0.0;
   for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
     const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 1, g);
@@ -674,22 +736,21 @@ __global__ void __launch_bounds__(256)
     for (int u = 0; u < kPassUnroll; ++u) {
       if (!cells.ok[u] || f[u] != 0) continue;
       const double t = fma(pe[u] + pw[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
-      const double pnew = fma(c.one_minus_w, pc[u], c.middle * t);
-      p[cells.o[u]] = pnew;
-      const double r = fma(-c.two_r_sum, pnew, t);
-      acc = fma(r, r, acc);
-      if (mean_free) acc1 += r;
+      const double r0 = fma(-c.two_r_sum, pc[u], t);
+      p[cells.o[u]] = fma(c.middle, r0, pc[u]);
+      acc = fma(r0, r0, acc);
+      if (MEAN_FREE) acc1 += r0;
     }
   }
-  const double bsum = block_reduce(acc, OpAdd(), 0.0);
-  if (mean_free) {
-    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      partials_b[2 * blockIdx.x] = bsum;
-      partials_b[2 * blockIdx.x + 1] = bsum1;
+  block_sum_pass<MEAN_FREE>(acc, acc1);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const double q = c.one_minus_w;
+    if (MEAN_FREE) {
+      partials_b[2 * blockIdx.x] = acc * (q * q);
+      partials_b[2 * blockIdx.x + 1] = acc1 * q;
+    } else {
+      partials_b[blockIdx.x] = acc * (q * q);
     }
-  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
-    partials_b[blockIdx.x] = bsum;
   }
 }
 
@@ -876,15 +937,21 @@ __global__ void __launch_bounds__(256)
 //   * red fluid cells next to a non-fluid cell (class 1) and the non-fluid
 //     interior cells read boundary values, which the copy before iteration
 //     k+1 changes (src/grid/mod.rs:343-412; the norm of iteration k uses the
-//     stale ones).  edge_res_kernel sums those cells from a list, after the
-//     black pass of k and before that copy;
+//     stale ones).  edge_res_kernel sums those cells from a list after the
+//     black pass of k, reading the boundary values of k from the copy the
+//     black pass saved;
 //   * the stop itself: when iteration k stops the solve, the red pass and
 //     the boundary copy of k+1 have run.  Both saved the values they
 //     overwrote (in pw), and sor_rollback_kernel puts them back, so the
 //     solve ends on iteration k's pressure, boundary values included.
+// The copy of iteration k+1 is split by the colour of the boundary cell: a
+// boundary cell's sources are its fluid neighbours, all of the other
+// colour, so the black-coloured ones (red sources) are copied in the black
+// pass of k and the red-coloured ones (black sources) in the edge pass.
 // Iteration k+1's red pass and copy run only when k < itermax.
-// Per iteration: black pass (+ its residual), edge list, copy, red pass (+
-// the stop test), instead of copy, red, black, residual.
+// Per iteration: black pass (+ its residual, the save and half the copy),
+// edge list (+ the other half), red pass (+ the stop test), instead of
+// copy, red, black, residual.
 // ------------------------------------------------------------------------
 
 // Solver class of a cell (per cell, pitch layout): 0 fluid interior cell with
@@ -894,65 +961,96 @@ enum : uint8_t { CLS_FLUID = 0, CLS_FLUID_EDGE = 1, CLS_OTHER = 2 };
 
 template <bool MEAN_FREE>
 __device__ __forceinline__ void store_sums(double acc, double acc1, double *partials) {
-  const double bsum = block_reduce(acc, OpAdd(), 0.0);
-  if (MEAN_FREE) {
-    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      partials[2 * blockIdx.x] = bsum;
-      partials[2 * blockIdx.x + 1] = bsum1;
+  block_sum_pass<MEAN_FREE>(acc, acc1);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (MEAN_FREE) {
+      partials[2 * blockIdx.x] = acc;
+      partials[2 * blockIdx.x + 1] = acc1;
+    } else {
+      partials[blockIdx.x] = acc;
     }
-  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
-    partials[blockIdx.x] = bsum;
   }
 }
 
-// The norm from three partial arrays (black pass, edge list, red pass), in
-// that fixed order.
+// The norm from three partial arrays (black pass, edge list, red pass): each
+// thread adds its entries of the three arrays in that order, then one block
+// sum — one chain of loads and one barrier pair on the critical path of the
+// iteration instead of three.
 __device__ __forceinline__ double finish_norm3(const double *pa, int na, const double *pb, int nb,
                                                const double *pc, int nc, bool mean_free,
                                                double fluid_cells) {
-  const int st = mean_free ? 2 : 1;
-  const double s2 = reduce_partials(pa, na, st, 0, OpAdd(), 0.0) +
-                    reduce_partials(pb, nb, st, 0, OpAdd(), 0.0) +
-                    reduce_partials(pc, nc, st, 0, OpAdd(), 0.0);
-  if (!mean_free) return s2 / fluid_cells;
-  const double s1 = reduce_partials(pa, na, 2, 1, OpAdd(), 0.0) +
-                    reduce_partials(pb, nb, 2, 1, OpAdd(), 0.0) +
-                    reduce_partials(pc, nc, 2, 1, OpAdd(), 0.0);
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nt = blockDim.x * blockDim.y;
+  double s2 = 0.0, s1 = 0.0;
+  if (!mean_free) {
+#pragma unroll 4
+    for (int k = tid; k < na; k += nt) s2 += __ldcg(pa + k);
+#pragma unroll 4
+    for (int k = tid; k < nb; k += nt) s2 += __ldcg(pb + k);
+#pragma unroll 4
+    for (int k = tid; k < nc; k += nt) s2 += __ldcg(pc + k);
+    block_sum_pass<false>(s2, s1);
+    return s2 / fluid_cells;
+  }
+#pragma unroll 4
+  for (int k = tid; k < na; k += nt) {
+    s2 += __ldcg(pa + 2 * k);
+    s1 += __ldcg(pa + 2 * k + 1);
+  }
+#pragma unroll 4
+  for (int k = tid; k < nb; k += nt) {
+    s2 += __ldcg(pb + 2 * k);
+    s1 += __ldcg(pb + 2 * k + 1);
+  }
+#pragma unroll 4
+  for (int k = tid; k < nc; k += nt) {
+    s2 += __ldcg(pc + 2 * k);
+    s1 += __ldcg(pc + 2 * k + 1);
+  }
+  block_sum_pass<true>(s2, s1);
   return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
 }
 
-// Residual sums of the listed cells (offsets, x-major): the non-fluid
-// interior cells (skipped by the fluid norms) and the red class-1 cells.
+// Residual sums of the listed cells (offsets, x-major) after the black pass
+// of iteration k: the non-fluid interior cells (skipped by the fluid norms)
+// and the red class-1 cells.  Their stencils read boundary values of
+// iteration k, which the black pass saved into pw; mask[i] says which of
+// the five stencil points (bit 0 the cell, 1 west, 2 east, 3 north, 4
+// south) are copied boundary cells, read from pw.  Blocks nres and up
+// write the boundary copy of iteration k+1 (when k < itermax) for the
+// red-coloured boundary cells pc[npc_b..npc) meanwhile: their sources are
+// black cells, final after the black pass, and the residuals read those
+// boundary cells from pw, not p.  Blocks 0..nres-1 store their sums in
+// partials_e.
 template <bool FLUID, bool MEAN_FREE>
 __global__ void __launch_bounds__(256)
-    edge_res_kernel(const double *__restrict__ p, const double *__restrict__ rhs,
-                    const uint8_t *__restrict__ flags, const unsigned int *__restrict__ list,
-                    int n, Geom g, Consts c, double *__restrict__ partials_e) {
-  double acc = 0.0, acc1 = 0.0;
+    edge_res_kernel(double *__restrict__ p, const double *__restrict__ pw,
+                    const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
+                    const unsigned int *__restrict__ list, const uint8_t *__restrict__ mask,
+                    int n, int nres, Geom g, Consts c, double *__restrict__ partials_e,
+                    const PCopy *__restrict__ pc, int npc_b, int npc, const StepState *st,
+                    unsigned int itermax) {
   const int nt = blockDim.x * blockDim.y;
-  for (int i = blockIdx.x * nt + threadIdx.x + threadIdx.y * blockDim.x; i < n;
-       i += gridDim.x * nt) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  if ((int)blockIdx.x >= nres) {
+    const int b = blockIdx.x - nres, nb = gridDim.x - nres;
+    if (npc_b + b * nt + tid < npc && st->sor_iters + 1 < itermax)
+      for (int k = npc_b + b * nt + tid; k < npc; k += nb * nt) pcopy_one(p, pc[k], g.pitch);
+    return;
+  }
+  double acc = 0.0, acc1 = 0.0;
+  for (int i = blockIdx.x * nt + tid; i < n; i += nres * nt) {
     const size_t o = list[i];
+    const unsigned int m = mask[i];
     if (FLUID && flags[o] != 0) continue;
-    const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1], p[o + 1],
-                                        rhs[o], c);
+    const double *s0 = (m & 1u) ? pw : p, *sw = (m & 2u) ? pw : p, *se = (m & 4u) ? pw : p;
+    const double *sn = (m & 8u) ? pw : p, *ss = (m & 16u) ? pw : p;
+    const double r = residual_of<false>(s0[o], sw[o - g.pitch], se[o + g.pitch], sn[o - 1],
+                                        ss[o + 1], rhs[o], c);
     acc = fma(r, r, acc);
     if (MEAN_FREE) acc1 += r;
   }
   store_sums<MEAN_FREE>(acc, acc1, partials_e);
-}
-
-// The boundary copy before iteration k+1 (only when k < itermax), saving the
-// values it overwrites into pw.
-__global__ void pcopy_save_kernel(double *p, double *pw, const PCopy *pc, int n, int pitch,
-                                  const StepState *st, unsigned int itermax) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const PCopy c = pc[k];  // loaded together with the iteration count
-  if (st->sor_iters + 1 >= itermax) return;
-  pw[c.off] = p[c.off];
-  pcopy_one(p, c, pitch);
 }
 
 // Red pass.  mode 0: update only (the first red pass of a solve, and the
@@ -1674,15 +1772,15 @@ __device__ __forceinline__ void mixed_residual_partial(
   else
     mixed_residual_sum<true, true>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
                                    &acc1);
-  const double bsum = block_reduce(acc, OpAdd(), 0.0);
   if (mean_free) {
-    const double bsum1 = block_reduce(acc1, OpAdd(), 0.0);
+    block_sum_pass<true>(acc, acc1);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-      partials[2 * bid] = bsum;
-      partials[2 * bid + 1] = bsum1;
+      partials[2 * bid] = acc;
+      partials[2 * bid + 1] = acc1;
     }
-  } else if (threadIdx.x == 0 && threadIdx.y == 0) {
-    partials[bid] = bsum;
+  } else {
+    block_sum_pass<false>(acc, acc1);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partials[bid] = acc;
   }
 }
 
@@ -1958,17 +2056,23 @@ int edge_blocks(int n) {
   return b < 1 ? 1 : b;
 }
 
+// Blocks of the edge pass that write the red-coloured boundary copies.
+static int copy_blocks(const DevFields &d) {
+  const int n = d.n_pcopy - d.n_pcopy_b;
+  return n > 0 ? std::min((n + 255) / 256, 256) : 0;
+}
+
 // Kernel choices of the FAST red-black solve for a stop-rule setting.
 struct FastSolveKernels {
-  const void *red_graph, *red_eager, *edge;
-  int mean_free;
+  const void *red_graph, *red_eager, *black, *edge;
 };
 
 static FastSolveKernels fast_solve_kernels(int strict) {
   const bool fluid = (strict & STOP_FLUID_NORM) != 0;
   const bool mf = fluid && (strict & STOP_MEAN_FREE) != 0;
   FastSolveKernels k;
-  k.mean_free = mf ? 1 : 0;
+  k.black = mf ? (const void *)sor_black_res_kernel<true>
+               : (const void *)sor_black_res_kernel<false>;
   k.red_graph = mf ? (const void *)sor_red_res_kernel<true, true>
                    : (const void *)sor_red_res_kernel<true, false>;
   k.red_eager = mf ? (const void *)sor_red_res_kernel<false, true>
@@ -2228,8 +2332,15 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
     sor_red_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
         d.p, d.pw, d.rhs, d.cls, r.g, r.c, d.st, d.partials_r, d.partials_b, bb, d.partials_e, 1,
         (int)sgrid.x, nvb, r.itermax, r.strict_eps, 0, 0);
-    sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.partials_b,
-                                                  mean_free, (int)sgrid.x, nvb);
+    // (npc = 0: the pass makes no boundary copy here)
+    if (mean_free)
+      sor_black_res_kernel<true><<<bb, kRedBlock, 0, s>>>(
+          d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
+          d.st, r.itermax);
+    else
+      sor_black_res_kernel<false><<<bb, kRedBlock, 0, s>>>(
+          d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
+          d.st, r.itermax);
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
                                                            d.partials, ty, nt, 0, r.itermax,
                                                            r.strict_eps, RES_NORM, d.partials_b,
@@ -2358,7 +2469,7 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       // norm (see sor_red_res_kernel); the same launches as the graph
       const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
       const int bb = black_pass_blocks(g);
-      const int nbe = edge_blocks(d.n_edge);
+      const int nbe = edge_blocks(d.n_edge), ncb = copy_blocks(d);
       int gx = (int)sgrid.x;
       unsigned int itermax = r.itermax;
       int strict = r.strict_eps, mode = 0;
@@ -2378,19 +2489,23 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
         return e;
       mode = 1;
       const unsigned int *list = d.edge_list;
-      const uint8_t *flags = d.flags;
-      int n_edge = d.n_edge;
-      void *edge_args[] = {&p, &rhs, &flags, &list, &n_edge, &gg, &cc, &prt_e};
+      const uint8_t *flags = d.flags, *emask = d.edge_mask;
+      const PCopy *pcl = d.pcopy;
+      int n_edge = d.n_edge, nres = nbe, npc_b = d.n_pcopy_b, npc = d.n_pcopy;
+      const StepState *cst = d.st;
+      void *edge_args[] = {&p,     &pw,  &rhs,   &flags, &list, &emask,  &n_edge, &nres,
+                           &gg,    &cc,  &prt_e, &pcl,   &npc_b, &npc,   &cst,    &itermax};
+      double *prt_bw = d.partials_b;
+      int nvb_b = nbb;
+      void *black_args[] = {&p,   &pw,  &rhs,   &flags, &gg,  &cc,      &prt_bw, &gx,
+                            &nvb_b, &pcl, &npc_b, &npc,  &cst, &itermax};
       while (!done) {
-        sor_black_res_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, g, c, d.partials_b,
-                                                      fk.mean_free, gx, nbb);
-        if ((e = cudaLaunchKernel(fk.edge, dim3(nbe), kRedBlock, edge_args, 0, s)) !=
+        if ((e = cudaLaunchKernel(fk.black, dim3(bb), kRedBlock, black_args, 0, s)) !=
             cudaSuccess)
           return e;
-        if (d.n_pcopy > 0)
-          pcopy_save_kernel<<<(d.n_pcopy + 255) / 256, 256, 0, s>>>(d.p, d.pw, d.pcopy,
-                                                                    d.n_pcopy, g.pitch, d.st,
-                                                                    r.itermax);
+        if ((e = cudaLaunchKernel(fk.edge, dim3(nbe + ncb), kRedBlock, edge_args, 0, s)) !=
+            cudaSuccess)
+          return e;
         if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
             cudaSuccess)
           return e;
@@ -2659,18 +2774,16 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
       if (r.arith) {
-        const int nbe = edge_blocks(d.n_edge);
-        bn = b.kernel(body, nullptr, (const void *)sor_black_res_kernel, dim3(bb), kRedBlock, d.p,
+        const int nbe = edge_blocks(d.n_edge), ncb = copy_blocks(d);
+        bn = b.kernel(body, nullptr, fk.black, dim3(bb), kRedBlock, d.p, d.pw,
                       (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
-                      fk.mean_free, (int)sgrid.x, nbb);
-        bn = b.kernel(body, bn, fk.edge, dim3(nbe), kRedBlock, (const double *)d.p,
+                      (int)sgrid.x, nbb, (const PCopy *)d.pcopy, d.n_pcopy_b, d.n_pcopy,
+                      (const StepState *)d.st, r.itermax);
+        bn = b.kernel(body, bn, fk.edge, dim3(nbe + ncb), kRedBlock, d.p, (const double *)d.pw,
                       (const double *)d.rhs, (const uint8_t *)d.flags,
-                      (const unsigned int *)d.edge_list, d.n_edge, g, c, d.partials_e);
-        if (d.n_pcopy > 0)
-          bn = b.kernel(body, bn, (const void *)pcopy_save_kernel,
-                        dim3((d.n_pcopy + 255) / 256), dim3(256), d.p, d.pw,
-                        (const PCopy *)d.pcopy, d.n_pcopy, g.pitch, (const StepState *)d.st,
-                        r.itermax);
+                      (const unsigned int *)d.edge_list, (const uint8_t *)d.edge_mask, d.n_edge,
+                      nbe, g, c, d.partials_e, (const PCopy *)d.pcopy, d.n_pcopy_b, d.n_pcopy,
+                      (const StepState *)d.st, r.itermax);
         bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
                       (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
                       (const double *)d.partials_b, bb, (const double *)d.partials_e, nbe,

@@ -27,14 +27,18 @@ struct DevFields {
   BcEntry *bc;            // compiled boundary program
   double *bc_val;         // its gathered values
   int n_bc;
-  PCopy *pcopy;
+  PCopy *pcopy;           // boundary pressure copies, black-coloured targets first
   int n_pcopy;
+  int n_pcopy_b;          // how many targets are black-coloured ((x + y) odd)
   // FAST red-black solve: solver class per cell (0 fluid with fluid
   // neighbours, 1 fluid next to a non-fluid cell, 2 other), the cells whose
-  // residual the edge pass sums (offsets, x-major), and the partial sums of
-  // the red pass and of the edge pass
+  // residual the edge pass sums (offsets, x-major) with, per cell, which of
+  // its five stencil points are copied boundary cells (bit 0 the cell, 1
+  // west, 2 east, 3 north, 4 south), and the partial sums of the red pass
+  // and of the edge pass
   uint8_t *cls;
   unsigned int *edge_list;
+  uint8_t *edge_mask;
   int n_edge;
   double *partials_r;
   double *partials_e;
