@@ -840,9 +840,9 @@ def main():
     iters = [s[0] for s in stats]
     if arith == ARITH_FAST:
         # boundary pass, F/G+RHS; copy + first red pass; per iteration black
-        # pass (+ half the next copy), edge list (+ the other half), red
-        # pass; rollback; pressure range, velocity
-        launches = sum(2 + 2 + 3 * k + 1 + 2 for k in iters)
+        # pass (+ half the next copy) and red pass (+ the other half);
+        # rollback; pressure range, velocity
+        launches = sum(2 + 2 + 2 * k + 1 + 2 for k in iters)
     else:
         # per iteration copy, red, black, residual
         launches = sum(2 + 4 * k + 2 for k in iters)
@@ -928,9 +928,9 @@ def main():
                     "rule": "reference stop rule; no step reached eps" if not any(
                         s[3] for s in stats) else "reference stop rule"},
         "roofline": {"bound": "hbm", "kernel": "one red-black SOR iteration of the solve graph "
-                     "(black pass + its residual + half the pressure copy, edge-list residual "
-                     "+ the other half, red pass + the previous iteration's red residual and "
-                     "stop test)",
+                     "(black pass + the black cells' residual + half the pressure copy, red "
+                     "pass + the other half + the previous iteration's red cells' residual "
+                     "and stop test)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": sor_bytes,

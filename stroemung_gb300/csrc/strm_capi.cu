@@ -69,7 +69,7 @@ struct strm_sim {
   cudaGraphExec_t exec_pre = nullptr, exec_post = nullptr;
   StepState *h_st = nullptr;   // pinned
   StepLog *h_log = nullptr;    // pinned
-  int bc_cap = 0, pcopy_cap = 0, edge_cap = 0;
+  int bc_cap = 0, pcopy_cap = 0, blist_cap = 0;
   void *rgba = nullptr;        // colour-map image, allocated on first use
 };
 
@@ -206,59 +206,60 @@ int classify_and_compile(strm_sim *s, long long *bad_out) {
     s->pcopy_cap = (int)pc.size() + 1024;
     CK(cudaMalloc(&s->d.pcopy, sizeof(PCopy) * s->pcopy_cap));
   }
-  // black-coloured copy targets ((x + y) odd: red sources) first, for the
-  // FAST red-black solve's split copy (the copies are independent: every
-  // source is a fluid cell)
-  const auto black_target = [&](const PCopy &c) {
-    return (((long long)(c.off / g.pitch) + c.off % g.pitch) & 1) != 0;
-  };
-  const int n_pc_b = (int)(std::stable_partition(pc.begin(), pc.end(), black_target) - pc.begin());
-  std::vector<uint8_t> copied((size_t)g.nx * g.pitch, 0);
-  for (const PCopy &c : pc) copied[(size_t)c.off] = 1;
-  // solver classes and the edge list of the FAST red-black solve
-  std::vector<uint8_t> cls(flags.size(), 2);
-  std::vector<unsigned int> elist;
+  // the FAST red-black solve: solver classes (with, for fluid cells next
+  // to a non-fluid cell, which neighbours are copied boundary cells) and the
+  // boundary-cell list, black-coloured cells ((x + y) odd) first, x-major
+  // within a colour
+  std::vector<uint8_t> copy_edge((size_t)g.nx * g.pitch, 0);
+  for (const PCopy &c : pc) copy_edge[(size_t)c.off] = (uint8_t)c.edge;
+  const auto copied = [&](size_t o) { return copy_edge[o] != 0 ? 1u : 0u; };
+  std::vector<uint8_t> cls(flags.size(), CLS_OTHER);
   for (int x = 1; x + 1 < g.nx; ++x)
     for (int y = 1; y + 1 < g.ny; ++y) {
       const size_t i = (size_t)x * g.ny + y;
-      const unsigned int off = (unsigned int)((size_t)x * g.pitch + y);
-      if (flags[i] != 0) {
-        elist.push_back(off);
-        continue;
-      }
+      const size_t o = (size_t)x * g.pitch + y;
+      if (flags[i] != 0) continue;
       const bool edge = flags[i - g.ny] || flags[i + g.ny] || flags[i - 1] || flags[i + 1];
-      cls[i] = edge ? 1 : 0;
-      if (edge && ((x + y) & 1) == 0) elist.push_back(off);
+      const unsigned int m = copied(o - g.pitch) | copied(o + g.pitch) << 1 |
+                             copied(o - 1) << 2 | copied(o + 1) << 3;
+      cls[i] = edge ? (uint8_t)(CLS_FLUID_EDGE | m << 2) : (uint8_t)CLS_FLUID;
     }
-  // which stencil points of each listed cell are copied boundary cells
-  std::vector<uint8_t> emask(elist.size());
-  for (size_t i = 0; i < elist.size(); ++i) {
-    const size_t o = elist[i];
-    emask[i] = (uint8_t)(copied[o] | copied[o - g.pitch] << 1 | copied[o + g.pitch] << 2 |
-                         copied[o - 1] << 3 | copied[o + 1] << 4);
+  std::vector<BCell> blist;
+  int n_blist_b = 0;
+  for (int colour = 1; colour >= 0; --colour) {
+    for (int x = 0; x < g.nx; ++x)
+      for (int y = 0; y < g.ny; ++y) {
+        const size_t i = (size_t)x * g.ny + y;
+        const size_t o = (size_t)x * g.pitch + y;
+        if (((x + y) & 1) != colour || flags[i] == 0) continue;
+        const bool interior = x >= 1 && x + 1 < g.nx && y >= 1 && y + 1 < g.ny;
+        BCell e{};
+        e.off = (unsigned int)o;
+        e.edge = copy_edge[o];
+        e.flags = (uint8_t)((interior ? BC_RES : 0) | (copied(o) ? BC_COPY : 0));
+        if (!e.flags) continue;
+        if (interior)
+          e.mask = (uint8_t)(copied(o) | copied(o - g.pitch) << 1 | copied(o + g.pitch) << 2 |
+                             copied(o - 1) << 3 | copied(o + 1) << 4);
+        blist.push_back(e);
+      }
+    if (colour == 1) n_blist_b = (int)blist.size();
   }
-  if ((int)elist.size() > s->edge_cap) {
-    if (s->d.edge_list) cudaFree(s->d.edge_list);
-  if (s->d.edge_mask) cudaFree(s->d.edge_mask);
-    if (s->d.edge_mask) cudaFree(s->d.edge_mask);
-    s->d.edge_list = nullptr;
-    s->d.edge_mask = nullptr;
-    s->edge_cap = (int)elist.size() + 1024;
-    CK(cudaMalloc(&s->d.edge_list, sizeof(unsigned int) * s->edge_cap));
-    CK(cudaMalloc(&s->d.edge_mask, s->edge_cap));
+  if ((int)blist.size() > s->blist_cap) {
+    if (s->d.blist) cudaFree(s->d.blist);
+    s->d.blist = nullptr;
+    s->blist_cap = (int)blist.size() + 1024;
+    CK(cudaMalloc(&s->d.blist, sizeof(BCell) * s->blist_cap));
   }
-  s->d.n_edge = (int)elist.size();
-  if (!elist.empty()) {
-    CK(cudaMemcpyAsync(s->d.edge_list, elist.data(), sizeof(unsigned int) * elist.size(),
+  s->d.n_blist = (int)blist.size();
+  s->d.n_blist_b = n_blist_b;
+  if (!blist.empty())
+    CK(cudaMemcpyAsync(s->d.blist, blist.data(), sizeof(BCell) * blist.size(),
                        cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(s->d.edge_mask, emask.data(), emask.size(), cudaMemcpyHostToDevice,
-                       s->stream));
-  }
   CK(cudaMemcpy2DAsync(s->d.cls, g.pitch, cls.data(), g.ny, g.ny, g.nx, cudaMemcpyHostToDevice,
                        s->stream));
   s->d.n_bc = (int)prog.size();
   s->d.n_pcopy = (int)pc.size();
-  s->d.n_pcopy_b = n_pc_b;
   if (!prog.empty())
     CK(cudaMemcpyAsync(s->d.bc, prog.data(), sizeof(BcEntry) * prog.size(),
                        cudaMemcpyHostToDevice, s->stream));
@@ -278,8 +279,7 @@ void free_sim(strm_sim *s) {
   if (s->d.bc) cudaFree(s->d.bc);
   if (s->d.bc_val) cudaFree(s->d.bc_val);
   if (s->d.pcopy) cudaFree(s->d.pcopy);
-  if (s->d.edge_list) cudaFree(s->d.edge_list);
-  if (s->d.edge_mask) cudaFree(s->d.edge_mask);
+  if (s->d.blist) cudaFree(s->d.blist);
   if (s->rgba) cudaFree(s->rgba);
   if (s->h_st) cudaFreeHost(s->h_st);
   if (s->h_log) cudaFreeHost(s->h_log);
@@ -378,7 +378,6 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   const size_t o_part = take(sizeof(double) * 4 * (size_t)nb);
   const size_t o_partb = take(sizeof(double) * 2 * (size_t)black_pass_blocks(s->g));
   const size_t o_partr = take(sizeof(double) * 2 * (size_t)black_pass_blocks(s->g));
-  const size_t o_parte = take(sizeof(double) * 2 * (size_t)kEdgeBlocksMax);
   const size_t o_cls = take(nfield);
   const size_t o_log = take(sizeof(StepLog) * kLogCap);
   const size_t o_bad = take(8), o_fc = take(8);
@@ -404,7 +403,6 @@ int strm_create(const strm_params *params, int nx, int ny, const uint8_t *kinds,
   d.n_partials = 4 * nb;
   d.partials_b = (double *)(base + o_partb);
   d.partials_r = (double *)(base + o_partr);
-  d.partials_e = (double *)(base + o_parte);
   d.cls = (uint8_t *)(base + o_cls);
   d.log = (StepLog *)(base + o_log);
   d.first_bad = (long long *)(base + o_bad);

@@ -10,13 +10,12 @@
 //     residual_kernel  residual norm, stop test, sets the WHILE condition
 //   fast arithmetic: pcopy_kernel, sor_red_res_kernel (first red pass), then
 //   WHILE(solve not done):
-//     sor_black_res_kernel  black pass + the black cells' residual; saves the
-//                           boundary values, copies the black-coloured ones
-//                           for the next iteration
-//     edge_res_kernel       residual of the cells next to boundary values;
+//     sor_black_res_kernel  black pass + the residual of the black cells;
+//                           saves the boundary values, copies the
+//                           black-coloured ones for the next iteration
+//     sor_red_res_kernel    red pass of the next iteration + this one's
+//                           residual of the red cells, norm, stop test;
 //                           copies the red-coloured boundary cells
-//     sor_red_res_kernel    red pass of the next iteration + this one's red
-//                           residual, norm, stop test
 //   sor_rollback_kernel  undoes the next iteration's copy and red pass
 //   mixed precision: FP32 sweeps with FP64 refinement (see the mixed solve)
 //   prange_kernel    pressure range when the solve ran out of iterations
@@ -677,41 +676,69 @@ __device__ __forceinline__ void block_sum_pass(double &a, double &b) {
   }
 }
 
+// Boundary pressure copy of one listed cell (src/grid/mod.rs:343-412).
+__device__ __forceinline__ void pcopy_cell(double *p, size_t o, int edge, int pitch) {
+  PCopy e;
+  e.off = (long long)o;
+  e.edge = edge;
+  pcopy_one(p, e, pitch);
+}
+
 // The black pass of a FAST red-black iteration fused with the residual of the
 // black fluid cells.  With t = (pe+pw)/dx^2 + (ps+pn)/dy^2 - rhs from the red
 // values and r0 = t - 2(1/dx^2+1/dy^2) p the residual before the update, the
 // update is p_new = p + omega r0 / (2(1/dx^2+1/dy^2)) (the reference update,
 // src/simulation.rs:260-271, rearranged), and since the four (red) neighbours
 // are final the cell's residual afterwards is r = (1-omega) r0.  The pass
-// sums r0^2 (and r0 when MEAN_FREE) and scales the block sums by (1-omega)^2
-// (and 1-omega): 7 FP64 operations per cell.  The sums go to
-// partials_b[blockIdx.x].
+// sums r0^2 (and r0 when MEAN_FREE) and scales the sums by (1-omega)^2 (and
+// 1-omega): 7 FP64 operations per cell.
 //
-// In the solve the pass also starts the boundary copy of iteration k+1
-// (src/grid/mod.rs:343-412; only when k < itermax, as the copy runs only
-// before another iteration): every copied boundary cell's value of
-// iteration k is saved into pw (the edge pass reads the residual's stale
-// boundary values from there, the rollback restores them), and the
-// black-coloured boundary cells pc[0..npc_b) get their new values here.
-// Their sources are red cells, final since the red pass, and no black
-// cell's stencil contains a black-coloured cell, so nothing in this pass
-// reads what the copy writes.  npc = 0: no copy (the phase entry points).
-template <bool MEAN_FREE>
+// In the solve (nbl > 0) the pass also works through the boundary-cell list
+// bl (black-coloured cells, (x + y) odd, in bl[0..nbl_b), then red-coloured
+// ones):
+//   * the residual of iteration k of every black-coloured non-fluid interior
+//     cell (when ALL: the norm over every interior cell).  Its stencil is
+//     the cell and four red-coloured cells, none of which this pass changes;
+//   * the boundary copy of iteration k+1 (src/grid/mod.rs:343-412; only
+//     when k < itermax, as the copy runs only before another iteration):
+//     every copied cell's value of iteration k is saved into pw (read by the
+//     red pass for the stale residual, restored by the rollback), and the
+//     black-coloured ones get their new values here.  A copied cell's
+//     sources are its fluid neighbours, of the other colour: red cells,
+//     final since the red pass; and no black cell's stencil holds a
+//     black-coloured cell, so nothing in this pass reads what the copy
+//     writes.  The cell's own residual is read before the copy, by the
+//     same thread.
+// The sums of the black fluid cells and of the list go to partials_b.
+template <bool MEAN_FREE, bool ALL>
 __global__ void __launch_bounds__(256)
     sor_black_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                          const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
                          Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
-                         const PCopy *__restrict__ pc, int npc_b, int npc, const StepState *st,
+                         const BCell *__restrict__ bl, int nbl_b, int nbl, const StepState *st,
                          unsigned int itermax) {
+  double accl = 0.0;  // residuals of the listed cells (ALL only, never MEAN_FREE)
   {
     const int nt = blockDim.x * blockDim.y;
-    int k = blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x;
-    if (k < npc) {
+    int i = blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x;
+    if (i < nbl) {
       const bool copy = st->sor_iters + 1 < itermax;
-      for (; k < npc; k += gridDim.x * nt) {
-        const PCopy e = pc[k];
-        pw[e.off] = p[e.off];
-        if (copy && k < npc_b) pcopy_one(p, e, g.pitch);
+      for (; i < nbl; i += gridDim.x * nt) {
+        const BCell e = bl[i];
+        const size_t o = e.off;
+        if (i < nbl_b) {
+          if (ALL && (e.flags & BC_RES)) {
+            const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
+                                                p[o + 1], rhs[o], c);
+            accl = fma(r, r, accl);
+          }
+          if (e.flags & BC_COPY) {
+            pw[o] = p[o];
+            if (copy) pcopy_cell(p, o, e.edge, g.pitch);
+          }
+        } else if (e.flags & BC_COPY) {
+          pw[o] = p[o];
+        }
       }
     }
   }
@@ -742,14 +769,15 @@ __global__ void __launch_bounds__(256)
       if (MEAN_FREE) acc1 += r0;
     }
   }
-  block_sum_pass<MEAN_FREE>(acc, acc1);
+  const double q = c.one_minus_w;
+  double a = fma(acc, q * q, accl), a1 = acc1 * q;
+  block_sum_pass<MEAN_FREE>(a, a1);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    const double q = c.one_minus_w;
     if (MEAN_FREE) {
-      partials_b[2 * blockIdx.x] = acc * (q * q);
-      partials_b[2 * blockIdx.x + 1] = acc1 * q;
+      partials_b[2 * blockIdx.x] = a;
+      partials_b[2 * blockIdx.x + 1] = a1;
     } else {
-      partials_b[blockIdx.x] = acc * (q * q);
+      partials_b[blockIdx.x] = a;
     }
   }
 }
@@ -933,31 +961,28 @@ __global__ void __launch_bounds__(256)
 // 260-271, rearranged).  So the red pass of iteration k+1 sums iteration k's
 // red residual and applies the stop test of k; the separate residual pass
 // over the red cells disappears (its FP64 operations and its reads of p and
-// rhs).  What that pass cannot see:
-//   * red fluid cells next to a non-fluid cell (class 1) and the non-fluid
-//     interior cells read boundary values, which the copy before iteration
-//     k+1 changes (src/grid/mod.rs:343-412; the norm of iteration k uses the
-//     stale ones).  edge_res_kernel sums those cells from a list after the
-//     black pass of k, reading the boundary values of k from the copy the
-//     black pass saved;
-//   * the stop itself: when iteration k stops the solve, the red pass and
-//     the boundary copy of k+1 have run.  Both saved the values they
-//     overwrote (in pw), and sor_rollback_kernel puts them back, so the
-//     solve ends on iteration k's pressure, boundary values included.
-// The copy of iteration k+1 is split by the colour of the boundary cell: a
-// boundary cell's sources are its fluid neighbours, all of the other
-// colour, so the black-coloured ones (red sources) are copied in the black
-// pass of k and the red-coloured ones (black sources) in the edge pass.
-// Iteration k+1's red pass and copy run only when k < itermax.
-// Per iteration: black pass (+ its residual, the save and half the copy),
-// edge list (+ the other half), red pass (+ the stop test), instead of
-// copy, red, black, residual.
+// rhs).  The boundary copy before iteration k+1 (src/grid/mod.rs:343-412)
+// needs no launch of its own either.  A copied cell's sources are its fluid
+// neighbours, all of the other colour, and a cell's stencil holds only
+// cells of the other colour besides itself.  So the black pass of k copies
+// the black-coloured boundary cells (red sources, final), which no black
+// cell reads, and the red pass of k+1 the red-coloured ones (black sources,
+// final), which no red cell reads; the black pass first saves every copied
+// cell's value of k into pw.  The norm of iteration k reads the stale
+// boundary values of k (the reference copies before each sweep): the black
+// pass sums the black-coloured non-fluid interior cells before it copies
+// them, and the red pass reads the copied cells in the stencils of the red
+// fluid cells next to them (class 1) and of the red-coloured non-fluid
+// interior cells from pw.  The stop itself: when iteration k stops the
+// solve, the red pass and the copy of k+1 have run; both saved what they
+// overwrote (in pw), and sor_rollback_kernel puts it back, so the solve
+// ends on iteration k's pressure, boundary values included.  Iteration
+// k+1's red pass and copy run only when k < itermax.
+// Per iteration: black pass (+ its residual, the save and half the copy)
+// and red pass (+ the other half, the red residual and the stop test),
+// instead of copy, red, black, residual.
 // ------------------------------------------------------------------------
 
-// Solver class of a cell (per cell, pitch layout): 0 fluid interior cell with
-// four fluid neighbours, 1 fluid interior cell next to a non-fluid cell,
-// 2 anything else.
-enum : uint8_t { CLS_FLUID = 0, CLS_FLUID_EDGE = 1, CLS_OTHER = 2 };
 
 template <bool MEAN_FREE>
 __device__ __forceinline__ void store_sums(double acc, double acc1, double *partials) {
@@ -972,13 +997,13 @@ __device__ __forceinline__ void store_sums(double acc, double acc1, double *part
   }
 }
 
-// The norm from three partial arrays (black pass, edge list, red pass): each
-// thread adds its entries of the three arrays in that order, then one block
+// The norm from the black pass's and the red pass's partial sums: each
+// thread adds its entries of the two arrays in that order, then one block
 // sum — one chain of loads and one barrier pair on the critical path of the
-// iteration instead of three.
-__device__ __forceinline__ double finish_norm3(const double *pa, int na, const double *pb, int nb,
-                                               const double *pc, int nc, bool mean_free,
-                                               double fluid_cells) {
+// iteration.
+__device__ __forceinline__ double finish_norm_passes(const double *pa, int na, const double *pb,
+                                                     int nb, bool mean_free,
+                                                     double fluid_cells) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
   const int nt = blockDim.x * blockDim.y;
   double s2 = 0.0, s1 = 0.0;
@@ -987,8 +1012,6 @@ __device__ __forceinline__ double finish_norm3(const double *pa, int na, const d
     for (int k = tid; k < na; k += nt) s2 += __ldcg(pa + k);
 #pragma unroll 4
     for (int k = tid; k < nb; k += nt) s2 += __ldcg(pb + k);
-#pragma unroll 4
-    for (int k = tid; k < nc; k += nt) s2 += __ldcg(pc + k);
     block_sum_pass<false>(s2, s1);
     return s2 / fluid_cells;
   }
@@ -1002,74 +1025,54 @@ __device__ __forceinline__ double finish_norm3(const double *pa, int na, const d
     s2 += __ldcg(pb + 2 * k);
     s1 += __ldcg(pb + 2 * k + 1);
   }
-#pragma unroll 4
-  for (int k = tid; k < nc; k += nt) {
-    s2 += __ldcg(pc + 2 * k);
-    s1 += __ldcg(pc + 2 * k + 1);
-  }
   block_sum_pass<true>(s2, s1);
   return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
 }
 
-// Residual sums of the listed cells (offsets, x-major) after the black pass
-// of iteration k: the non-fluid interior cells (skipped by the fluid norms)
-// and the red class-1 cells.  Their stencils read boundary values of
-// iteration k, which the black pass saved into pw; mask[i] says which of
-// the five stencil points (bit 0 the cell, 1 west, 2 east, 3 north, 4
-// south) are copied boundary cells, read from pw.  Blocks nres and up
-// write the boundary copy of iteration k+1 (when k < itermax) for the
-// red-coloured boundary cells pc[npc_b..npc) meanwhile: their sources are
-// black cells, final after the black pass, and the residuals read those
-// boundary cells from pw, not p.  Blocks 0..nres-1 store their sums in
-// partials_e.
-template <bool FLUID, bool MEAN_FREE>
-__global__ void __launch_bounds__(256)
-    edge_res_kernel(double *__restrict__ p, const double *__restrict__ pw,
-                    const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
-                    const unsigned int *__restrict__ list, const uint8_t *__restrict__ mask,
-                    int n, int nres, Geom g, Consts c, double *__restrict__ partials_e,
-                    const PCopy *__restrict__ pc, int npc_b, int npc, const StepState *st,
-                    unsigned int itermax) {
-  const int nt = blockDim.x * blockDim.y;
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  if ((int)blockIdx.x >= nres) {
-    const int b = blockIdx.x - nres, nb = gridDim.x - nres;
-    if (npc_b + b * nt + tid < npc && st->sor_iters + 1 < itermax)
-      for (int k = npc_b + b * nt + tid; k < npc; k += nb * nt) pcopy_one(p, pc[k], g.pitch);
-    return;
-  }
-  double acc = 0.0, acc1 = 0.0;
-  for (int i = blockIdx.x * nt + tid; i < n; i += nres * nt) {
-    const size_t o = list[i];
-    const unsigned int m = mask[i];
-    if (FLUID && flags[o] != 0) continue;
-    const double *s0 = (m & 1u) ? pw : p, *sw = (m & 2u) ? pw : p, *se = (m & 4u) ? pw : p;
-    const double *sn = (m & 8u) ? pw : p, *ss = (m & 16u) ? pw : p;
-    const double r = residual_of<false>(s0[o], sw[o - g.pitch], se[o + g.pitch], sn[o - 1],
-                                        ss[o + 1], rhs[o], c);
-    acc = fma(r, r, acc);
-    if (MEAN_FREE) acc1 += r;
-  }
-  store_sums<MEAN_FREE>(acc, acc1, partials_e);
-}
-
 // Red pass.  mode 0: update only (the first red pass of a solve, and the
-// phase entry points).  mode 1: sum the residual of iteration k over the
-// class-0 red cells, update (saving the old value into pw) only when k <
-// itermax; the last block adds the black pass's and the edge list's sums
-// and applies the stop test of iteration k.  The update is the same in both
-// modes.
-template <bool IN_GRAPH, bool MEAN_FREE>
-__global__ void __launch_bounds__(256)
+// phase entry points).  mode 1 (the solve's loop): the red pass of iteration
+// k+1, which updates (saving the old value into pw) only when k < itermax
+// and sums the residual of iteration k of
+//   * the red fluid cells: class 0 from the values it reads for its update
+//     (the four black neighbours are fluid and final); class 1 with the
+//     copied neighbours' stale values of iteration k from pw (the black
+//     pass wrote their new values into p; the cls byte's bits 2-5 say which
+//     of west, east, north, south are copied cells);
+//   * the red-coloured non-fluid interior cells bl[nbl_b..nbl) (when ALL),
+//     reading the copied cells of their stencil (BCell::mask) from pw;
+// and writes the boundary copy of iteration k+1 of the red-coloured listed
+// cells (their sources are black cells, final; red cells' stencils hold no
+// red-coloured cell, and the residuals here read copied cells from pw).  The
+// last block adds the black pass's sums and applies the stop test of
+// iteration k.
+template <bool IN_GRAPH, bool MEAN_FREE, bool ALL>
+__global__ void __launch_bounds__(256, 4)
     sor_red_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                        const double *__restrict__ rhs, const uint8_t *__restrict__ cls, Geom g,
                        Consts c, StepState *st, double *__restrict__ partials_r,
-                       const double *partials_b, int nbb, const double *partials_e, int nbe,
-                       int gx, int nvb, unsigned int itermax, int strict, int mode,
-                       cudaGraphConditionalHandle h) {
+                       const double *partials_b, int nbb, const BCell *__restrict__ bl,
+                       int nbl_b, int nbl, int gx, int nvb, unsigned int itermax, int strict,
+                       int mode, cudaGraphConditionalHandle h) {
   const bool sum = mode == 1;
   const bool write = !sum || st->sor_iters + 1 < itermax;
   double acc = 0.0, acc1 = 0.0;
+  if (sum) {
+    const int nt = blockDim.x * blockDim.y;
+    for (int i = nbl_b + blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x; i < nbl;
+         i += gridDim.x * nt) {
+      const BCell e = bl[i];
+      const size_t o = e.off;
+      if (ALL && (e.flags & BC_RES)) {
+        const unsigned int m = e.mask;
+        const double *s0 = (m & 1u) ? pw : p, *sw = (m & 2u) ? pw : p, *se = (m & 4u) ? pw : p;
+        const double *sn = (m & 8u) ? pw : p, *ss = (m & 16u) ? pw : p;
+        const double r = residual_of<false>(s0[o], sw[o - g.pitch], se[o + g.pitch], sn[o - 1],
+                                            ss[o + 1], rhs[o], c);
+        acc = fma(r, r, acc);
+      }
+      if (write && (e.flags & BC_COPY)) pcopy_cell(p, o, e.edge, g.pitch);
+    }
+  }
   for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
     const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 0, g);
     unsigned int k[kPassUnroll];
@@ -1088,12 +1091,23 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int u = 0; u < kPassUnroll; ++u) {
-      if (!cells.ok[u] || k[u] >= CLS_OTHER) continue;
+      const unsigned int kc = k[u] & 3u;
+      if (!cells.ok[u] || kc >= CLS_OTHER) continue;
       const double t = fma(pe[u] + pwv[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
       const double r = fma(-c.two_r_sum, pc[u], t);
-      if (sum && k[u] == CLS_FLUID) {
-        acc = fma(r, r, acc);
-        if (MEAN_FREE) acc1 += r;
+      if (sum) {
+        double rk = r;
+        if (kc == CLS_FLUID_EDGE) {
+          const size_t o = cells.o[u];
+          const unsigned int m = k[u] >> 2;
+          const double w0 = (m & 1u) ? pw[o - g.pitch] : pwv[u];
+          const double e0 = (m & 2u) ? pw[o + g.pitch] : pe[u];
+          const double n0 = (m & 4u) ? pw[o - 1] : pn[u];
+          const double s0 = (m & 8u) ? pw[o + 1] : ps[u];
+          rk = residual_of<false>(pc[u], w0, e0, n0, s0, rh[u], c);
+        }
+        acc = fma(rk, rk, acc);
+        if (MEAN_FREE) acc1 += rk;
       }
       if (write) {
         if (sum) pw[cells.o[u]] = pc[u];
@@ -1105,8 +1119,8 @@ __global__ void __launch_bounds__(256)
   store_sums<MEAN_FREE>(acc, acc1, partials_r);
   loop_guard<IN_GRAPH>(st, itermax, h);
   if (!last_block_done(&st->counter)) return;
-  const double ns = finish_norm3(partials_b, nbb, partials_e, nbe, partials_r, gridDim.x,
-                                 MEAN_FREE, st->fluid_cells);
+  const double ns = finish_norm_passes(partials_b, nbb, partials_r, gridDim.x, MEAN_FREE,
+                                       st->fluid_cells);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     st->counter = 0;
     solve_iteration_done<IN_GRAPH>(st, ns, c, strict, itermax, h);
@@ -1125,7 +1139,7 @@ __global__ void __launch_bounds__(256)
     const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + (x & 1);
     if (x > g.nx - 2 || y < 1 || y > g.ny - 2) continue;
     const size_t o = OFF(x, y);
-    if (cls[o] < CLS_OTHER) p[o] = pw[o];
+    if ((cls[o] & 3u) < CLS_OTHER) p[o] = pw[o];
   }
   const int nt = blockDim.x * blockDim.y;
   for (int k = blockIdx.x * nt + threadIdx.x + threadIdx.y * blockDim.x; k < npc;
@@ -2050,36 +2064,28 @@ int black_pass_blocks(const Geom &g) {
   return n < 1 ? 1 : (int)n;
 }
 
-int edge_blocks(int n) {
-  int b = (n + 255) / 256;
-  if (b > kEdgeBlocksMax) b = kEdgeBlocksMax;
-  return b < 1 ? 1 : b;
-}
-
-// Blocks of the edge pass that write the red-coloured boundary copies.
-static int copy_blocks(const DevFields &d) {
-  const int n = d.n_pcopy - d.n_pcopy_b;
-  return n > 0 ? std::min((n + 255) / 256, 256) : 0;
-}
-
 // Kernel choices of the FAST red-black solve for a stop-rule setting.
 struct FastSolveKernels {
-  const void *red_graph, *red_eager, *black, *edge;
+  const void *red_graph, *red_eager, *black;
 };
 
 static FastSolveKernels fast_solve_kernels(int strict) {
   const bool fluid = (strict & STOP_FLUID_NORM) != 0;
   const bool mf = fluid && (strict & STOP_MEAN_FREE) != 0;
   FastSolveKernels k;
-  k.black = mf ? (const void *)sor_black_res_kernel<true>
-               : (const void *)sor_black_res_kernel<false>;
-  k.red_graph = mf ? (const void *)sor_red_res_kernel<true, true>
-                   : (const void *)sor_red_res_kernel<true, false>;
-  k.red_eager = mf ? (const void *)sor_red_res_kernel<false, true>
-                   : (const void *)sor_red_res_kernel<false, false>;
-  k.edge = !fluid ? (const void *)edge_res_kernel<false, false>
-           : mf   ? (const void *)edge_res_kernel<true, true>
-                  : (const void *)edge_res_kernel<true, false>;
+  if (mf) {
+    k.black = (const void *)sor_black_res_kernel<true, false>;
+    k.red_graph = (const void *)sor_red_res_kernel<true, true, false>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, true, false>;
+  } else if (fluid) {
+    k.black = (const void *)sor_black_res_kernel<false, false>;
+    k.red_graph = (const void *)sor_red_res_kernel<true, false, false>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, false, false>;
+  } else {
+    k.black = (const void *)sor_black_res_kernel<false, true>;
+    k.red_graph = (const void *)sor_red_res_kernel<true, false, true>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, false, true>;
+  }
   return k;
 }
 
@@ -2329,16 +2335,16 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
     // the red pass of the solve (its update formula), without its sums
     const int bb = black_pass_blocks(r.g);
     const int nvb = (int)(sgrid.x * sgrid.y);
-    sor_red_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
-        d.p, d.pw, d.rhs, d.cls, r.g, r.c, d.st, d.partials_r, d.partials_b, bb, d.partials_e, 1,
+    sor_red_res_kernel<false, false, true><<<bb, kRedBlock, 0, s>>>(
+        d.p, d.pw, d.rhs, d.cls, r.g, r.c, d.st, d.partials_r, d.partials_b, bb, nullptr, 0, 0,
         (int)sgrid.x, nvb, r.itermax, r.strict_eps, 0, 0);
-    // (npc = 0: the pass makes no boundary copy here)
+    // (an empty boundary-cell list: the pass makes no boundary copy here)
     if (mean_free)
-      sor_black_res_kernel<true><<<bb, kRedBlock, 0, s>>>(
+      sor_black_res_kernel<true, false><<<bb, kRedBlock, 0, s>>>(
           d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
           d.st, r.itermax);
     else
-      sor_black_res_kernel<false><<<bb, kRedBlock, 0, s>>>(
+      sor_black_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
           d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
           d.st, r.itermax);
     residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
@@ -2469,41 +2475,30 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       // norm (see sor_red_res_kernel); the same launches as the graph
       const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
       const int bb = black_pass_blocks(g);
-      const int nbe = edge_blocks(d.n_edge), ncb = copy_blocks(d);
       int gx = (int)sgrid.x;
       unsigned int itermax = r.itermax;
       int strict = r.strict_eps, mode = 0;
       cudaGraphConditionalHandle h0 = 0;
-      double *p = d.p, *pw = d.pw, *prt_r = d.partials_r;
-      const double *rhs = d.rhs, *prt_b = d.partials_b, *prt_e = d.partials_e;
-      const uint8_t *cls = d.cls;
+      double *p = d.p, *pw = d.pw, *prt_r = d.partials_r, *prt_bw = d.partials_b;
+      const double *rhs = d.rhs, *prt_b = d.partials_b;
+      const uint8_t *cls = d.cls, *flags = d.flags;
+      const BCell *bl = d.blist;
       StepState *st = d.st;
+      const StepState *cst = d.st;
       Geom gg = g;
       Consts cc = c;
-      int nbb_b = bb, nbe_e = nbe, nvb = nbb;
-      void *red_args[] = {&p, &pw, &rhs, &cls, &gg, &cc, &st, &prt_r, &prt_b, &nbb_b, &prt_e,
-                          &nbe_e, &gx, &nvb, &itermax, &strict, &mode, &h0};
+      int nbb_b = bb, nvb = nbb, nbl_b = d.n_blist_b, nbl = d.n_blist;
+      void *red_args[] = {&p,   &pw,  &rhs,   &cls, &gg,      &cc,     &st,   &prt_r, &prt_b, &nbb_b,
+                          &bl, &nbl_b, &nbl, &gx,  &nvb, &itermax, &strict, &mode, &h0};
+      void *black_args[] = {&p,  &pw,  &rhs,   &flags, &gg,  &cc,      &prt_bw, &gx,
+                            &nvb, &bl, &nbl_b, &nbl,   &cst, &itermax};
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
       if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
           cudaSuccess)
         return e;
       mode = 1;
-      const unsigned int *list = d.edge_list;
-      const uint8_t *flags = d.flags, *emask = d.edge_mask;
-      const PCopy *pcl = d.pcopy;
-      int n_edge = d.n_edge, nres = nbe, npc_b = d.n_pcopy_b, npc = d.n_pcopy;
-      const StepState *cst = d.st;
-      void *edge_args[] = {&p,     &pw,  &rhs,   &flags, &list, &emask,  &n_edge, &nres,
-                           &gg,    &cc,  &prt_e, &pcl,   &npc_b, &npc,   &cst,    &itermax};
-      double *prt_bw = d.partials_b;
-      int nvb_b = nbb;
-      void *black_args[] = {&p,   &pw,  &rhs,   &flags, &gg,  &cc,      &prt_bw, &gx,
-                            &nvb_b, &pcl, &npc_b, &npc,  &cst, &itermax};
       while (!done) {
         if ((e = cudaLaunchKernel(fk.black, dim3(bb), kRedBlock, black_args, 0, s)) !=
-            cudaSuccess)
-          return e;
-        if ((e = cudaLaunchKernel(fk.edge, dim3(nbe + ncb), kRedBlock, edge_args, 0, s)) !=
             cudaSuccess)
           return e;
         if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
@@ -2759,8 +2754,8 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
       n = b.kernel(b.graph, n, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
                    (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
-                   (const double *)d.partials_b, bb, (const double *)d.partials_e,
-                   edge_blocks(d.n_edge), (int)sgrid.x, nbb, r.itermax, r.strict_eps, 0, h);
+                   (const double *)d.partials_b, bb, (const BCell *)d.blist, d.n_blist_b,
+                   d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 0, h);
     }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
@@ -2774,20 +2769,14 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
       if (r.arith) {
-        const int nbe = edge_blocks(d.n_edge), ncb = copy_blocks(d);
         bn = b.kernel(body, nullptr, fk.black, dim3(bb), kRedBlock, d.p, d.pw,
                       (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
-                      (int)sgrid.x, nbb, (const PCopy *)d.pcopy, d.n_pcopy_b, d.n_pcopy,
-                      (const StepState *)d.st, r.itermax);
-        bn = b.kernel(body, bn, fk.edge, dim3(nbe + ncb), kRedBlock, d.p, (const double *)d.pw,
-                      (const double *)d.rhs, (const uint8_t *)d.flags,
-                      (const unsigned int *)d.edge_list, (const uint8_t *)d.edge_mask, d.n_edge,
-                      nbe, g, c, d.partials_e, (const PCopy *)d.pcopy, d.n_pcopy_b, d.n_pcopy,
+                      (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
                       (const StepState *)d.st, r.itermax);
         bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
                       (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
-                      (const double *)d.partials_b, bb, (const double *)d.partials_e, nbe,
-                      (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
+                      (const double *)d.partials_b, bb, (const BCell *)d.blist, d.n_blist_b,
+                      d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
       } else {
         if (d.n_pcopy > 0)
           bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),

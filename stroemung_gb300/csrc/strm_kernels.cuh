@@ -10,6 +10,25 @@
 
 namespace strm {
 
+// Solver class of an interior cell for the FAST red-black solve (cls byte,
+// pitch layout): bits 0-1 the class (0 fluid with four fluid neighbours, 1
+// fluid next to a non-fluid cell, 2 anything else); for class 1, bits 2-5
+// say which of the west, east, north, south neighbours are copied boundary
+// cells.
+enum : uint8_t { CLS_FLUID = 0, CLS_FLUID_EDGE = 1, CLS_OTHER = 2 };
+
+// A listed boundary cell of the FAST red-black solve: every non-fluid
+// interior cell (its residual) and every cell of the boundary pressure copy.
+enum : uint8_t { BC_RES = 1, BC_COPY = 2 };
+struct BCell {
+  unsigned int off;     // pitched offset
+  unsigned char edge;   // the copy's EdgeType (BC_COPY)
+  unsigned char flags;  // BC_RES: a non-fluid interior cell; BC_COPY: copied
+  unsigned char mask;   // copied stencil points: bit 0 the cell, 1 west, 2 east,
+                        // 3 north, 4 south
+  unsigned char pad;
+};
+
 // Device buffers of one simulation.
 struct DevFields {
   double *u, *v, *p, *f, *g, *rhs;
@@ -27,21 +46,15 @@ struct DevFields {
   BcEntry *bc;            // compiled boundary program
   double *bc_val;         // its gathered values
   int n_bc;
-  PCopy *pcopy;           // boundary pressure copies, black-coloured targets first
+  PCopy *pcopy;
   int n_pcopy;
-  int n_pcopy_b;          // how many targets are black-coloured ((x + y) odd)
-  // FAST red-black solve: solver class per cell (0 fluid with fluid
-  // neighbours, 1 fluid next to a non-fluid cell, 2 other), the cells whose
-  // residual the edge pass sums (offsets, x-major) with, per cell, which of
-  // its five stencil points are copied boundary cells (bit 0 the cell, 1
-  // west, 2 east, 3 north, 4 south), and the partial sums of the red pass
-  // and of the edge pass
+  // FAST red-black solve: solver class per cell (CLS_*), the boundary-cell
+  // list (black-coloured cells first), the red pass's partial sums
   uint8_t *cls;
-  unsigned int *edge_list;
-  uint8_t *edge_mask;
-  int n_edge;
+  BCell *blist;
+  int n_blist;
+  int n_blist_b;
   double *partials_r;
-  double *partials_e;
   long long *first_bad;   // classification: first thin-wall cell (x*ny+y)
   unsigned long long *fluid_count;
 };
@@ -78,10 +91,6 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
 // (the inner iteration of the mixed solve), by the configured schedule.
 cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_t s, int n);
 int num_sweep_schedules();
-// Blocks of the edge-list residual pass for n listed cells (at most
-// kEdgeBlocksMax).
-constexpr int kEdgeBlocksMax = 256;
-int edge_blocks(int n);
 
 // Colour map into a device RGBA8 image [ny][nx] (0 pressure, 1 speed).
 cudaError_t launch_render(const DevFields &d, const Geom &g, int color_type, void *rgba,

@@ -208,6 +208,56 @@ def test_random_layouts_all_boundary_kinds(seed):
     assert_fields_equal(o2, s2, "red-black after 5 steps")
 
 
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("strict,eps", [(False, 1e-3), (True, 1e-3), (True, 100.0)],
+                         ids=["reference_rule", "to_itermax", "strict_eps_100"])
+def test_random_layouts_fast_red_black(seed, strict, eps):
+    """The FAST red-black solve on random layouts with every boundary kind:
+    its boundary copy is split by the colour of the copied cell between the
+    black and the edge passes, the edge pass reads the stale boundary values
+    from the saved copy, and an early stop rolls the next iteration back.
+    With these random fields the reference rule stops every solve after one
+    or two iterations (a rollback each step), strict eps 1e-3 runs every
+    solve to max_iterations, strict eps 100 stops some solves in between.
+    Against the oracle's red-black order: the same iteration counts, norms
+    and fields within 1e-9; eager launches bit-identical to the graph."""
+    from stroemung_gb300.simulation import ARITH_FAST
+    from tests.test_host_boundary import random_layout
+    rng = np.random.default_rng(200 + seed)
+    nx, ny = int(rng.integers(8, 48)), int(rng.integers(6, 36))
+    for _ in range(100):
+        kind = random_layout(rng, nx, ny, int(rng.integers(0, 6)))
+        if orc.classify(kind)[2] is None:
+            break
+    else:
+        pytest.skip("no valid layout drawn")
+    g = presets.empty((nx, ny))
+    g["kind"] = kind
+    g["wall_uv"] = rng.normal(size=(nx, ny, 2))
+    g["u"] = rng.normal(size=(nx, ny))
+    g["v"] = rng.normal(size=(nx, ny))
+    g["p"] = rng.normal(size=(nx, ny))
+    prm = dict(cell_size=(0.1, 0.07), delt=0.002, gamma=0.8, reynolds=50.0, eps=eps,
+               max_iterations=60, omega=1.6)
+    mode = {"sor_order": 0, "arithmetic": ARITH_FAST}
+    o, s = make_pair(g, orc_order=orc.RED_BLACK, gpu_mode=mode, strict_eps=strict, **prm)
+    _, e = make_pair(g, orc_order=orc.RED_BLACK, gpu_mode=dict(mode, execution=1),
+                     strict_eps=strict, **prm)
+    iters = []
+    for step in range(6):
+        io, no = o.tick()
+        i_s, ns = s.run_simulation_tick()
+        assert e.run_simulation_tick() == (i_s, ns), step
+        assert i_s == io, (step, i_s, io)
+        assert abs(ns - no) <= 1e-9 * abs(no) + 1e-300, (step, ns, no)
+        iters.append(i_s)
+    for n in ("u", "v", "p"):
+        assert rel_l2(s.download(n), o.field(n)) < 1e-9, n
+        assert_bits_equal(e.download(n), s.download(n), n)
+    if not strict:
+        assert max(iters) < prm["max_iterations"], iters
+
+
 def test_phase_entry_points_match_oracle_phases():
     g = presets.channel(60, 20, [(20, 8, 4, 5)])
     prm = dict(cell_size=(0.1, 0.1), delt=0.01, gamma=0.9, reynolds=100.0)
