@@ -193,9 +193,9 @@ def run_reference(args):
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
 
 # DRAM traffic from the committed ncu captures of this workload (bytes):
-# one FP64 iteration (red 88.4 + 20.1 MB, black 72.1 + 1.0 MB, edge list
-# 2.8 MB) and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
-SOR_ITERATION_TRAFFIC = (88.4 + 20.1 + 72.1 + 1.0 + 2.8) * 1e6
+# one FP64 iteration (red pass 88.9 + 19.6 MB, black pass 72.5 + 1.0 MB)
+# and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
+SOR_ITERATION_TRAFFIC = (88.9 + 19.6 + 72.5 + 1.0) * 1e6
 SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
 
 
@@ -934,8 +934,8 @@ def main():
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": sor_bytes,
-                     # DRAM bytes of one iteration's kernels (red, black, edge
-                     # list) in one ncu capture of this workload, cold cache:
+                     # DRAM bytes of one iteration's kernels (red and black
+                     # passes) in one ncu capture of this workload, cold cache:
                      # profiles/fp64_sor_kernels_channel_4096x1024.md
                      "traffic": SOR_ITERATION_TRAFFIC,
                      "traffic_note": "ncu dram__bytes read+write of one iteration's kernels, "
