@@ -410,6 +410,7 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
     plain = Simulation(grid=grid, **mk, **PARAMS)
     wsim = Simulation(grid=grid, **mk, **PARAMS)
     ws = warmstart.WarmStartSolver(wsim, net)
+    ws.warm_up()
     scratch = torch.zeros(IMAX + 2, JMAX + 2, dtype=torch.float64, device="cuda")
     plain.step_n(args.warmup)
     warmstart.sync_state(wsim, plain, scratch)
@@ -498,6 +499,7 @@ def learned_cavity_block(args):
             wsim = warmstart.make_simulation(presets.cavity(n), re, 1.0 / n, delt=1e-3,
                                              max_iterations=40000)
             ws = warmstart.WarmStartSolver(wsim, net, judge_sweeps=judge)
+            ws.warm_up()
             scratch = torch.zeros(n + 2, n + 2, dtype=torch.float64, device="cuda")
             for _ in range(args.ws_cavity_steps):
                 r = warmstart.compare_step(plain, ws, scratch)
@@ -687,6 +689,7 @@ def batched_learned(args, specs, cfg, sched, st_plain, t_plain):
     batch.set_schedule(sched)
     batch.step(1)
     bws = warmstart.BatchWarmStart(batch, net, judge_sweeps=args.ws_judge_sweeps)
+    bws.warm_up()
     sweeps, acc = [], 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()

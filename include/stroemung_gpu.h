@@ -228,7 +228,9 @@ int strm_copy_field_device(strm_sim *sim, int field, double *dense, int to_sim);
  * sweeps remove).  Either way the pressure is left at the chosen candidate
  * without the judge's sweeps, boundary copy applied; ns_prev / ns_pred
  * receive the two norms, accepted 1 when the correction was kept (each may
- * be NULL).  No reference counterpart. */
+ * be NULL).  The judge's launches run as one CUDA graph, recorded on the
+ * first call for this q buffer and sweep count (and again after a mode
+ * change or a cell edit).  No reference counterpart. */
 int strm_judge_correction(strm_sim *sim, const float *q, double scale, int sweeps,
                           double *ns_prev, double *ns_pred, int *accepted);
 

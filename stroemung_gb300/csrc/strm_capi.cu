@@ -71,6 +71,12 @@ struct strm_sim {
   StepLog *h_log = nullptr;    // pinned
   int bc_cap = 0, pcopy_cap = 0, blist_cap = 0;
   void *rgba = nullptr;        // colour-map image, allocated on first use
+  // strm_judge_correction's launches as one graph, for this q buffer and
+  // sweep count; jd: device [scale, norm without, norm with the correction]
+  cudaGraphExec_t judge_exec = nullptr;
+  const float *judge_q = nullptr;
+  int judge_sweeps = -1;
+  double *jd = nullptr;
 };
 
 namespace {
@@ -135,6 +141,9 @@ void update_cfg(strm_sim *s) {
 }
 
 void destroy_graphs(strm_sim *s) {
+  if (s->judge_exec) cudaGraphExecDestroy(s->judge_exec);
+  s->judge_exec = nullptr;
+  s->judge_q = nullptr;
   cudaGraphExec_t *ex[3] = {&s->exec, &s->exec_pre, &s->exec_post};
   cudaGraph_t *gr[3] = {&s->graph, &s->graph_pre, &s->graph_post};
   for (int i = 0; i < 3; ++i) {
@@ -281,6 +290,7 @@ void free_sim(strm_sim *s) {
   if (s->d.pcopy) cudaFree(s->d.pcopy);
   if (s->d.blist) cudaFree(s->d.blist);
   if (s->rgba) cudaFree(s->rgba);
+  if (s->jd) cudaFree(s->jd);
   if (s->h_st) cudaFreeHost(s->h_st);
   if (s->h_log) cudaFreeHost(s->h_log);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -736,44 +746,77 @@ int strm_apply_correction(strm_sim *s, const float *q, double scale) {
   return STRM_OK;
 }
 
+namespace {
+
+// The judge's launches on s->stream: both candidates' norms after `sweeps`
+// FP64 red-black iterations (fast arithmetic, the sim's norm; 0: the
+// initial norm after the boundary copy) into jd[2] (with the correction)
+// and jd[1] (without), then the choice, made on the device.
+cudaError_t record_judge(strm_sim *s, const float *q, int sweeps) {
+  const size_t bytes = sizeof(double) * (size_t)s->g.nx * s->g.pitch;
+  DevFields &d = s->d;
+  RunCfg rj = s->cfg;
+  rj.precision = 0;
+  rj.arith = 1;
+  cudaError_t e;
+  auto norm_into = [&](double *dst) -> cudaError_t {
+    cudaError_t err;
+    if (sweeps == 0) {
+      if ((err = launch_pcopy(d, s->g, s->stream)) != cudaSuccess) return err;
+      if ((err = launch_norm(d, s->cfg, s->stream, 0)) != cudaSuccess) return err;
+    } else {
+      for (int k = 0; k < sweeps; ++k)  // the norm after the last iteration only
+        if ((err = launch_sor_iteration(d, rj, s->stream, k + 1 == sweeps)) != cudaSuccess)
+          return err;
+    }
+    return cudaMemcpyAsync(dst, &d.st->aux, sizeof(double), cudaMemcpyDeviceToDevice, s->stream);
+  };
+  if ((e = cudaMemcpyAsync(d.pw, d.p, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 0)) != cudaSuccess) return e;
+  if ((e = norm_into(s->jd + 2)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = norm_into(s->jd + 1)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 1)) != cudaSuccess) return e;
+  return launch_pcopy(d, s->g, s->stream);
+}
+
+}  // namespace
+
 int strm_judge_correction(strm_sim *s, const float *q, double scale, int sweeps,
                           double *ns_prev, double *ns_pred, int *accepted) {
   if (!s || !q || sweeps < 0 || sweeps > 4096) return fail(STRM_ERR_INVALID, "invalid arguments");
   CK(cudaSetDevice(s->dev));
-  const size_t bytes = sizeof(double) * (size_t)s->g.nx * s->g.pitch;
-  DevFields &d = s->d;
-  // the judge's sweeps: FP64 red-black with fast arithmetic, the sim's norm
-  RunCfg rj = s->cfg;
-  rj.precision = 0;
-  rj.arith = 1;
-  auto norm_after = [&](double *out) -> int {
-    if (sweeps == 0) {
-      CK(launch_pcopy(d, s->g, s->stream));
-      CK(launch_norm(d, s->cfg, s->stream, 0));
-    } else {
-      for (int k = 0; k < sweeps; ++k) CK(launch_sor_iteration(d, rj, s->stream));
-    }
-    int rc = sync_state(s);
-    if (rc) return rc;
-    *out = s->h_st->aux;
-    return STRM_OK;
-  };
-  CK(cudaMemcpyAsync(d.pw, d.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
-  double a = 0.0, b = 0.0;
-  CK(launch_apply_correction(d, s->g, q, scale, s->stream));
-  int rc = norm_after(&b);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream));
-  rc = norm_after(&a);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream));
-  const bool take = b < a;
-  if (take) CK(launch_apply_correction(d, s->g, q, scale, s->stream));
-  CK(launch_pcopy(d, s->g, s->stream));
+  if (!s->jd) CK(cudaMalloc(&s->jd, 4 * sizeof(double)));
+  // the launches (~8 per sweep) as one graph, captured once for this q
+  // buffer and sweep count (and again after the step graphs are rebuilt)
+  if (!s->judge_exec || s->judge_q != q || s->judge_sweeps != sweeps) {
+    if (s->judge_exec) cudaGraphExecDestroy(s->judge_exec);
+    s->judge_exec = nullptr;
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t er = record_judge(s, q, sweeps);
+    const cudaError_t ec = cudaStreamEndCapture(s->stream, &gr);
+    cudaError_t ei = cudaSuccess;
+    if (er == cudaSuccess && ec == cudaSuccess) ei = cudaGraphInstantiate(&s->judge_exec, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    CK(er);
+    CK(ec);
+    CK(ei);
+    s->judge_q = q;
+    s->judge_sweeps = sweeps;
+  }
+  CK(cudaMemcpyAsync(s->jd, &scale, sizeof scale, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaGraphLaunch(s->judge_exec, s->stream));
+  double hv[3] = {0.0, 0.0, 0.0};
+  CK(cudaMemcpyAsync(hv, s->jd, sizeof hv, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
-  if (ns_prev) *ns_prev = a;
-  if (ns_pred) *ns_pred = b;
-  if (accepted) *accepted = take ? 1 : 0;
+  if (ns_prev) *ns_prev = hv[1];
+  if (ns_pred) *ns_pred = hv[2];
+  if (accepted) *accepted = hv[2] < hv[1] ? 1 : 0;
   return STRM_OK;
 }
 

@@ -1995,11 +1995,19 @@ __global__ void export_kernel(const double *__restrict__ rhs, const double *__re
   if (fl8) fl8[dn] = flags[o];
 }
 
+// p += scale * q on fluid cells.  With jd (device [scale, norm without,
+// norm with the correction]) the scale is jd[0], and when cond is set the
+// correction is applied only if jd[2] < jd[1] (the judge's choice).
 __global__ void apply_correction_kernel(double *__restrict__ p, const uint8_t *__restrict__ flags,
-                                        Geom g, const float *__restrict__ q, double scale) {
+                                        Geom g, const float *__restrict__ q, double scale,
+                                        const double *__restrict__ jd, int cond) {
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   const int x = blockIdx.y + 1;
   if (y < 1 || y > g.ny - 2 || x > g.nx - 2) return;
+  if (jd) {
+    if (cond && !(jd[2] < jd[1])) return;
+    scale = jd[0];
+  }
   const size_t o = OFF(x, y);
   if (flags[o] != 0) return;
   p[o] = p[o] + scale * (double)q[(size_t)(x - 1) * (g.ny - 2) + (y - 1)];
@@ -2013,10 +2021,10 @@ cudaError_t launch_export(const DevFields &d, const Geom &g, float *rhs32, float
 }
 
 cudaError_t launch_apply_correction(const DevFields &d, const Geom &g, const float *q,
-                                    double scale, cudaStream_t s) {
+                                    double scale, cudaStream_t s, const double *jd, int cond) {
   if (g.nx < 3 || g.ny < 3) return cudaSuccess;
   apply_correction_kernel<<<dim3((g.ny + 127) / 128, g.nx - 2), 128, 0, s>>>(d.p, d.flags, g, q,
-                                                                             scale);
+                                                                             scale, jd, cond);
   return cudaGetLastError();
 }
 
@@ -2319,7 +2327,7 @@ cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_
   return e;
 }
 
-cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s) {
+cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s, int norm) {
   int ty, nt;
   tiles_of(r.g, 1, &ty, &nt);
   if (nt == 0) return cudaSuccess;
@@ -2347,16 +2355,17 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
       sor_black_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
           d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
           d.st, r.itermax);
-    residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
-                                                           d.partials, ty, nt, 0, r.itermax,
-                                                           r.strict_eps, RES_NORM, d.partials_b,
-                                                           bb);
+    if (norm)
+      residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(
+          d.p, d.rhs, d.flags, r.g, r.c, d.st, d.partials, ty, nt, 0, r.itermax, r.strict_eps,
+          RES_NORM, d.partials_b, bb);
   } else {
     for (int color = 0; color < 2; ++color)
       sor_color_kernel<<<sgrid, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, color);
-    residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
-                                                          d.partials, ty, nt, 0, r.itermax,
-                                                          r.strict_eps, RES_NORM, nullptr, 0);
+    if (norm)
+      residual_kernel<true, false><<<nb, kRedBlock, 0, s>>>(d.p, d.rhs, d.flags, r.g, r.c, d.st,
+                                                            d.partials, ty, nt, 0, r.itermax,
+                                                            r.strict_eps, RES_NORM, nullptr, 0);
   }
   return cudaGetLastError();
 }

@@ -85,8 +85,10 @@ cudaError_t launch_velocity(const DevFields &d, const RunCfg &r, cudaStream_t s,
                             int commit_speed, int advance);
 cudaError_t launch_prange(const DevFields &d, const RunCfg &r, cudaStream_t s, int force);
 cudaError_t launch_sor_lex(const DevFields &d, const RunCfg &r, cudaStream_t s);
-// One red-black pressure iteration (copy, red, black, residual) without a stop test.
-cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s);
+// One red-black pressure iteration (copy, red, black, residual) without a
+// stop test; norm = 0 leaves the residual norm out.
+cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream_t s,
+                                 int norm = 1);
 // n FP32 red-black sweeps of the correction equation on the current defect
 // (the inner iteration of the mixed solve), by the configured schedule.
 cudaError_t launch_mixed_sweeps(const DevFields &d, const RunCfg &r, cudaStream_t s, int n);
@@ -106,11 +108,14 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
 cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out, int part);
 
 // Dense FP32 copies ([nx][ny]) of RHS and pressure and the flag bytes (any
-// output may be NULL); p += scale*q on fluid interior cells, q [nx-2][ny-2].
+// output may be NULL); p += scale*q on fluid interior cells, q [nx-2][ny-2]
+// (with jd, device [scale, norm without, norm with]: the scale from jd[0],
+// and when cond only if jd[2] < jd[1]).
 cudaError_t launch_export(const DevFields &d, const Geom &g, float *rhs32, float *p32,
                           uint8_t *fl8, cudaStream_t s);
 cudaError_t launch_apply_correction(const DevFields &d, const Geom &g, const float *q,
-                                    double scale, cudaStream_t s);
+                                    double scale, cudaStream_t s, const double *jd = nullptr,
+                                    int cond = 0);
 
 int residual_blocks(const Geom &g);
 // Blocks of the fused black pass of the FAST FP64 solve (2 partials each).

@@ -78,6 +78,11 @@ class UNet:
         self._finalize()
         self._bufs = {}
         self.step = 0
+        # the stream the forward launches on (None: the default stream; a
+        # capture stream while forward_graphed records), and the recorded
+        # forwards by (input buffer, sizes)
+        self._stream = None
+        self._graphs = {}
 
     # ---- parameters: one flat FP32 buffer (weights, grads, Adam moments) ----
     def _param(self, arr):
@@ -213,7 +218,11 @@ class UNet:
         pool = getattr(self, "_pool", None)
         if pool is None or pool.numel() < total:
             # zeroed once: the forward writes every buffer in full before it
-            # reads it, so views of an earlier shape's data need no clearing
+            # reads it, so views of an earlier shape's data need no clearing.
+            # Recorded forwards point into the old pool: drop them.
+            if self._stream is not None:
+                raise RuntimeError("the forward pool cannot grow while a forward is recorded")
+            self._graphs.clear()
             pool = self._pool = torch.zeros(total, dtype=torch.uint8, device=self.device)
         B = {}
         for (name, hh, ww, c), o in zip(spec, offs):
@@ -226,7 +235,7 @@ class UNet:
     def _conv(self, layer, x, cs_in, y, cs_out, b, h, w, relu=1):
         self._check(self.L.strm_nn_conv3x3(
             x, cs_in, layer.cin_p, self._wbf(layer), layer.kp, self._ptr(layer.b), y,
-            None, cs_out, layer.cout, b, h, w, relu, None), "conv3x3")
+            None, cs_out, layer.cout, b, h, w, relu, self._stream), "conv3x3")
 
     def forward(self, xin, b, h, w, keep: bool = True):
         """xin: BF16 [b][h][w][8] device tensor (see strm_nn_prepare_input).
@@ -235,6 +244,37 @@ class UNet:
         then valid until the next such call."""
         with self._deferred():
             return self._forward(xin, b, h, w, keep)
+
+    def forward_graphed(self, xin, b, h, w):
+        """forward(keep=False) replayed from a CUDA graph, recorded on the
+        first call for this input buffer and these sizes: one launch instead
+        of some twenty host calls, for predictions on small grids, where the
+        host calls take longer than the kernels.  Same kernels, same q
+        buffer (valid until the next forward); the tensor-core kernels'
+        timeout flag is checked after each replay."""
+        import ctypes
+        import torch
+        key = (xin.data_ptr(), b, h, w)
+        rec = self._graphs.get(key)
+        if rec is None:
+            # a plain run first: sizes the pool and configures the kernels
+            self.forward(xin, b, h, w, keep=False)
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            self.L.strm_nn_set_sync(0)
+            try:
+                with torch.cuda.graph(graph):
+                    self._stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+                    q = self._forward(xin, b, h, w, False)
+            finally:
+                self._stream = None
+                self.L.strm_nn_set_sync(1)
+            rec = self._graphs[key] = (graph, q)
+        graph, q = rec
+        graph.replay()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._check(self.L.strm_nn_status(stream), "tensor-core kernels")
+        return q
 
     def _forward(self, xin, b, h, w, keep):
         B = self._buffers(b, h, w) if keep else self._forward_buffers(b, h, w)
@@ -250,35 +290,35 @@ class UNet:
         self._conv(e0a, xin.data_ptr(), IN_CH, ptr("a0"), c0, b, h, w)
         e0 = ptr("cat0") + bf2 * c1
         self._conv(e0b, ptr("a0"), c0, e0, c1 + c0, b, h, w)
-        self._check(L.strm_nn_avgpool(e0, c1 + c0, ptr("p0"), c0, b, h, w, c0, None), "pool")
+        self._check(L.strm_nn_avgpool(e0, c1 + c0, ptr("p0"), c0, b, h, w, c0, self._stream), "pool")
         h1, w1 = h // 2, w // 2
         self._conv(e1a, ptr("p0"), c0, ptr("a1"), c1, b, h1, w1)
         e1 = ptr("cat1") + bf2 * c2
         self._conv(e1b, ptr("a1"), c1, e1, c2 + c1, b, h1, w1)
-        self._check(L.strm_nn_avgpool(e1, c2 + c1, ptr("p1"), c1, b, h1, w1, c1, None), "pool")
+        self._check(L.strm_nn_avgpool(e1, c2 + c1, ptr("p1"), c1, b, h1, w1, c1, self._stream), "pool")
         h2, w2 = h // 4, w // 4
         self._conv(e2a, ptr("p1"), c1, ptr("a2"), c2, b, h2, w2)
         e2 = ptr("cat2") + bf2 * c3
         self._conv(e2b, ptr("a2"), c2, e2, c3 + c2, b, h2, w2)
-        self._check(L.strm_nn_avgpool(e2, c3 + c2, ptr("p2"), c2, b, h2, w2, c2, None), "pool")
+        self._check(L.strm_nn_avgpool(e2, c3 + c2, ptr("p2"), c2, b, h2, w2, c2, self._stream), "pool")
         h3, w3 = h // 8, w // 8
         self._conv(m1, ptr("p2"), c2, ptr("b1"), c3, b, h3, w3)
         self._conv(m2, ptr("b1"), c3, ptr("b2"), c3, b, h3, w3)
         # decoder
-        self._check(L.strm_nn_upsample(ptr("b2"), c3, ptr("cat2"), c3 + c2, b, h2, w2, c3, None),
+        self._check(L.strm_nn_upsample(ptr("b2"), c3, ptr("cat2"), c3 + c2, b, h2, w2, c3, self._stream),
                     "up")
         self._conv(d2a, ptr("cat2"), c3 + c2, ptr("d2a"), c2, b, h2, w2)
         self._conv(d2b, ptr("d2a"), c2, ptr("d2"), c2, b, h2, w2)
-        self._check(L.strm_nn_upsample(ptr("d2"), c2, ptr("cat1"), c2 + c1, b, h1, w1, c2, None),
+        self._check(L.strm_nn_upsample(ptr("d2"), c2, ptr("cat1"), c2 + c1, b, h1, w1, c2, self._stream),
                     "up")
         self._conv(d1a, ptr("cat1"), c2 + c1, ptr("d1a"), c1, b, h1, w1)
         self._conv(d1b, ptr("d1a"), c1, ptr("d1"), c1, b, h1, w1)
-        self._check(L.strm_nn_upsample(ptr("d1"), c1, ptr("cat0"), c1 + c0, b, h, w, c1, None),
+        self._check(L.strm_nn_upsample(ptr("d1"), c1, ptr("cat0"), c1 + c0, b, h, w, c1, self._stream),
                     "up")
         self._conv(d0a, ptr("cat0"), c1 + c0, ptr("d0a"), c0, b, h, w)
         self._conv(d0b, ptr("d0a"), c0, ptr("d0"), c0, b, h, w)
         self._check(L.strm_nn_head(ptr("d0"), c0, c0, self._ptr(self.wh), self._ptr(self.bh),
-                                   ptr("q"), b * h * w, None), "head")
+                                   ptr("q"), b * h * w, self._stream), "head")
         return B["q"]
 
     # ---- backward ----------------------------------------------------------------

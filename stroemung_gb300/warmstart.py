@@ -242,10 +242,11 @@ class WarmStartSolver:
     previous pressure is restored (plain SOR is judge and fallback); then
     tick_solve runs the unchanged solve from there."""
 
-    def __init__(self, sim, net: UNet, judge_sweeps: int = 0):
+    def __init__(self, sim, net: UNet, judge_sweeps: int = 0, graphed: bool = True):
         import torch
         self.sim, self.net = sim, net
         self.judge_sweeps = int(judge_sweeps)
+        self.graphed = bool(graphed)  # replay the network's forward from a CUDA graph
         nx, ny = sim.size
         self.planes = PlaneBatch(1, nx, ny, net.device)
         self.trainer = Trainer(net, nx, ny, sim.cell_size[0], sim.cell_size[1], batch=1)
@@ -265,9 +266,18 @@ class WarmStartSolver:
                                                 tr.pmean.data_ptr(), tr.work2.data_ptr(),
                                                 tr.dx2, tr.xin.data_ptr(), 1, tr.nx, tr.ny,
                                                 None), "prepare")
-        q = self.net.forward(tr.xin, 1, tr.nx - 2, tr.ny - 2, keep=False)
+        if self.graphed:
+            q = self.net.forward_graphed(tr.xin, 1, tr.nx - 2, tr.ny - 2)
+        else:
+            q = self.net.forward(tr.xin, 1, tr.nx - 2, tr.ny - 2, keep=False)
         torch.cuda.synchronize()
         return q, float(tr.smax[0].item()) * tr.dx2
+
+    def warm_up(self):
+        """Records the predictor's graph now (the first prediction does it
+        otherwise); the simulation's state is not changed."""
+        if self.graphed:
+            self.predict()
 
     def judge(self, q, scale):
         """Keeps the correction if it beats the previous pressure on the
@@ -315,6 +325,14 @@ class BatchWarmStart:
         self.batch = batch
         self.members = [WarmStartSolver(s, net, judge_sweeps) for s in batch.sims]
         self.last = {}
+
+    def warm_up(self):
+        """Records every member's predictor graph now.  Two passes: a member
+        whose forward needs a larger pool than the earlier ones drops their
+        recordings, and the second pass finds the pool at its final size."""
+        for _ in range(2):
+            for w in self.members:
+                w.warm_up()
 
     def step(self):
         """One batch step; returns the per-member records of Batch.solve and

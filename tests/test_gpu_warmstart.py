@@ -292,3 +292,75 @@ def test_learned_warm_start_saves_sweeps_on_cavities():
     plain.close()
     wsim.close()
     assert sw <= 0.95 * sp, (sp, sw)
+
+
+def test_recorded_forward_equals_forward():
+    """forward_graphed replays the forward from a CUDA graph: the same bits
+    as forward(keep=False), on the first call, on replays, and after the
+    forward pool grew (the recording is made again)."""
+    import torch
+    net, _ = _net_with_random_head(seed=4)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    x = torch.randn(1, 64, 48, 8, device="cuda", generator=g).to(torch.bfloat16)
+    big = torch.randn(1, 128, 96, 8, device="cuda", generator=g).to(torch.bfloat16)
+    want = net.forward(x, 1, 64, 48, keep=False).clone()
+    for _ in range(3):
+        got = net.forward_graphed(x, 1, 64, 48).clone()
+        assert torch.equal(got, want)
+    net.forward(big, 1, 128, 96, keep=False)
+    x.mul_(-1.0)  # the recording reads the input buffer at replay time
+    want = net.forward(x, 1, 64, 48, keep=False).clone()
+    assert torch.equal(net.forward_graphed(x, 1, 64, 48).clone(), want)
+
+
+@pytest.mark.parametrize("sweeps", [0, 4])
+def test_judge_matches_the_phase_entry_points(sweeps):
+    """strm_judge_correction, its launches recorded as one CUDA graph, gives
+    the norms the phase entry points give for the two candidates (the
+    previous pressure and the corrected one, each after the boundary copy
+    and `sweeps` FP64 red-black iterations), leaves the pressure at the
+    better candidate without the judge's sweeps, and does the same on a
+    second call (a replay)."""
+    import ctypes
+    import torch
+    from stroemung_gb300 import _lib, presets
+    from stroemung_gb300.simulation import ARITH_FAST, Simulation
+    grid = presets.channel(96, 40, [(30, 12, 8, 6), (60, 20, 5, 9)])
+    sim = Simulation(grid=grid, cell_size=(0.01, 0.01), delt=0.002, gamma=0.9, reynolds=200.0,
+                     max_iterations=50, tau=0.5, arithmetic=ARITH_FAST)
+    sim.run_simulation_tick()
+    sim.tick_prepare()
+    nx, ny = sim.size
+    p0 = sim.download("p")
+    g = torch.Generator(device="cuda").manual_seed(3)
+    q = torch.randn(nx - 2, ny - 2, device="cuda", generator=g, dtype=torch.float32)
+    fluid = grid["kind"][1:-1, 1:-1] == 0
+    qn = q.cpu().numpy().astype(np.float64)
+
+    def candidate(scale):
+        p = p0.copy()
+        p[1:-1, 1:-1] = np.where(fluid, p[1:-1, 1:-1] + scale * qn, p[1:-1, 1:-1])
+        return p
+
+    def norm_and_field(p):
+        sim.upload("p", p)
+        sim.copy_pressure_to_boundaries()
+        field = sim.download("p")
+        ns = sim.sor_sweeps(sweeps) if sweeps else sim.calculate_norm_squared()
+        return ns, field
+
+    L = _lib.load()
+    for scale in (1e-4, -3e-2):
+        nb, fb = norm_and_field(candidate(scale))
+        na, fa = norm_and_field(p0)
+        for _ in range(2):
+            sim.upload("p", p0)
+            a, b, acc = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+            _lib.check(L.strm_judge_correction(sim._h, q.data_ptr(), scale, sweeps,
+                                               ctypes.byref(a), ctypes.byref(b),
+                                               ctypes.byref(acc)))
+            assert (a.value, b.value) == (na, nb)
+            assert acc.value == (1 if nb < na else 0)
+            want = fb if nb < na else fa
+            assert np.array_equal(sim.download("p").view(np.int64), want.view(np.int64))
+    sim.close()
