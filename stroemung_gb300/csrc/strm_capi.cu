@@ -316,6 +316,46 @@ int check_device(int *dev_out) {
 
 }  // namespace
 
+namespace {
+
+// The judge's launches on s->stream: both candidates' norms after `sweeps`
+// FP64 red-black iterations (fast arithmetic, the sim's norm; 0: the
+// initial norm after the boundary copy) into jd[2] (with the correction)
+// and jd[1] (without), then the choice, made on the device.
+cudaError_t record_judge(strm_sim *s, const float *q, int sweeps) {
+  const size_t bytes = sizeof(double) * (size_t)s->g.nx * s->g.pitch;
+  DevFields &d = s->d;
+  RunCfg rj = s->cfg;
+  rj.precision = 0;
+  rj.arith = 1;
+  cudaError_t e;
+  auto norm_into = [&](double *dst) -> cudaError_t {
+    cudaError_t err;
+    if (sweeps == 0) {
+      if ((err = launch_pcopy(d, s->g, s->stream)) != cudaSuccess) return err;
+      if ((err = launch_norm(d, s->cfg, s->stream, 0)) != cudaSuccess) return err;
+    } else {
+      for (int k = 0; k < sweeps; ++k)  // the norm after the last iteration only
+        if ((err = launch_sor_iteration(d, rj, s->stream, k + 1 == sweeps)) != cudaSuccess)
+          return err;
+    }
+    return cudaMemcpyAsync(dst, &d.st->aux, sizeof(double), cudaMemcpyDeviceToDevice, s->stream);
+  };
+  if ((e = cudaMemcpyAsync(d.pw, d.p, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 0)) != cudaSuccess) return e;
+  if ((e = norm_into(s->jd + 2)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = norm_into(s->jd + 1)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
+    return e;
+  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 1)) != cudaSuccess) return e;
+  return launch_pcopy(d, s->g, s->stream);
+}
+
+}  // namespace
+
 extern "C" {
 
 int strm_abi_version(void) { return kAbiVersion; }
@@ -745,46 +785,6 @@ int strm_apply_correction(strm_sim *s, const float *q, double scale) {
   CK(cudaStreamSynchronize(s->stream));
   return STRM_OK;
 }
-
-namespace {
-
-// The judge's launches on s->stream: both candidates' norms after `sweeps`
-// FP64 red-black iterations (fast arithmetic, the sim's norm; 0: the
-// initial norm after the boundary copy) into jd[2] (with the correction)
-// and jd[1] (without), then the choice, made on the device.
-cudaError_t record_judge(strm_sim *s, const float *q, int sweeps) {
-  const size_t bytes = sizeof(double) * (size_t)s->g.nx * s->g.pitch;
-  DevFields &d = s->d;
-  RunCfg rj = s->cfg;
-  rj.precision = 0;
-  rj.arith = 1;
-  cudaError_t e;
-  auto norm_into = [&](double *dst) -> cudaError_t {
-    cudaError_t err;
-    if (sweeps == 0) {
-      if ((err = launch_pcopy(d, s->g, s->stream)) != cudaSuccess) return err;
-      if ((err = launch_norm(d, s->cfg, s->stream, 0)) != cudaSuccess) return err;
-    } else {
-      for (int k = 0; k < sweeps; ++k)  // the norm after the last iteration only
-        if ((err = launch_sor_iteration(d, rj, s->stream, k + 1 == sweeps)) != cudaSuccess)
-          return err;
-    }
-    return cudaMemcpyAsync(dst, &d.st->aux, sizeof(double), cudaMemcpyDeviceToDevice, s->stream);
-  };
-  if ((e = cudaMemcpyAsync(d.pw, d.p, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
-    return e;
-  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 0)) != cudaSuccess) return e;
-  if ((e = norm_into(s->jd + 2)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
-    return e;
-  if ((e = norm_into(s->jd + 1)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(d.p, d.pw, bytes, cudaMemcpyDeviceToDevice, s->stream)) != cudaSuccess)
-    return e;
-  if ((e = launch_apply_correction(d, s->g, q, 0.0, s->stream, s->jd, 1)) != cudaSuccess) return e;
-  return launch_pcopy(d, s->g, s->stream);
-}
-
-}  // namespace
 
 int strm_judge_correction(strm_sim *s, const float *q, double scale, int sweeps,
                           double *ns_prev, double *ns_pred, int *accepted) {
