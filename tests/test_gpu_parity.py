@@ -214,8 +214,9 @@ def test_random_layouts_all_boundary_kinds(seed):
 def test_random_layouts_fast_red_black(seed, strict, eps):
     """The FAST red-black solve on random layouts with every boundary kind:
     its boundary copy is split by the colour of the copied cell between the
-    black and the edge passes, the edge pass reads the stale boundary values
-    from the saved copy, and an early stop rolls the next iteration back.
+    black and the red passes, the residuals next to boundary cells read the
+    stale boundary values from the saved copy, and an early stop rolls the
+    next iteration back.
     With these random fields the reference rule stops every solve after one
     or two iterations (a rollback each step), strict eps 1e-3 runs every
     solve to max_iterations, strict eps 100 stops some solves in between.
