@@ -792,11 +792,16 @@ enum : int {
   STOP_RELATIVE = 8,    // stop at ns < eps^2 * (the norm the solve started from)
 };
 
+__device__ __forceinline__ bool stop_rule_of(double ns, const Consts &c, double ns0,
+                                             double ns_start, int strict) {
+  if (strict & STOP_RELATIVE) return ns < c.eps2 * ns_start;
+  if (strict & STOP_STRICT) return ns < c.eps2;
+  return (ns < ns0) || (ns < c.eps2);
+}
+
 __device__ __forceinline__ bool stop_rule(double ns, const Consts &c, const StepState *st,
                                           int strict) {
-  if (strict & STOP_RELATIVE) return ns < c.eps2 * st->ns_start;
-  if (strict & STOP_STRICT) return ns < c.eps2;
-  return (ns < st->ns0) || (ns < c.eps2);
+  return stop_rule_of(ns, c, st->ns0, st->ns_start, strict);
 }
 
 // The norm from the block sums: sum r^2 (and sum r when mean_free, stored
@@ -997,23 +1002,24 @@ __device__ __forceinline__ void store_sums(double acc, double acc1, double *part
   }
 }
 
-// The norm from the black pass's and the red pass's partial sums: each
-// thread adds its entries of the two arrays in that order, then one block
-// sum — one chain of loads and one barrier pair on the critical path of the
-// iteration.
-__device__ __forceinline__ double finish_norm_passes(const double *pa, int na, const double *pb,
-                                                     int nb, bool mean_free,
-                                                     double fluid_cells) {
+// The sums of the black pass's and the red pass's partials: each thread
+// adds its entries of the two arrays in that order, then one block sum —
+// one chain of loads and one barrier pair on the critical path of the
+// iteration.  s2 = sum r^2, s1 = sum r (when mean_free); valid in thread 0.
+__device__ __forceinline__ void sum_partials_passes(const double *pa, int na, const double *pb,
+                                                    int nb, bool mean_free, double &s2,
+                                                    double &s1) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
   const int nt = blockDim.x * blockDim.y;
-  double s2 = 0.0, s1 = 0.0;
+  s2 = 0.0;
+  s1 = 0.0;
   if (!mean_free) {
 #pragma unroll 4
     for (int k = tid; k < na; k += nt) s2 += __ldcg(pa + k);
 #pragma unroll 4
     for (int k = tid; k < nb; k += nt) s2 += __ldcg(pb + k);
     block_sum_pass<false>(s2, s1);
-    return s2 / fluid_cells;
+    return;
   }
 #pragma unroll 4
   for (int k = tid; k < na; k += nt) {
@@ -1026,7 +1032,48 @@ __device__ __forceinline__ double finish_norm_passes(const double *pa, int na, c
     s1 += __ldcg(pb + 2 * k + 1);
   }
   block_sum_pass<true>(s2, s1);
-  return (s2 - s1 * (s1 / fluid_cells)) / fluid_cells;
+}
+
+// What the red pass's stop test needs of the step state, loaded by each
+// block's thread 0 when the pass starts (nothing changes it during the
+// pass but the last block), so that the test waits for no load of its own.
+struct SolveSnap {
+  double ns0, ns_start, fluid_cells;
+  double *hist;
+  unsigned int sor_iters, hist_n, hist_cap;
+};
+
+__device__ __forceinline__ SolveSnap solve_snap(const StepState *st) {
+  SolveSnap sn;
+  sn.ns0 = st->ns0;
+  sn.ns_start = st->ns_start;
+  sn.fluid_cells = st->fluid_cells;
+  sn.hist = st->hist;
+  sn.sor_iters = st->sor_iters;
+  sn.hist_n = st->hist_n;
+  sn.hist_cap = st->hist_cap;
+  return sn;
+}
+
+// solve_iteration_done from a snapshot of the state (one thread).
+template <bool IN_GRAPH>
+__device__ __forceinline__ void solve_iteration_done_snap(StepState *st, const SolveSnap &sn,
+                                                          double ns, const Consts &c,
+                                                          int strict, unsigned int itermax,
+                                                          cudaGraphConditionalHandle h) {
+  const unsigned int it = sn.sor_iters + 1;
+  st->sor_iters = it;
+  st->ns = ns;
+  if (sn.hist && sn.hist_n < sn.hist_cap) {
+    sn.hist[2 * (size_t)sn.hist_n] = (double)it;
+    sn.hist[2 * (size_t)sn.hist_n + 1] = ns;
+    st->hist_n = sn.hist_n + 1;
+  }
+  st->nonfinite = !isfinite(ns);
+  const bool done = stop_rule_of(ns, c, sn.ns0, sn.ns_start, strict);
+  if (done) st->converged = 1;
+  else if (it >= itermax) st->exhausted = 1;
+  if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
 }
 
 // Red pass.  mode 0: update only (the first red pass of a solve, and the
@@ -1055,6 +1102,8 @@ __global__ void __launch_bounds__(256, 4)
                        int mode, cudaGraphConditionalHandle h) {
   const bool sum = mode == 1;
   const bool write = !sum || st->sor_iters + 1 < itermax;
+  __shared__ SolveSnap sn;  // written and read by thread 0 only
+  if (sum && threadIdx.x == 0 && threadIdx.y == 0) sn = solve_snap(st);
   double acc = 0.0, acc1 = 0.0;
   if (sum) {
     const int nt = blockDim.x * blockDim.y;
@@ -1119,11 +1168,13 @@ __global__ void __launch_bounds__(256, 4)
   store_sums<MEAN_FREE>(acc, acc1, partials_r);
   loop_guard<IN_GRAPH>(st, itermax, h);
   if (!last_block_done(&st->counter)) return;
-  const double ns = finish_norm_passes(partials_b, nbb, partials_r, gridDim.x, MEAN_FREE,
-                                       st->fluid_cells);
+  double s2, s1;
+  sum_partials_passes(partials_b, nbb, partials_r, gridDim.x, MEAN_FREE, s2, s1);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const double n = sn.fluid_cells;
+    const double ns = MEAN_FREE ? (s2 - s1 * (s1 / n)) / n : s2 / n;
     st->counter = 0;
-    solve_iteration_done<IN_GRAPH>(st, ns, c, strict, itermax, h);
+    solve_iteration_done_snap<IN_GRAPH>(st, sn, ns, c, strict, itermax, h);
   }
 }
 
