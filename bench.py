@@ -492,7 +492,7 @@ def learned_cavity_block(args):
         torch.cuda.synchronize()
         t_train = time.perf_counter() - t0
         sp = sw = acc = steps = 0
-        t_plain = t_ws = 0.0
+        t_plain = t_ws = t_pred = t_judge = 0.0
         for re in out["held_out_re"]:
             plain = warmstart.make_simulation(presets.cavity(n), re, 1.0 / n, delt=1e-3,
                                               max_iterations=40000)
@@ -509,6 +509,8 @@ def learned_cavity_block(args):
                 steps += 1
                 t_plain += r["solve_plain_ms"]
                 t_ws += r["predict_ms"] + r["judge_ms"] + r["solve_ws_ms"]
+                t_pred += r["predict_ms"]
+                t_judge += r["judge_ms"]
             plain.close()
             wsim.close()
         out[name] = {"loss": loss, "judge_sweeps": judge, "epochs": args.ws_cavity_epochs,
@@ -517,6 +519,7 @@ def learned_cavity_block(args):
                      "sweeps_plain": sp, "sweeps_learned": sw, "sweeps_saved": 1 - sw / sp,
                      "accepted": f"{acc}/{steps}", "ms_plain": t_plain,
                      "ms_learned_incl_predict_and_judge": t_ws,
+                     "predict_ms_per_step": t_pred / steps, "judge_ms_per_step": t_judge / steps,
                      "time_saved": 1 - t_ws / t_plain}
     return out
 
