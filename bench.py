@@ -193,9 +193,9 @@ def run_reference(args):
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
 
 # DRAM traffic from the committed ncu captures of this workload (bytes):
-# one FP64 iteration (red pass 88.9 + 19.6 MB, black pass 72.5 + 1.0 MB)
+# one FP64 iteration (red pass 89.0 + 20.0 MB, black pass 72.5 + 1.1 MB)
 # and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
-SOR_ITERATION_TRAFFIC = (88.9 + 19.6 + 72.5 + 1.0) * 1e6
+SOR_ITERATION_TRAFFIC = (89.0 + 20.0 + 72.5 + 1.1) * 1e6
 SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
 
 
