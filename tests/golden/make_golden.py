@@ -1,9 +1,9 @@
 """Regenerates tests/golden/reference_golden.json from the reference's own tests.
 
-Run in a checkout that has the reference tree mounted (default
-/root/reference, override with STROEMUNG_REF):
+Run it with the reference's source tree given as the first argument or in
+the STROEMUNG_REF environment variable:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path to the stroemung checkout>
 
 It reads, as text, the known-answer tables of src/math.rs:192-402 and
 src/simulation.rs:449-569, the classification tables of
@@ -19,9 +19,10 @@ import ast
 import json
 import os
 import re
+import sys
 from pathlib import Path
 
-REF = Path(os.environ.get("STROEMUNG_REF", "/root/reference"))
+REF: Path = Path()  # the reference checkout, set by main()
 OUT = Path(__file__).resolve().parent / "reference_golden.json"
 
 
@@ -116,6 +117,11 @@ def _edge_list(text: str):
 
 
 def main():
+    global REF
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STROEMUNG_REF", "")
+    if not root:
+        sys.exit("usage: make_golden.py <stroemung checkout>  (or set STROEMUNG_REF)")
+    REF = Path(root)
     # only the #[cfg(test)] modules hold the tables
     math_rs = (REF / "src/math.rs").read_text().split("#[cfg(test)]", 1)[1]
     sim_rs = (REF / "src/simulation.rs").read_text().split("#[cfg(test)]", 1)[1]
