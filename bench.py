@@ -55,6 +55,9 @@ PARAMS = dict(cell_size=(0.01, 0.01), delt=0.005, gamma=0.9, reynolds=400.0,
 # delt is the adaptive rule's value at t = 0 (u = 1): 0.5 * min(Re/2/(2/dx^2), dx/1)
 CELLS = IMAX * JMAX
 L2_BYTES = 129e6
+# the warm-start network's parameters, trained at 512 x 128 outside the
+# benchmark (python -m stroemung_gb300.train_warmstart)
+WS_WEIGHTS = ROOT / "stroemung_gb300" / "weights" / "warmstart_unet_channel_512x128.npy"
 
 
 def load_peaks():
@@ -136,17 +139,25 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_sample(grid, k_iters: float, ticks: int, cap: int):
-    """Times the oracle on the host: `ticks` ticks of the full workload with the
-    solve capped at `cap` iterations; returns the per-step time for a step of
-    k_iters iterations (phase times measured, iterations scaled)."""
+def oracle_sim(grid):
+    """The oracle (the reference's algorithm restated in C: lexicographic SOR
+    in its x-major order, FP64, one thread) on `grid` with the workload's
+    parameters."""
     from oracle import oracle as orc
     orc.build()
     p = PARAMS
-    o = orc.OracleSim(kind=grid["kind"], wall_uv=grid["wall_uv"], u=grid["u"], v=grid["v"],
-                      p=grid["p"], dx=p["cell_size"][0], dy=p["cell_size"][1], delt=p["delt"],
-                      gamma=p["gamma"], reynolds=p["reynolds"], eps=p["sor_absolute_epsilon"],
-                      omega=p["omega"], max_iterations=p["max_iterations"], tau=p["tau"])
+    return orc.OracleSim(kind=grid["kind"], wall_uv=grid["wall_uv"], u=grid["u"], v=grid["v"],
+                         p=grid["p"], dx=p["cell_size"][0], dy=p["cell_size"][1],
+                         delt=p["delt"], gamma=p["gamma"], reynolds=p["reynolds"],
+                         eps=p["sor_absolute_epsilon"], omega=p["omega"],
+                         max_iterations=p["max_iterations"], tau=p["tau"])
+
+
+def cpu_phases(grid, ticks: int, cap: int):
+    """Times `ticks` oracle ticks of the full workload with the solve capped
+    at `cap` iterations: mean seconds before the solve, per solve iteration
+    and after it, and the wall time."""
+    o = oracle_sim(grid)
     pre, it_s, post = [], [], []
     t0 = time.perf_counter()
     for _ in range(ticks):
@@ -156,38 +167,88 @@ def cpu_sample(grid, k_iters: float, ticks: int, cap: int):
         if n > 0:
             it_s.append(b / n)
     wall = time.perf_counter() - t0
-    t_iter = statistics.mean(it_s) if it_s else 0.0
-    t_step = statistics.mean(pre) + k_iters * t_iter + statistics.mean(post)
-    return t_step, t_iter, wall
+    return (statistics.mean(pre), statistics.mean(it_s) if it_s else 0.0,
+            statistics.mean(post), wall)
+
+
+def cpu_sample(grid, k_iters: float, ticks: int, cap: int):
+    """The oracle's step time for a step of k_iters iterations, from `ticks`
+    capped ticks (phase times measured, iterations scaled)."""
+    pre, t_iter, post, wall = cpu_phases(grid, ticks, cap)
+    return pre + k_iters * t_iter + post, t_iter, wall
 
 
 def run_reference(args):
+    """The reference arm: the oracle on the host, one thread (the reference's
+    ndarray loops are single-threaded), on the same workload.  Each of the
+    warmup + steps samples is one tick with the solve capped at --ref-cap
+    iterations, its step time modelled as pre-solve + max_iterations x the
+    per-iteration time + post-solve (every step this workload's GPU arm times
+    runs max_iterations); then the first 1 + --ref-full-steps uncapped ticks
+    from the workload's start are timed whole, and the model's error against
+    the ticks after the first (which run max_iterations) is reported."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     grid = workload(SEED)
     k = PARAMS["max_iterations"]
-    times = []
+    phases = []
     for i in range(args.warmup + args.steps):
-        t_step, t_iter, _ = cpu_sample(grid, k, 1, args.ref_cap)
+        ph = cpu_phases(grid, 1, args.ref_cap)
         if i >= args.warmup:
-            times.append(t_step)
-    t = statistics.mean(times)
+            phases.append(ph)
+    pre = statistics.mean(x[0] for x in phases)
+    t_iter = statistics.mean(x[1] for x in phases)
+    post = statistics.mean(x[2] for x in phases)
+    t = pre + k * t_iter + post
     value = CELLS / t
     sample = (f"each step: one oracle tick of the full 4096x1024 workload with the pressure "
               f"solve capped at {args.ref_cap} iterations; step time = measured pre-solve + "
               f"{k} x measured per-iteration + measured post-solve time ({k} = "
               f"max_iterations, what this configuration's solve runs per step)")
-    print(json.dumps({
+    full = None
+    if args.ref_full_steps > 0:
+        # whole ticks from the workload's start: the first tick's solve stops
+        # after a few iterations (its norm drops below the initial norm at
+        # once); from the second on every tick runs max_iterations, as in the
+        # window the GPU arm times, so the model is checked on those
+        o = oracle_sim(grid)
+        ticks = []
+        for i in range(1 + args.ref_full_steps):
+            t0 = time.perf_counter()
+            it, ns = o.tick()
+            ticks.append((it, time.perf_counter() - t0))
+            print(f"reference tick {i + 1}: {it} iterations, norm {ns:.6e}, "
+                  f"{ticks[-1][1]:.2f} s", file=sys.stderr, flush=True)
+        long_ticks = [w for it, w in ticks[1:] if it == k] or [w for _, w in ticks[1:]]
+        its = [it for it, _ in ticks[1:]]
+        measured = statistics.mean(long_ticks)
+        model = pre + statistics.mean(its) * t_iter + post
+        full = {"ticks": [{"sor_iterations": it, "ms": w * 1e3} for it, w in ticks],
+                "measured_full_step_ms": measured * 1e3, "model_full_step_ms": model * 1e3,
+                "model_error": (model - measured) / measured,
+                "measured_value": CELLS / measured,
+                "bound": "the model is accepted when |model_error| <= 0.05",
+                "note": "uncapped oracle ticks from the workload's start, timed whole; "
+                        "measured_full_step_ms averages the ticks after the first (each runs "
+                        f"{k} iterations); the model is the sampled steps' pre-solve + "
+                        "iterations x per-iteration + post-solve time for the same iteration "
+                        "counts"}
+    line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(args),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(args, reference=True),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": 1, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "host_cpu": os.uname().machine,
+                         "nproc": os.cpu_count()},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-    }))
+    }
+    if full is not None:
+        line["full_step"] = full
+    print(json.dumps(line))
 
 
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
@@ -199,11 +260,13 @@ SOR_ITERATION_TRAFFIC = (89.0 + 20.0 + 72.5 + 1.1) * 1e6
 SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
 
 
-def config_dict(args):
+def config_dict(args, reference: bool = False):
+    solver = ("lexicographic SOR (x outer, y inner), FP64, the reference's operation order, "
+              "one thread" if reference else f"red-black SOR, FP64, {args.arith} arithmetic")
     return {"workload": "channel 4096x1024, 64 rectangles (seed 0), Re 400, tau 0.5, "
                         "eps 1e-3, max_iterations 2000",
             "imax": IMAX, "jmax": JMAX, "obstacles": NRECTS,
-            "solver": f"red-black SOR, FP64, {args.arith} arithmetic",
+            "solver": solver,
             "stop_rule": "reference (ns < initial norm or ns < eps^2)",
             "l2": "per-step working set (9 FP64 fields + flags, 285 MB) exceeds the 129 MB L2; "
                   "no flush", "parallelism": f"replicas x{args.gpus}"}
@@ -344,12 +407,84 @@ def mixed_block(args, grid, fp64_ms_step, peak):
                                 "algorithmic_bytes": sw_bytes,
                                 "traffic": SWEEP_TRAFFIC,
                                 "traffic_note": "ncu dram__bytes read+write of one blocked "
-                                                "launch (4 sweeps) divided by 4, cold cache "
-                                                "(profiles/sor32_blocked_sweeps_channel_"
-                                                "4096x1024.md): the sweeps read e, s and the "
-                                                "flags once per launch"},
+                                                "launch (4 sweeps) of this workload divided "
+                                                "by 4, cold cache: the sweeps read e, s and "
+                                                "the flags once per launch"},
         "dtype": "f32 stencil and sweeps, f64 norm/refinement/dt",
     }
+
+
+def run_lengths(xs):
+    """[[count, value], ...] of consecutive equal values."""
+    out = []
+    for x in xs:
+        if out and out[-1][1] == x:
+            out[-1][0] += 1
+        else:
+            out.append([1, x])
+    return out
+
+
+def full_run_block(args, grid):
+    """The whole configuration: --full-steps steps (500) of the workload from
+    its start, in FP64 (fast arithmetic) and in mixed precision.  Each step is
+    issued as its two graph halves (boundary pass, F/G, RHS; pressure solve,
+    velocity update) with CUDA events around each, so the time of both
+    phases is measured per step."""
+    import torch
+    from stroemung_gb300.simulation import ARITH_FAST, PREC_FP64, PREC_MIXED, Simulation
+    out = {}
+    n = args.full_steps
+    for label, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        kw = dict(grid=grid, arithmetic=ARITH_FAST, precision=prec,
+                  inner_sweeps=args.inner_sweeps, **PARAMS)
+        sched = 0
+        if prec == PREC_MIXED:
+            tmp = Simulation(**kw)
+            tmp.step_n(1)
+            sched, _ = tmp.autotune_sweeps(reps=2)
+            tmp.close()
+        sim = Simulation(sweep_schedule=sched, **kw)
+        stream = torch.cuda.ExternalStream(sim.device_view()["stream"])
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(n)]
+        iters = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(n):
+            ev[k][0].record(stream)
+            sim.tick_prepare()
+            ev[k][1].record(stream)
+            it, _ = sim.tick_solve()
+            ev[k][2].record(stream)
+            iters.append(it)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        prep = [ev[k][0].elapsed_time(ev[k][1]) for k in range(n)]
+        solve = [ev[k][1].elapsed_time(ev[k][2]) for k in range(n)]
+        dev_s = (sum(prep) + sum(solve)) / 1e3
+        itermax = PARAMS["max_iterations"]
+        full = [k for k, it in enumerate(iters) if it >= itermax]
+        short = [it for it in iters if it < itermax]
+        out[label] = {
+            "steps": n, "device_s": dev_s, "wall_s": wall,
+            "value": CELLS * n / dev_s, "unit": "cell-updates/s",
+            "prepare_ms_total": sum(prep), "solve_ms_total": sum(solve),
+            "prepare_ms_per_step": sum(prep) / n,
+            "solve_ms_per_step_at_itermax": statistics.mean(solve[k] for k in full) if full
+            else None,
+            "solve_ms_per_step_below_itermax": statistics.mean(
+                solve[k] for k in range(n) if iters[k] < itermax) if short else None,
+            "sweeps_total": sum(iters), "steps_at_itermax": len(full),
+            "last_step_at_itermax": (full[-1] + 1) if full else None,
+            "mean_sweeps_below_itermax": statistics.mean(short) if short else None,
+            "sweeps_per_step": run_lengths(iters)}
+        if prec == PREC_MIXED:
+            out[label]["sweep_schedule"] = sched
+        sim.close()
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["device_s"] / out["mixed"]["device_s"]
+    out["note"] = ("device_s sums the two halves' CUDA-event times of every step; wall_s "
+                   "includes the host's per-step read of the iteration count")
+    return out
 
 
 def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
@@ -361,11 +496,15 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
     from stroemung_gb300 import warmstart
     from stroemung_gb300.simulation import PREC_MIXED, ARITH_FAST, Simulation
     from stroemung_gb300.unet import UNet
+    from stroemung_gb300.train_warmstart import load_weights
     net = UNet(seed=0)
     train_info = {}
-    if args.ws_weights:
-        net.load_state_dict({"theta": np.load(args.ws_weights), "step": 1})
-        train_info["weights"] = os.path.basename(args.ws_weights)
+    weights = args.ws_weights or (str(WS_WEIGHTS) if WS_WEIGHTS.exists() else "")
+    if weights:
+        sha = load_weights(net, weights)
+        train_info = {"weights": os.path.basename(weights), "weights_sha256": sha,
+                      "note": "trained outside the benchmark by stroemung_gb300.train_warmstart "
+                              "(512 x 128 channel snapshots, Adam, batch 32, error loss)"}
     else:
         t0 = time.perf_counter()
         train = warmstart.generate_snapshots(args.ws_snapshots, imax=512, jmax=128,
@@ -409,7 +548,7 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
     mk = dict(precision=PREC_MIXED, inner_sweeps=args.inner_sweeps, arithmetic=ARITH_FAST)
     plain = Simulation(grid=grid, **mk, **PARAMS)
     wsim = Simulation(grid=grid, **mk, **PARAMS)
-    ws = warmstart.WarmStartSolver(wsim, net)
+    ws = warmstart.WarmStartSolver(wsim, net, judge_sweeps=args.ws_judge_sweeps)
     ws.warm_up()
     scratch = torch.zeros(IMAX + 2, JMAX + 2, dtype=torch.float64, device="cuda")
     plain.step_n(args.warmup)
@@ -457,8 +596,11 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
                 "tensor_frac_of_measured_bf16": (flops / fwd_ms / 1e9) / BF16_PEAK,
                 "params": net.parameter_count()},
         "training": train_info,
+        "judge_sweeps": args.ws_judge_sweeps,
         "note": "the reference stop rule runs 2000 sweeps in every step of this workload, so no "
-                "warm start can save sweeps here; see learned_cavity for a converging case",
+                "warm start can save sweeps here; sweeps_to_plain_norm counts the sweeps each "
+                "run needs to reach the plain run's norms; see learned_cavity for a converging "
+                "case",
     }
 
 
@@ -561,6 +703,65 @@ def cavity_block(args):
     return out
 
 
+def cavity_run(args):
+    """The 2048 x 2048 lid-driven cavity (Re 1000, omega 1.8, tau 0.5, eps
+    1e-5 on the residual relative to each solve's starting norm) for
+    --cavity-run steps, FP64 (fast arithmetic) and mixed precision stepped in
+    lockstep from the same state, each solve capped at --cavity-run-itermax
+    sweeps.  Per step: device time, sweeps and the relative residual each
+    solve reached (from its residual history); every --cavity-run-every steps
+    the fields' relative L2 and max error of mixed against FP64.  Prints one
+    JSON document (not a benchmark line)."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import presets
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    n = args.cavity_n
+    grid = presets.cavity(n)
+    fluid = grid["kind"] == 0
+    cfg = dict(grid=grid, cell_size=(1.0 / n, 1.0 / n), delt=1e-4, gamma=0.9,
+               reynolds=1000.0, sor_absolute_epsilon=1e-5,
+               max_iterations=args.cavity_run_itermax, omega=1.8, tau=0.5,
+               arithmetic=ARITH_FAST, strict_eps=2)
+    tmp = Simulation(precision=PREC_MIXED, **cfg)
+    tmp.step_n(1)
+    sched, _ = tmp.autotune_sweeps(reps=2)
+    tmp.close()
+    sims = {"fp64": Simulation(precision=PREC_FP64, **cfg),
+            "mixed": Simulation(precision=PREC_MIXED, sweep_schedule=sched, **cfg)}
+    streams = {k: torch.cuda.ExternalStream(v.device_view()["stream"]) for k, v in sims.items()}
+    rows = {k: {"ms": [], "sweeps": [], "rel_residual": [], "converged": []} for k in sims}
+    errors = []
+    for step in range(1, args.cavity_run + 1):
+        for k, sim in sims.items():
+            ms, st = timed_steps(sim, 1, streams[k])
+            h = sim.residual_history()
+            rel = float(np.sqrt(h[-1, 1] / h[0, 1])) if len(h) and h[0, 1] > 0 else None
+            rows[k]["ms"].append(ms)
+            rows[k]["sweeps"].append(int(st[0][0]))
+            rows[k]["rel_residual"].append(rel)
+            rows[k]["converged"].append(bool(st[0][3]))
+        if step % args.cavity_run_every == 0 or step == args.cavity_run:
+            f = {k: {n_: sim.download(n_) for n_ in ("u", "v", "p")} for k, sim in sims.items()}
+            errors.append({"step": step, **field_errors(f["mixed"], f["fp64"], fluid)})
+    for sim in sims.values():
+        sim.close()
+    out = {"grid": f"{n}x{n}", "steps": args.cavity_run,
+           "max_iterations": args.cavity_run_itermax, "sweep_schedule_mixed": sched,
+           "stop_rule": "ns < (1e-5)^2 x the norm the solve starts from, capped at "
+                        "max_iterations sweeps",
+           "errors_mixed_vs_fp64": errors}
+    for k, r in rows.items():
+        out[k] = {"device_s": sum(r["ms"]) / 1e3,
+                  "ms_per_step_median": statistics.median(r["ms"]),
+                  "steps_converged": sum(r["converged"]),
+                  "sweeps_per_step": run_lengths(r["sweeps"]),
+                  "rel_residual_per_step": r["rel_residual"],
+                  "ms_per_step": r["ms"]}
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["device_s"] / out["mixed"]["device_s"]
+    print(json.dumps(out))
+
+
 def time_to_residual(n, steps):
     """Poisson time-to-residual where the solve converges: the n x n cavity
     (Re 1000, omega 1.8, eps 1e-5 relative to each solve's starting norm),
@@ -589,18 +790,17 @@ def time_to_residual(n, steps):
     return out
 
 
-def batched_block(args):
-    """Channel instances of uneven sizes (imax in 128..2048 step 128, jmax in
-    32..512 step 32, Re log-uniform in [50, 1000], 1..16 rectangles), stepped
-    as one batch vs one after another on the plain FP64 path."""
+def batch_specs(n: int):
+    """n channel instances of uneven sizes (imax in 128..2048 step 128, jmax
+    in 32..512 step 32, Re log-uniform in [50, 1000], 1..16 rectangles with
+    the channel workload's placement rules), seeded; and their solver
+    settings (mixed-precision members need ARITH_FAST here)."""
     import numpy as np
-    import torch
     from stroemung_gb300 import presets
-    from stroemung_gb300.batch import Batch
-    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    from stroemung_gb300.simulation import ARITH_FAST
     rng = np.random.default_rng(4)
     specs = []
-    for k in range(args.batch_n):
+    for k in range(n):
         imax = int(rng.integers(1, 17)) * 128
         jmax = int(rng.integers(1, 17)) * 32
         re = float(np.exp(rng.uniform(np.log(50.0), np.log(1000.0))))
@@ -611,6 +811,91 @@ def batched_block(args):
         specs.append((presets.channel(imax, jmax, rects), re, imax * jmax))
     cfg = dict(cell_size=(0.01, 0.01), delt=0.005, gamma=0.9, sor_absolute_epsilon=1e-3,
                max_iterations=2000, omega=1.7, tau=0.5, arithmetic=ARITH_FAST)
+    return specs, cfg
+
+
+def batch_run(args):
+    """--batch-run steps of the --batch-n channel instances as one batch, the
+    members' mixed-precision solves as one persistent kernel per step, and in
+    lockstep a second copy with the graph's WHILE loop; afterwards every
+    member's u, v, p are compared bit for bit.  Then every instance one after
+    another on the plain FP64 path (one warm step, one timed step each: the
+    sequential baseline, which costs minutes per step over all instances).
+    Prints one JSON document (not a benchmark line)."""
+    import numpy as np
+    import torch
+    from stroemung_gb300.batch import Batch
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, Simulation
+    specs, cfg = batch_specs(args.batch_n)
+    cells = sum(c for _, _, c in specs)
+    sets = {}
+    for mode in ("persistent", "graph_loop"):
+        sims = [Simulation(grid=g, reynolds=re, precision=PREC_MIXED, inner_sweeps=16, **cfg)
+                for g, re, _ in specs]
+        sets[mode] = (sims, Batch(sims))
+    bp, bg = sets["persistent"][1], sets["graph_loop"][1]
+    best, sched_ms = bg.autotune(reps=1)
+    for b in (bp, bg):
+        b.set_schedule(best)
+    bp.set_solver(True)
+    rows = {"persistent": [], "graph_loop": []}
+    sweeps = []
+    for step in range(args.batch_run):
+        for mode, b in (("persistent", bp), ("graph_loop", bg)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = b.step(1)
+            rows[mode].append(time.perf_counter() - t0)
+            if mode == "persistent":
+                sweeps.append(st["sor_iterations"][:, 0].astype(int))
+    identical = True
+    for a, b in zip(sets["persistent"][0], sets["graph_loop"][0]):
+        for name in ("u", "v", "p"):
+            if not np.array_equal(a.download(name), b.download(name)):
+                identical = False
+    for sims, b in sets.values():
+        b.close()
+        for sim in sims:
+            sim.close()
+    sw = np.array(sweeps)  # [step][member]
+    t_seq, c_seq = 0.0, 0
+    for g, re, c in specs:
+        sim = Simulation(grid=g, reynolds=re, precision=PREC_FP64, **cfg)
+        sim.run_simulation_tick()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.step_n(1)
+        t_seq += time.perf_counter() - t0
+        c_seq += c
+        sim.close()
+    out = {"instances": len(specs), "cells": cells, "steps": args.batch_run,
+           "sweep_schedule": best,
+           "fields_identical_persistent_vs_graph_loop": identical,
+           "sweeps_per_step_mean": [float(x) for x in sw.mean(axis=1)],
+           "sweeps_total": int(sw.sum()),
+           "sequential_fp64": {"value": c_seq / t_seq, "unit": "cell-updates/s",
+                               "sample": "every instance, its second step (the first "
+                                         "untimed), one after another"}}
+    for mode, r in rows.items():
+        out[mode] = {"s_total": sum(r), "value": cells * len(r) / sum(r),
+                     "unit": "cell-updates/s", "ms_per_step_first": r[0] * 1e3,
+                     "ms_per_step_median": statistics.median(r) * 1e3}
+    out["steps_1_2_batch_vs_sequential_fp64"] = (
+        cells * 2 / sum(rows["persistent"][:2])) / out["sequential_fp64"]["value"] \
+        if len(rows["persistent"]) >= 2 else None
+    print(json.dumps(out))
+
+
+def batched_block(args):
+    """Channel instances of uneven sizes (imax in 128..2048 step 128, jmax in
+    32..512 step 32, Re log-uniform in [50, 1000], 1..16 rectangles), stepped
+    as one batch vs one after another on the plain FP64 path."""
+    import numpy as np
+    import torch
+    from stroemung_gb300 import presets
+    from stroemung_gb300.batch import Batch
+    from stroemung_gb300.simulation import PREC_FP64, PREC_MIXED, ARITH_FAST, Simulation
+    specs, cfg = batch_specs(args.batch_n)
     cells = sum(c for _, _, c in specs)
     sims = [Simulation(grid=g, reynolds=re, precision=PREC_MIXED, inner_sweeps=16, **cfg)
             for g, re, _ in specs]
@@ -622,6 +907,13 @@ def batched_block(args):
     st = batch.step(args.batch_steps)
     torch.cuda.synchronize()
     t_batch = (time.perf_counter() - t0) / args.batch_steps
+    # the same members' next steps with the solves as one persistent kernel
+    batch.set_solver(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st_p = batch.step(args.batch_steps)
+    torch.cuda.synchronize()
+    t_persist = (time.perf_counter() - t0) / args.batch_steps
     batch.close()
     for s in sims:
         s.close()
@@ -652,6 +944,11 @@ def batched_block(args):
         "sweep_schedule": {"chosen": best, "ms_per_batch_step": {str(k): v for k, v in
                                                                  sched_ms.items()}},
         "sor_iterations_mean": float(np.mean(st["sor_iterations"])),
+        "persistent": {"value": cells / t_persist, "unit": "cell-updates/s",
+                       "ms_per_batch_step": t_persist * 1e3,
+                       "sor_iterations_mean": float(np.mean(st_p["sor_iterations"])),
+                       "note": "the next steps of the same members with each step's "
+                               "pressure solves as one persistent cooperative kernel"},
         "solver": "mixed precision (FP32 sweeps, FP64 norm/refinement), reference stop rule, "
                   "eps 1e-3, max_iterations 2000; one graph per step",
         "learned": learned,
@@ -760,6 +1057,9 @@ def main():
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-cap", type=int, default=10)
+    ap.add_argument("--ref-full-steps", type=int, default=1,
+                    help="reference arm: uncapped oracle ticks after the first, timed whole "
+                         "beside the samples")
     ap.add_argument("--cpu-ticks", type=int, default=3)
     ap.add_argument("--cpu-cap", type=int, default=50)
     ap.add_argument("--eager", type=int, default=0,
@@ -770,6 +1070,8 @@ def main():
     ap.add_argument("--mixed", type=int, default=1)
     ap.add_argument("--err-steps", type=int, default=100,
                     help="steps after which mixed precision is compared with FP64")
+    ap.add_argument("--full-steps", type=int, default=500,
+                    help="steps of the whole-run block (FP64 and mixed from the start); 0 skips")
     ap.add_argument("--learned", type=int, default=1)
     ap.add_argument("--ws-weights", default="", help="trained U-Net parameters (.npy)")
     ap.add_argument("--ws-snapshots", type=int, default=1024)
@@ -783,12 +1085,20 @@ def main():
     ap.add_argument("--cavity-n", type=int, default=2048)
     ap.add_argument("--cavity-steps", type=int, default=3)
     ap.add_argument("--cavity-itermax", type=int, default=20000)
+    ap.add_argument("--cavity-run", type=int, default=0,
+                    help="run the cavity for this many steps, FP64 and mixed in lockstep, "
+                         "and print a JSON report instead of the benchmark")
+    ap.add_argument("--cavity-run-itermax", type=int, default=2000)
+    ap.add_argument("--cavity-run-every", type=int, default=50)
     ap.add_argument("--cavity-small", type=int, default=256,
                     help="size of a cavity whose solves converge (time-to-residual); 0 skips")
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-seq-sample", type=int, default=16)
+    ap.add_argument("--batch-run", type=int, default=0,
+                    help="step the batch this many steps, persistent and graph loop in "
+                         "lockstep, and print a JSON report instead of the benchmark")
     ap.add_argument("--batch-learned", type=int, default=1,
                     help="also step the batch with the learned warm start")
     ap.add_argument("--batch-ws-snapshots", type=int, default=512)
@@ -798,6 +1108,12 @@ def main():
     args = ap.parse_args()
     if args.profile:
         profile_target(args.profile, max(args.steps if args.steps != 10 else 1, 1))
+        return
+    if args.cavity_run > 0:
+        cavity_run(args)
+        return
+    if args.batch_run > 0:
+        batch_run(args)
         return
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -941,14 +1257,23 @@ def main():
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": sor_bytes,
                      # DRAM bytes of one iteration's kernels (red and black
-                     # passes) in one ncu capture of this workload, cold cache:
-                     # profiles/fp64_sor_kernels_channel_4096x1024.md
+                     # passes) in one ncu capture of this workload, cold cache
                      "traffic": SOR_ITERATION_TRAFFIC,
                      "traffic_note": "ncu dram__bytes read+write of one iteration's kernels, "
                                      "cold cache; each colour pass touches the whole of p and "
-                                     "rhs (the colours interleave within cache lines)"},
+                                     "rhs (the colours interleave within cache lines)",
+                     # the pipe that binds the FP64 iteration: its FP64
+                     # operations per second against the FP64 instruction
+                     # rate of a DGEMM measured here (2 FLOP per FMA)
+                     "fp64_pipe_frac": (ops / t_iter) / (fp64_peak * 1e12 / 2) if fp64_peak
+                     else None,
+                     "fp64_pipe_note": "FP64 add/mul/fma instructions per second of the "
+                                       "iteration over half the measured DGEMM FLOP rate (one "
+                                       "FMA per two FLOP): the fraction of the FP64 pipe the "
+                                       "iteration keeps busy"},
         "fp64": {"ops_per_iteration": ops, "achieved_tflops": ops / t_iter / 1e12,
                  "dgemm_tflops_measured": fp64_peak,
+                 "pipe_ops_per_s_peak": fp64_peak * 1e12 / 2 if fp64_peak else None,
                  "note": "FP64 pipe operations (add, mul, fma each 1) of the solve"},
         "e2e": e2e,
         "clocks": clocks.summary(),
@@ -982,6 +1307,8 @@ def main():
         if args.mixed:
             guarded("mixed_precision", lambda: mixed_block(args, grid, fp64_ms_step, peak))
             mixed_ms = out["mixed_precision"].get("ms_per_step")
+        if args.full_steps > 0:
+            guarded("full_run", lambda: full_run_block(args, grid))
         if args.learned:
             guarded("learned", lambda: learned_block(args, grid, fp64_ms_step, mixed_ms))
             guarded("learned_cavity", lambda: learned_cavity_block(args))

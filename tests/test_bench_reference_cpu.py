@@ -21,7 +21,8 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     monkeypatch.setattr(bench, "NRECTS", 4)
     monkeypatch.setattr(bench, "CELLS", 256 * 64)
     monkeypatch.delenv("RANK", raising=False)
-    args = argparse.Namespace(gpus=1, steps=2, warmup=1, ref_cap=3, arith="fast")
+    args = argparse.Namespace(gpus=1, steps=2, warmup=1, ref_cap=3, ref_full_steps=1,
+                              arith="fast")
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(args)
@@ -39,6 +40,12 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert d["config"]["solver"].startswith("lexicographic SOR")
+    full = d["full_step"]
+    assert len(full["ticks"]) == 2 and full["measured_full_step_ms"] > 0
+    assert all(t["sor_iterations"] >= 1 for t in full["ticks"])
+    # the extrapolation and the whole-tick measurement describe the same tick
+    assert abs(full["model_error"]) < 0.5, full
 
 
 def test_reference_arm_prints_nothing_on_other_ranks(monkeypatch):
@@ -47,5 +54,5 @@ def test_reference_arm_prints_nothing_on_other_ranks(monkeypatch):
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(argparse.Namespace(gpus=2, steps=1, warmup=1, ref_cap=1,
-                                               arith="fast"))
+                                               ref_full_steps=1, arith="fast"))
     assert out.getvalue() == ""
