@@ -64,8 +64,12 @@ enum {
                                   bit-identical to the reference, for small grids */
 };
 
-/* Arithmetic of the pressure solve.  Boundary conditions, F/G, RHS and the
- * velocity update always follow the reference's operation order exactly. */
+/* Arithmetic of the FP64 step.  EXACT keeps the reference's operation order
+ * everywhere (bit-identical boundary pass, F/G, RHS and velocity update).
+ * FAST uses fused multiply-adds and reciprocal multiplies in the pressure
+ * solve, F/G/RHS as face fluxes computed once per face, and a fused velocity
+ * update: those pointwise kernels stay within 1e-12 relative of the
+ * reference's; the boundary pass and classification stay exact. */
 enum {
     STRM_ARITH_EXACT = 0, /* reference operation order, correctly rounded divisions */
     STRM_ARITH_FAST = 1   /* fused multiply-adds and reciprocal multiplies */
@@ -304,6 +308,20 @@ int strm_batch_prepare(strm_batch *batch);
 int strm_batch_solve(strm_batch *batch, strm_step_stats *stats);
 /* Blocked sweep schedule of the batch (2..STRM_SWEEPS_COUNT-1). */
 int strm_batch_set_schedule(strm_batch *batch, int schedule);
+/* How a batch step issues the members' pressure solves (no reference
+ * counterpart): STRM_BATCH_GRAPH_LOOP as a WHILE loop of table-driven graph
+ * kernels (the default); STRM_BATCH_PERSISTENT as one persistent cooperative
+ * kernel per step whose CTAs walk the members' tile tables phase by phase,
+ * with a grid barrier between phases.  Results are identical.  A barrier
+ * wait gives up after wait_limit polls (0: about a second or two); the CTA
+ * then flags the step, every CTA returns, and the step returns
+ * STRM_ERR_TIMEOUT with the members' fields partly solved (no fault, the
+ * context stays usable). */
+enum {
+    STRM_BATCH_GRAPH_LOOP = 0,
+    STRM_BATCH_PERSISTENT = 1
+};
+int strm_batch_set_solver(strm_batch *batch, int solver, uint64_t wait_limit);
 /* Times `reps` whole batch steps under each blocked schedule (members'
  * u, v, p and step state restored afterwards), keeps the fastest; best and
  * ms_per_step[STRM_SWEEPS_COUNT] (per schedule, [0] the best) may be NULL. */
@@ -326,22 +344,29 @@ int strm_residual_history(strm_sim *sim, double *out, int cap, int *n);
 int strm_autotune_sweeps(strm_sim *sim, int reps, int *best, double *ms_per_sweep);
 
 /* Residual norm that allocates nothing.  No counterpart in the reference.
- * For callers that cannot allocate device memory when they need the norm:
- * code running inside a CUDA stream capture (cudaMalloc is not permitted
- * there), host frameworks whose own memory pool owns the device budget, and
- * fixed-footprint real-time loops.  Same quantity as
- * strm_calculate_norm_squared (sum of squared residuals over the interior
- * cells divided by fluid_cells, reference operation order) on caller-owned
- * pitched fields p and rhs ([nx][pitch], y contiguous); the result is written
- * to the device double *norm_squared, asynchronously on `stream` (a
- * cudaStream_t, NULL for the default stream).
+ * For callers that must not allocate device memory once they are running:
+ * host frameworks whose caching allocator owns the device budget (a
+ * cudaMalloc beside that pool can fail or fragment it) and fixed-footprint
+ * loops that reserve all memory at start-up (cudaMalloc may synchronise the
+ * device and has no latency bound).  Computes the quantity that
+ * strm_calculate_norm_squared returns under the default STRM_NORM_ALL_INTERIOR
+ * (sum of squared residuals over every interior cell divided by fluid_cells,
+ * reference operation order; the other norm_cells modes are not offered
+ * here), equal to it within rounding: the partial sums are added in another
+ * order.  p and rhs are caller-owned pitched fields ([nx][pitch], y
+ * contiguous); the result is written to the device double *norm_squared,
+ * asynchronously on `stream` (a cudaStream_t, NULL for the default stream).
+ * fluid_cells must be positive and finite.
  * Its reduction scratch is a fixed __device__ array inside this library
  * (about 130 KB, held by every GPU that loads it until the process exits):
  * grids with more than STRM_NORM_NOALLOC_MAX_TILES interior tiles of 8 x 64
  * cells are rejected with STRM_ERR_INVALID.  The first call on a device looks
- * up that array's device address; make that first call before any stream
- * capture.  All calls share the one array: calls whose GPU work overlaps
- * (different streams or threads) race and must be serialised by the caller. */
+ * up that array's device address (cudaGetSymbolAddress) and keeps it for the
+ * life of the process; make that first call before any stream capture, and
+ * do not reset the device while the library is in use.  All calls share the
+ * one array and it keeps the last call's contents: calls whose GPU work
+ * overlaps (different streams or threads) race and must be serialised by
+ * the caller. */
 #define STRM_NORM_NOALLOC_MAX_TILES 16384
 int strm_norm_squared_noalloc(const double *p, const double *rhs, int nx, int ny, int pitch,
                               double dx, double dy, double fluid_cells, double *norm_squared,

@@ -26,6 +26,7 @@ SOR_RED_BLACK, SOR_LEXICOGRAPHIC = 0, 1
 ARITH_EXACT, ARITH_FAST = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 EXEC_GRAPH, EXEC_EAGER = 0, 1
+BATCH_GRAPH_LOOP, BATCH_PERSISTENT = 0, 1
 NORM_ALL_INTERIOR, NORM_FLUID, NORM_FLUID_MEAN_FREE = 0, 1, 2
 SWEEPS_DEFAULT, SWEEPS_PER_COLOUR, SWEEPS_COUNT = 0, 1, 8
 STOP_REFERENCE, STOP_STRICT, STOP_RELATIVE = 0, 1, 2
@@ -112,6 +113,7 @@ SIGNATURES = {
     "strm_batch_prepare": [_vp],
     "strm_batch_solve": [_vp, _vp],
     "strm_batch_set_schedule": [_vp, ctypes.c_int],
+    "strm_batch_set_solver": [_vp, ctypes.c_int, ctypes.c_uint64],
     "strm_batch_autotune": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
     "strm_apply_correction": [_vp, _vp, ctypes.c_double],
     "strm_copy_field_device": [_vp, ctypes.c_int, _vp, ctypes.c_int],

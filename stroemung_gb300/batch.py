@@ -1,7 +1,7 @@
 """Batches of independent simulations stepped by one CUDA graph
 (strm_batch_* in include/stroemung_gpu.h): the members' pressure solves run
-as one WHILE loop of table-driven kernels, each member ending exactly where
-stepping it alone ends.  No reference counterpart (the crate steps one
+as one WHILE loop of table-driven kernels or as one persistent cooperative
+kernel, each member ending exactly where stepping it alone ends.  No reference counterpart (the crate steps one
 simulation)."""
 from __future__ import annotations
 
@@ -58,6 +58,14 @@ class Batch:
 
     def set_schedule(self, schedule: int) -> None:
         _lib.check(_lib.load().strm_batch_set_schedule(self._h, int(schedule)))
+
+    def set_solver(self, persistent: bool, wait_limit: int = 0) -> None:
+        """persistent: the members' pressure solves run as one persistent
+        cooperative kernel per step (grid barriers between its phases, each
+        wait bounded by wait_limit polls, 0 = about a second or two) instead
+        of the graph's WHILE loop; results are identical."""
+        solver = _lib.BATCH_PERSISTENT if persistent else _lib.BATCH_GRAPH_LOOP
+        _lib.check(_lib.load().strm_batch_set_solver(self._h, solver, int(wait_limit)))
 
     def autotune(self, reps: int = 2):
         """Times whole batch steps under every blocked schedule (members'

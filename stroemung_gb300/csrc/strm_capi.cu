@@ -44,6 +44,9 @@ int fail(int code, const char *fmt, ...) {
   } while (0)
 
 constexpr int kLogCap = 4096;
+// Polls a grid-barrier wait of the persistent batch solve may take before it
+// gives up (each poll sleeps ~64 ns and reads L2: about a second or two).
+constexpr unsigned long long kDefaultWaitPolls = 1ull << 22;
 constexpr int kHistCap = 65536;  // residual history entries of one solve
 constexpr int kAbiVersion = 1;
 
@@ -849,6 +852,8 @@ struct strm_batch {
   std::vector<strm_sim *> sims;
   int schedule = 0;     // public sweep schedule number (2..)
   int inner = 16;
+  int solver = STRM_BATCH_GRAPH_LOOP;
+  unsigned long long wait_limit = kDefaultWaitPolls;
   BatchPlan plan{};
   cudaGraphExec_t exec = nullptr;
   cudaGraphExec_t exec_pre = nullptr, exec_solve = nullptr;
@@ -869,7 +874,8 @@ int batch_rebuild(strm_batch *b) {
   free_batch(&b->plan);
   std::vector<BatchMember> mem;
   for (strm_sim *s : b->sims) mem.push_back(BatchMember{s->d, s->cfg});
-  cudaError_t e = build_batch(mem, b->schedule - 1, b->inner, &b->plan);
+  cudaError_t e = build_batch(mem, b->schedule - 1, b->inner, &b->plan,
+                              b->solver == STRM_BATCH_PERSISTENT, b->wait_limit);
   if (e == cudaErrorInvalidValue)
     return fail(STRM_ERR_INVALID, "a batch member has max_iterations below the inner sweeps");
   CK(e);
@@ -882,8 +888,10 @@ int batch_rebuild(strm_batch *b) {
 // Copies each member's state and the last n log entries to the host and
 // fills stats[member * n + i].
 int batch_collect(strm_batch *b, int n, strm_step_stats *stats) {
-  unsigned int overrun = 0;
+  unsigned int overrun = 0, timeout = 0;
   CK(cudaMemcpyAsync(&overrun, (char *)b->plan.state + kBatchOverrunOffset, sizeof overrun,
+                     cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaMemcpyAsync(&timeout, (char *)b->plan.state + kBatchTimeoutOffset, sizeof timeout,
                      cudaMemcpyDeviceToHost, b->stream));
   const int ns = (int)b->sims.size();
   for (int k = 0; k < ns; ++k) {
@@ -902,6 +910,9 @@ int batch_collect(strm_batch *b, int n, strm_step_stats *stats) {
         o.delt = s->h_log[i].dt;
       }
   }
+  if (timeout)
+    return fail(STRM_ERR_TIMEOUT, "a grid barrier of the persistent batch solve gave up "
+                                  "waiting");
   if (overrun) return fail(STRM_ERR_TIMEOUT, "batch pressure loop passed its bound");
   for (strm_sim *s : b->sims)
     if (s->h_st->nonfinite) return fail(STRM_ERR_NONFINITE, "norm_squared is not finite");
@@ -916,7 +927,7 @@ int batch_begin(strm_batch *b) {
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpyAsync(&s->d.st->log_pos, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
   }
-  CK(cudaMemsetAsync((char *)b->plan.state + kBatchOverrunOffset, 0, sizeof(unsigned int),
+  CK(cudaMemsetAsync((char *)b->plan.state + kBatchOverrunOffset, 0, 2 * sizeof(unsigned int),
                      b->stream));
   return STRM_OK;
 }
@@ -973,6 +984,16 @@ int strm_batch_set_schedule(strm_batch *b, int schedule) {
   CK(cudaSetDevice(b->dev));
   CK(cudaStreamSynchronize(b->stream));
   b->schedule = schedule;
+  return batch_rebuild(b);
+}
+
+int strm_batch_set_solver(strm_batch *b, int solver, uint64_t wait_limit) {
+  if (!b || (solver != STRM_BATCH_GRAPH_LOOP && solver != STRM_BATCH_PERSISTENT))
+    return fail(STRM_ERR_INVALID, "invalid arguments");
+  CK(cudaSetDevice(b->dev));
+  CK(cudaStreamSynchronize(b->stream));
+  b->solver = solver;
+  b->wait_limit = wait_limit ? (unsigned long long)wait_limit : kDefaultWaitPolls;
   return batch_rebuild(b);
 }
 

@@ -27,6 +27,7 @@
 // rounded), so results are bit-identical to the reference's FP64 arithmetic.
 #include <cooperative_groups.h>
 #include <float.h>
+#include <stddef.h>
 
 #include <algorithm>
 #include <initializer_list>
@@ -45,6 +46,41 @@ constexpr int RT_X = 8;
 constexpr int RT_Y = 64;
 
 __device__ __forceinline__ double sqd(double x) { return x * x; }
+
+// Load of a buffer that other CTAs of the same launch may have written
+// earlier (the persistent batch solve): COH reads it at L2 (ld.global.cg),
+// never through the read-only path; otherwise a plain load.
+template <bool COH, typename T>
+__device__ __forceinline__ T ldv(const T *p) {
+  if constexpr (COH) return __ldcg(p);
+  else return *p;
+}
+
+// Thread coordinates of a work group of (32 x 8)-style tile kernels: the
+// whole CTA of a graph kernel (bar 0: __syncthreads), or one 256-thread half
+// of a 512-thread persistent CTA (its own named barrier 1 + half).
+struct Thr {
+  int tx, ty;      // within the group
+  int dx, dy;      // the group's extent (blockDim of a graph kernel)
+  int tid;         // tx + dx * ty
+  int half;        // 0 or 1
+  int bar;         // 0: __syncthreads; 1, 2: named barrier of 256 threads
+};
+__device__ __forceinline__ Thr thr_cta() {
+  Thr t;
+  t.tx = threadIdx.x;
+  t.ty = threadIdx.y;
+  t.dx = blockDim.x;
+  t.dy = blockDim.y;
+  t.tid = threadIdx.x + blockDim.x * threadIdx.y;
+  t.half = 0;
+  t.bar = 0;
+  return t;
+}
+__device__ __forceinline__ void gsync(const Thr &t) {
+  if (t.bar == 0) __syncthreads();
+  else asm volatile("bar.sync %0, 256;" ::"r"(t.bar) : "memory");
+}
 
 // ------------------------------------------------------------------------
 // reductions
@@ -549,6 +585,160 @@ static Consts32F consts32f_of(const Consts &c) {
   k.r_four_dy = (float)c.r_four_dy;
   k.r_re = (float)c.r_re;
   return k;
+}
+
+// F/G/RHS of the FAST arithmetic (fused multiply-adds, reciprocal
+// multiplies): the reference's terms (src/simulation.rs:122-214,
+// src/math.rs:19-174) regrouped as face fluxes, each computed once per face
+// instead of once per neighbouring cell.  With k1 = dt/(Re dx^2),
+// k2 = dt/(Re dy^2), k3 = dt/(4 dx), k4 = dt/(4 dy):
+//
+//   PX(x,y) = k1 DX + k3 (SX^2 + gamma |SX| DX),  SX = u(x)+u(x+1), DX = u(x)-u(x+1)
+//   PY(x,y) = k2 C + k4 (A B + gamma |A| C),       A = v(x,y)+v(x+1,y),
+//                                                  B = u(x,y)+u(x,y+1), C = u(x,y)-u(x,y+1)
+//   QX(x,y) = k1 C' + k3 (A B + gamma |B| C'),     C' = v(x,y)-v(x+1,y)
+//   QY(x,y) = k2 DY + k3' (SY^2 + gamma |SY| DY),  SY = v(y)+v(y+1), DY = v(y)-v(y+1)
+//   F = u + (PX(x-1,y) - PX(x,y)) + (PY(x,y-1) - PY(x,y))
+//   G = v + (QX(x-1,y) - QX(x,y)) + (QY(x,y-1) - QY(x,y))
+//   RHS = (F(x,y) - F(x-1,y)) / (dx dt) + (G(x,y) - G(x,y-1)) / (dy dt)
+//
+// In real arithmetic this is the reference's F (u + dt (lap/Re - du2dx -
+// duvdy)), G and RHS term for term; only the rounding differs.  About 37
+// FP64 operations per cell instead of ~140: the FP64 pipe, about 1.75
+// operations per clock per SM on this part, bounds the kernel.  Boundary
+// copies (F = u, G = v), the cells left unchanged and the RHS region are
+// those of fg_rhs_kernel.  Tiles of 32 x 32 cells; the fluxes of a tile and
+// its one-face halo live in dynamic shared memory.
+constexpr int FF_T = 32;
+constexpr int FF_THREADS = 256;
+struct FastFgSmem {
+  double u[FF_T + 3][FF_T + 3];  // rows x0-2 .. x0+32, cols y0-2 .. y0+32
+  double v[FF_T + 3][FF_T + 3];
+  double px[FF_T + 2][FF_T];     // rows x0-2 .. x0+31, cols y0 .. y0+31
+  double py[FF_T + 1][FF_T + 1]; // rows x0-1 .. x0+31, cols y0-1 .. y0+31
+  double qx[FF_T + 1][FF_T + 1]; // rows x0-1 .. x0+31, cols y0-1 .. y0+31
+  double qy[FF_T][FF_T + 2];     // rows x0 .. x0+31,   cols y0-2 .. y0+31
+  double f[FF_T + 1][FF_T];      // rows x0-1 .. x0+31, cols y0 .. y0+31
+  double g[FF_T][FF_T + 1];      // rows x0 .. x0+31,   cols y0-1 .. y0+31
+  uint8_t fl[FF_T + 2][FF_T + 2];  // rows x0-1 .. x0+32, cols y0-1 .. y0+32
+  double k[8];                   // k1 k2 k3 k4 k3*gamma k4*gamma c1 c2
+};
+
+__global__ void __launch_bounds__(FF_THREADS, 3)
+    fg_rhs_fast_kernel(const double *__restrict__ u, const double *__restrict__ v, double *f,
+                       double *gg, double *__restrict__ rhs, const uint8_t *__restrict__ flags,
+                       Geom g, Consts c, const StepState *st) {
+  extern __shared__ __align__(16) unsigned char ff_raw[];
+  FastFgSmem &S = *reinterpret_cast<FastFgSmem *>(ff_raw);
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * FF_T;
+  const int x0 = blockIdx.y * FF_T;
+  if (tid == 0) {
+    const double dt = st->dt;
+    const double rdt = 1.0 / dt;
+    S.k[0] = dt * (c.r_re * c.r_dx2);
+    S.k[1] = dt * (c.r_re * c.r_dy2);
+    S.k[2] = dt * c.r_four_dx;
+    S.k[3] = dt * c.r_four_dy;
+    S.k[4] = S.k[2] * c.gamma;
+    S.k[5] = S.k[3] * c.gamma;
+    S.k[6] = c.r_dx * rdt;
+    S.k[7] = c.r_dy * rdt;
+  }
+  constexpr int W = FF_T + 3;
+  for (int q = tid; q < W * W; q += FF_THREADS) {
+    const int i = q / W, j = q % W;
+    const int x = x0 - 2 + i, y = y0 - 2 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    S.u[i][j] = in ? u[OFF(x, y)] : 0.0;
+    S.v[i][j] = in ? v[OFF(x, y)] : 0.0;
+  }
+  constexpr int WF = FF_T + 2;
+  for (int q = tid; q < WF * WF; q += FF_THREADS) {
+    const int i = q / WF, j = q % WF;
+    const int x = x0 - 1 + i, y = y0 - 1 + j;
+    const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
+    S.fl[i][j] = in ? flags[OFF(x, y)] : (uint8_t)0;
+  }
+  __syncthreads();
+  const double k1 = S.k[0], k2 = S.k[1], k3 = S.k[2], k4 = S.k[3];
+  const double k3g = S.k[4], k4g = S.k[5];
+
+  // x faces of u: PX at rows x0-2 .. x0+31 (u row index i = row - x0 + 2)
+  for (int q = tid; q < (FF_T + 2) * FF_T; q += FF_THREADS) {
+    const int i = q / FF_T, j = q % FF_T;
+    const double a = S.u[i][j + 2], b = S.u[i + 1][j + 2];
+    const double sx = a + b, dx_ = a - b;
+    S.px[i][j] = fma(dx_, fma(k3g, fabs(sx), k1), (k3 * sx) * sx);
+  }
+  // y faces of u and x faces of v (they share A B): rows x0-1 .. x0+31,
+  // cols y0-1 .. y0+31
+  for (int q = tid; q < (FF_T + 1) * (FF_T + 1); q += FF_THREADS) {
+    const int i = q / (FF_T + 1), j = q % (FF_T + 1);
+    const double u0 = S.u[i + 1][j + 1], uS = S.u[i + 1][j + 2];
+    const double v0 = S.v[i + 1][j + 1], vE = S.v[i + 2][j + 1];
+    const double A = v0 + vE, B = u0 + uS, C = u0 - uS, Cp = v0 - vE;
+    const double AB = A * B;
+    S.py[i][j] = fma(C, fma(k4g, fabs(A), k2), k4 * AB);
+    S.qx[i][j] = fma(Cp, fma(k3g, fabs(B), k1), k3 * AB);
+  }
+  // y faces of v: rows x0 .. x0+31, cols y0-2 .. y0+31
+  for (int q = tid; q < FF_T * (FF_T + 2); q += FF_THREADS) {
+    const int i = q / (FF_T + 2), j = q % (FF_T + 2);
+    const double a = S.v[i + 2][j], b = S.v[i + 2][j + 1];
+    const double sy = a + b, dy_ = a - b;
+    S.qy[i][j] = fma(dy_, fma(k4g, fabs(sy), k2), (k4 * sy) * sy);
+  }
+  __syncthreads();
+
+  // F at rows x0-1 .. x0+31, cols y0 .. y0+31
+  for (int q = tid; q < (FF_T + 1) * FF_T; q += FF_THREADS) {
+    const int i = q / FF_T, j = q % FF_T;
+    const int x = x0 - 1 + i, y = y0 + j;
+    double Fv = 0.0;
+    if (x >= 0 && x < g.nx && y < g.ny) {
+      const bool keep = is_bnd(S.fl[i][j + 1]) || (x + 1 < g.nx && is_bnd(S.fl[i + 1][j + 1]));
+      const bool interior = x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+      const double u0 = S.u[i + 1][j + 2];
+      if (keep) {
+        Fv = u0;
+      } else if (interior) {
+        Fv = u0 + ((S.px[i][j] - S.px[i + 1][j]) + (S.py[i][j] - S.py[i][j + 1]));
+      } else {
+        Fv = f[OFF(x, y)];
+      }
+      if (i >= 1 && (keep || interior)) f[OFF(x, y)] = Fv;
+    }
+    S.f[i][j] = Fv;
+  }
+  // G at rows x0 .. x0+31, cols y0-1 .. y0+31
+  for (int q = tid; q < FF_T * (FF_T + 1); q += FF_THREADS) {
+    const int i = q / (FF_T + 1), j = q % (FF_T + 1);
+    const int x = x0 + i, y = y0 - 1 + j;
+    double Gv = 0.0;
+    if (x < g.nx && y >= 0 && y < g.ny) {
+      const bool keep = is_bnd(S.fl[i + 1][j]) || (y + 1 < g.ny && is_bnd(S.fl[i + 1][j + 1]));
+      const bool interior = x >= 1 && y >= 1 && x <= g.nx - 2 && y <= g.ny - 2;
+      const double v0 = S.v[i + 2][j + 1];
+      if (keep) {
+        Gv = v0;
+      } else if (interior) {
+        Gv = v0 + ((S.qx[i][j] - S.qx[i + 1][j]) + (S.qy[i][j] - S.qy[i][j + 1]));
+      } else {
+        Gv = gg[OFF(x, y)];
+      }
+      if (j >= 1 && (keep || interior)) gg[OFF(x, y)] = Gv;
+    }
+    S.g[i][j] = Gv;
+  }
+  __syncthreads();
+  const double c1 = S.k[6], c2 = S.k[7];
+  for (int q = tid; q < FF_T * FF_T; q += FF_THREADS) {
+    const int i = q / FF_T, j = q % FF_T;
+    const int x = x0 + i, y = y0 + j;
+    if (x >= 1 && y >= 1 && x < g.nx && y < g.ny)
+      rhs[OFF(x, y)] = fma(S.g[i][j + 1] - S.g[i][j], c2, (S.f[i + 1][j] - S.f[i][j]) * c1);
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -1302,6 +1492,14 @@ __global__ void __launch_bounds__(256)
 // values the boundary pass recorded (their final value in the reference's
 // u_v_restore replay); the rest keep their value.  Then max|u|, max|v| over
 // every cell, the fluid speed range and, for a step, time += delt.
+//
+// FAST (fused multiply-adds) forms u = fma(-dt/dx, dp, F) and
+// u^2 + v^2 = fma(u, u, v^2); the exact form keeps the reference's order.
+// The maxima and minima are taken on the bit patterns (non-negative doubles
+// order like their bits), skipping NaNs as fmax / fmin do, so they are
+// exact and cost no FP64-pipe operation: 6 (FAST) or 9 FP64 operations per
+// cell instead of 13.
+template <bool FASTA>
 __global__ void __launch_bounds__(256)
     velocity_kernel(double *u, double *v, const double *__restrict__ f,
                     const double *__restrict__ gg, const double *__restrict__ p,
@@ -1309,6 +1507,7 @@ __global__ void __launch_bounds__(256)
                     const uint8_t *__restrict__ flags, Geom g, Consts c, StepState *st,
                     double *partials, StepLog *log, int tiles_y, int ntiles, int update,
                     int commit_speed, int advance) {
+  constexpr uint64_t kAbs = 0x7FFFFFFFFFFFFFFFull, kInf = 0x7FF0000000000000ull;
   __shared__ double s_cu, s_cv;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     s_cu = st->dt / c.dx;
@@ -1316,7 +1515,7 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const double cu = s_cu, cv = s_cv;
-  double umax = 1.0e-10, vmax = 1.0e-10, smin = DBL_MAX, smax = 0.0;
+  uint64_t umax = f64_bits(1.0e-10), vmax = umax, smin = f64_bits(DBL_MAX), smax = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int x = (t / tiles_y) * RT_X + threadIdx.y;
     if (x >= g.nx) continue;
@@ -1335,28 +1534,36 @@ __global__ void __launch_bounds__(256)
           v[o] = vn;
         } else if (update && !is_bnd(fl) && x < g.nx - 1 && y < g.ny - 1) {
           const double pc = p[o];
-          un = f[o] - cu * (p[o + g.pitch] - pc);
-          vn = gg[o] - cv * (p[o + 1] - pc);
+          if (FASTA) {
+            un = fma(-cu, p[o + g.pitch] - pc, f[o]);
+            vn = fma(-cv, p[o + 1] - pc, gg[o]);
+          } else {
+            un = f[o] - cu * (p[o + g.pitch] - pc);
+            vn = gg[o] - cv * (p[o + 1] - pc);
+          }
           u[o] = un;
           v[o] = vn;
         } else {
           un = u[o];
           vn = v[o];
         }
-        umax = fmax(umax, fabs(un));
-        vmax = fmax(vmax, fabs(vn));
+        const uint64_t au = f64_bits(un) & kAbs, av = f64_bits(vn) & kAbs;
+        if (au <= kInf) umax = au > umax ? au : umax;
+        if (av <= kInf) vmax = av > vmax ? av : vmax;
         if (!is_bnd(fl)) {
-          const double s2 = sqd(un) + sqd(vn);
-          smin = fmin(smin, s2);
-          smax = fmax(smax, s2);
+          const uint64_t s2 = f64_bits(FASTA ? fma(un, un, vn * vn) : sqd(un) + sqd(vn));
+          if (s2 <= kInf) {
+            smin = s2 < smin ? s2 : smin;
+            smax = s2 > smax ? s2 : smax;
+          }
         }
       }
     }
   }
-  const double b0 = block_reduce(umax, OpMax(), 1.0e-10);
-  const double b1 = block_reduce(vmax, OpMax(), 1.0e-10);
-  const double b2 = block_reduce(smin, OpMin(), DBL_MAX);
-  const double b3 = block_reduce(smax, OpMax(), 0.0);
+  const double b0 = block_reduce(f64_of(umax), OpMax(), 1.0e-10);
+  const double b1 = block_reduce(f64_of(vmax), OpMax(), 1.0e-10);
+  const double b2 = block_reduce(f64_of(smin), OpMin(), DBL_MAX);
+  const double b3 = block_reduce(f64_of(smax), OpMax(), 0.0);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     double *pp = partials + 4 * (size_t)blockIdx.x;
     pp[0] = b0;
@@ -1435,23 +1642,25 @@ __device__ __forceinline__ float copy32(const float *e, size_t o, int pitch, int
 // One colour over the whole grid: fluid interior cells of the colour get the
 // SOR update, boundary cells of the colour with an edge get the copy (when
 // copy_boundary is set).
+template <bool COH = false>
 __device__ __forceinline__ void sor32_color_cells(float *__restrict__ e,
                                                   const float *__restrict__ s,
                                                   const uint8_t *__restrict__ flags,
                                                   const Geom &g, const Consts32 &k, int color,
-                                                  int copy_boundary, int bx, int by) {
-  const int x = by * blockDim.y + threadIdx.y;
-  const int y = 2 * (bx * blockDim.x + threadIdx.x) + ((x + color) & 1);
+                                                  int copy_boundary, int bx, int by,
+                                                  const Thr t = thr_cta()) {
+  const int x = by * t.dy + t.ty;
+  const int y = 2 * (bx * t.dx + t.tx) + ((x + color) & 1);
   if (x >= g.nx || y >= g.ny) return;
   const size_t o = OFF(x, y);
   const uint8_t fl = flags[o];
   if (fl == 0) {
     if (x < 1 || y < 1 || x > g.nx - 2 || y > g.ny - 2) return;
-    const float sum_x = e[o - g.pitch] + e[o + g.pitch];
-    const float sum_y = e[o - 1] + e[o + 1];
-    e[o] = fmaf(k.omw, e[o], fmaf(k.a, sum_x, fmaf(k.b, sum_y, s[o])));
+    const float sum_x = ldv<COH>(e + o - g.pitch) + ldv<COH>(e + o + g.pitch);
+    const float sum_y = ldv<COH>(e + o - 1) + ldv<COH>(e + o + 1);
+    e[o] = fmaf(k.omw, ldv<COH>(e + o), fmaf(k.a, sum_x, fmaf(k.b, sum_y, ldv<COH>(s + o))));
   } else if (copy_boundary && edge_of(fl) != E_NONE) {
-    e[o] = s[o] + copy32(e, o, g.pitch, edge_of(fl));
+    e[o] = ldv<COH>(s + o) + copy32(e, o, g.pitch, edge_of(fl));
   }
 }
 
@@ -1555,7 +1764,7 @@ __device__ __forceinline__ void tb_strip(float *ec, const float *eo, const float
 // One tile.  Extended rows are EY = 128 cells wide, so each colour row is 64
 // words and every lane owns two neighbouring compacted cells (j, j+1): the
 // four cells y = 4*lane .. 4*lane+3 of a row land as one pair per colour.
-template <int H, int TX, int TY>
+template <int H, int TX, int TY, int WARPS = 16, bool COH = false>
 __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
                                               float *__restrict__ eout,
                                               const float *__restrict__ s,
@@ -1567,13 +1776,14 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
   static_assert(H % 4 == 0 && TX % 2 == 0 && TY % 4 == 0, "tile origins must be multiples of 4");
   static_assert(TY + 2 * H == 128, "extended rows are 128 cells");
   constexpr int EX = TX + 2 * H, EY = 128, W = EY / 2, NC = EX * W;
-  constexpr int WARPS = 16;
   float *se = reinterpret_cast<float *>(smem_raw);         // [2][EX][W]
   float *ss = se + 2 * NC;                                   // [2][EX][W]
   uint8_t *sc = reinterpret_cast<uint8_t *>(ss + 2 * NC);  // [2][EX][W]: 0 SOR, 1..8 copy, kFrozen
   const int gx0 = (tile / tiles_y) * TX - H;
   const int gy0 = (tile % tiles_y) * TY - H;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // WARPS warps of 32 threads, in a 1-D block or a (32, WARPS) block
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   const int j0 = 2 * lane;  // this lane's compacted pair in every row
   // load: lane takes cells y0 .. y0+3 of each row (16-byte aligned: the tile
   // origin and the pitch are multiples of 4 cells)
@@ -1587,8 +1797,8 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
     if (x >= 0 && x < g.nx) {
       if (y0 >= 0 && y0 + 3 < g.ny) {
         const size_t o = OFF(x, y0);
-        const float4 e4 = *reinterpret_cast<const float4 *>(ein + o);
-        const float4 s4 = *reinterpret_cast<const float4 *>(s + o);
+        const float4 e4 = ldv<COH>(reinterpret_cast<const float4 *>(ein + o));
+        const float4 s4 = ldv<COH>(reinterpret_cast<const float4 *>(s + o));
         const uchar4 f4 = *reinterpret_cast<const uchar4 *>(flags + o);
         ev[0] = e4.x; ev[1] = e4.y; ev[2] = e4.z; ev[3] = e4.w;
         sv[0] = s4.x; sv[1] = s4.y; sv[2] = s4.z; sv[3] = s4.w;
@@ -1602,8 +1812,8 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
           const int y = y0 + q;
           if (y >= 0 && y < g.ny) {
             const size_t o = OFF(x, y);
-            ev[q] = ein[o];
-            sv[q] = s[o];
+            ev[q] = ldv<COH>(ein + o);
+            sv[q] = ldv<COH>(s + o);
             cv[q] = tb_code(flags[o], x, y, g);
           }
         }
@@ -1675,7 +1885,7 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
         // four consecutive cells: 32-byte aligned (y0 and the pitch are
         // multiples of 4), two 16-byte accesses per FP64 field
         double2 *p2 = reinterpret_cast<double2 *>(pf + o);
-        const double2 lo = p2[0], hi = p2[1];
+        const double2 lo = ldv<COH>(p2), hi = ldv<COH>(p2 + 1);
         if (pw) {
           double2 *w2 = reinterpret_cast<double2 *>(pw + o);
           w2[0] = lo;
@@ -1692,7 +1902,7 @@ __device__ __forceinline__ void sor32_tb_tile(const float *__restrict__ ein,
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           if (y0 + q >= g.ny) break;
-          const double p0 = pf[o + q];
+          const double p0 = ldv<COH>(pf + o + q);
           if (pw) pw[o + q] = p0;
           if (cv[q] != kFrozen) pf[o + q] = p0 + widen(ev[q]);
           eout[o + q] = 0.0f;
@@ -1738,9 +1948,10 @@ __global__ void __launch_bounds__(512)
 __device__ __forceinline__ void refine_cells(double *__restrict__ p, const float *e, float *ez,
                                              const uint8_t *__restrict__ flags, const Geom &g,
                                              int apply, int bx, int by,
-                                             double *__restrict__ save) {
-  const int x = by * blockDim.y + threadIdx.y;
-  const int y0 = 2 * (bx * blockDim.x + threadIdx.x);
+                                             double *__restrict__ save,
+                                             const Thr t = thr_cta()) {
+  const int x = by * t.dy + t.ty;
+  const int y0 = 2 * (bx * t.dx + t.tx);
   if (x >= g.nx) return;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
@@ -1764,46 +1975,51 @@ __global__ void __launch_bounds__(256)
 
 // delta_b = copy(p) - p_b on boundary cells with an edge (FP64, stored FP32
 // in s and as the starting correction e_b).
+template <bool COH = false>
 __device__ __forceinline__ void delta_entry(const double *__restrict__ p, float *__restrict__ s,
                                             float *__restrict__ e, const PCopy &pc, int pitch) {
   const long long o = pc.off;
+  const double pN = ldv<COH>(p + o - 1), pS = ldv<COH>(p + o + 1);
+  const double pW = ldv<COH>(p + o - pitch), pE = ldv<COH>(p + o + pitch);
   double c;
   switch (pc.edge) {
-    case E_N: c = p[o - 1]; break;
-    case E_NE: c = (p[o - 1] + p[o + pitch]) * 0.5; break;
-    case E_E: c = p[o + pitch]; break;
-    case E_SE: c = (p[o + 1] + p[o + pitch]) * 0.5; break;
-    case E_S: c = p[o + 1]; break;
-    case E_SW: c = (p[o + 1] + p[o - pitch]) * 0.5; break;
-    case E_W: c = p[o - pitch]; break;
-    default: c = (p[o - 1] + p[o - pitch]) * 0.5; break;
+    case E_N: c = pN; break;
+    case E_NE: c = (pN + pE) * 0.5; break;
+    case E_E: c = pE; break;
+    case E_SE: c = (pS + pE) * 0.5; break;
+    case E_S: c = pS; break;
+    case E_SW: c = (pS + pW) * 0.5; break;
+    case E_W: c = pW; break;
+    default: c = (pN + pW) * 0.5; break;
   }
-  const float d = (float)(c - p[o]);
+  const float d = (float)(c - ldv<COH>(p + o));
   s[o] = d;
   e[o] = d;
 }
 
 
-template <bool FLUID, bool MEAN_FREE>
+template <bool FLUID, bool MEAN_FREE, bool COH = false>
 __device__ __forceinline__ void mixed_residual_sum(
     const double *__restrict__ p, const double *__restrict__ rhs,
     const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
-    int tiles_y, int ntiles, int bid, int nblocks, double *acc_out, double *acc1_out) {
+    int tiles_y, int ntiles, int bid, int nblocks, double *acc_out, double *acc1_out,
+    const Thr th = thr_cta()) {
   double acc = 0.0, acc1 = 0.0;
   // the defect is rounded to FP32 before the scaling (integer conversion,
   // FP32 multiply): no FP64 operation beyond the residual and its sums
   const float mid32 = narrow(c.middle);
   for (int t = bid; t < ntiles; t += nblocks) {
-    const int x = 1 + (t / tiles_y) * RT_X + threadIdx.y;
+    const int x = 1 + (t / tiles_y) * RT_X + th.ty;
     if (x > g.nx - 2) continue;
-    const int yb = 1 + (t % tiles_y) * RT_Y + 2 * threadIdx.x;
+    const int yb = 1 + (t % tiles_y) * RT_Y + 2 * th.tx;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int y = yb + q;
       if (y <= g.ny - 2) {
         const size_t o = OFF(x, y);
-        const double r = residual_of<false>(p[o], p[o - g.pitch], p[o + g.pitch], p[o - 1],
-                                            p[o + 1], rhs[o], c);
+        const double r = residual_of<false>(ldv<COH>(p + o), ldv<COH>(p + o - g.pitch),
+                                            ldv<COH>(p + o + g.pitch), ldv<COH>(p + o - 1),
+                                            ldv<COH>(p + o + 1), rhs[o], c);
         const bool fluid = flags[o] == 0;
         if (fluid || !FLUID) {
           acc = fma(r, r, acc);
@@ -1817,35 +2033,93 @@ __device__ __forceinline__ void mixed_residual_sum(
   *acc1_out = acc1;
 }
 
+// Group versions of the block sums for 256-thread groups (a graph kernel's
+// CTA or half of a persistent CTA), with the same summation trees as
+// block_sum_pass / block_reduce / reduce_partials on 256 threads, so the
+// results are bit-identical.  Their scratch is passed in (the persistent
+// kernel lends the dynamic shared memory its sweep tiles use between
+// phases): 2 x 512 + 2 x 32 doubles.
+template <bool TWO>
+__device__ __forceinline__ void block_sum_pass_g(double &a, double &b, const Thr &t,
+                                                 double *scratch) {
+  double *sa = scratch + t.half * 512, *sb = sa + 256;
+  sa[t.tid] = a;
+  if (TWO) sb[t.tid] = b;
+  gsync(t);
+  if (t.tid < 32) {
+    double s0 = sa[t.tid], s1 = TWO ? sb[t.tid] : 0.0;
+    for (int k = t.tid + 32; k < 256; k += 32) {
+      s0 += sa[k];
+      if (TWO) s1 += sb[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      if (TWO) s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    a = s0;
+    b = s1;
+  }
+}
+
+template <typename Op>
+__device__ double block_reduce_g(double v, Op op, double identity, const Thr &t,
+                                 double *scratch) {
+  double *sm = scratch + 1024 + t.half * 32;
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = t.tid & 31, w = t.tid >> 5;
+  gsync(t);
+  if (lane == 0) sm[w] = v;
+  gsync(t);
+  if (w == 0) {
+    v = lane < 8 ? sm[lane] : identity;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;  // valid in thread 0 of the group
+}
+
+template <typename Op>
+__device__ double reduce_partials_g(const double *part, int n, int stride, int idx, Op op,
+                                    double identity, const Thr &t, double *scratch) {
+  double v = identity;
+  for (int k = t.tid; k < n; k += 256) v = op(v, __ldcg(part + (size_t)k * stride + idx));
+  return block_reduce_g(v, op, identity, t, scratch);
+}
+
 // FP64 norm of the residual on every interior cell (the reference's norm),
 // the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
 // and the stop rule every m sweeps.  Block `bid` of `nblocks` sums its tiles
 // into partials[bid] (interleaved with the residual sum when mean-free).
+// GRP, th, scratch: a 256-thread group and its reduction scratch (the
+// persistent batch solve); by default the CTA and block_sum_pass.
+template <bool COH = false, bool GRP = false>
 __device__ __forceinline__ void mixed_residual_partial(
     const double *__restrict__ p, const double *__restrict__ rhs,
     const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
-    double *partials, int tiles_y, int ntiles, int strict, int bid, int nblocks) {
+    double *partials, int tiles_y, int ntiles, int strict, int bid, int nblocks,
+    const Thr th = thr_cta(), double *scratch = nullptr) {
   const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
   const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
   double acc = 0.0, acc1 = 0.0;
   if (!fluid_only)
-    mixed_residual_sum<false, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
-                                     &acc1);
+    mixed_residual_sum<false, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
+                                          &acc, &acc1, th);
   else if (!mean_free)
-    mixed_residual_sum<true, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
-                                    &acc1);
+    mixed_residual_sum<true, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
+                                         &acc, &acc1, th);
   else
-    mixed_residual_sum<true, true>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks, &acc,
-                                   &acc1);
+    mixed_residual_sum<true, true, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
+                                        &acc, &acc1, th);
   if (mean_free) {
-    block_sum_pass<true>(acc, acc1);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if constexpr (GRP) block_sum_pass_g<true>(acc, acc1, th, scratch);
+    else block_sum_pass<true>(acc, acc1);
+    if (th.tid == 0) {
       partials[2 * bid] = acc;
       partials[2 * bid + 1] = acc1;
     }
   } else {
-    block_sum_pass<false>(acc, acc1);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partials[bid] = acc;
+    if constexpr (GRP) block_sum_pass_g<false>(acc, acc1, th, scratch);
+    else block_sum_pass<false>(acc, acc1);
+    if (th.tid == 0) partials[bid] = acc;
   }
 }
 
@@ -1863,6 +2137,40 @@ __device__ __forceinline__ int mixed_residual_stop(const double *partials, int n
   const double ns = finish_norm(partials, nblocks, mean_free, st->fluid_cells);
   int status = SOLVE_GO_ON;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
+    st->ns = ns;
+    hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
+    if (!check) st->ns_start = ns;
+    if (check) {
+      const unsigned int it = st->sor_iters + sweeps;
+      st->sor_iters = it;
+      st->nonfinite = !isfinite(ns);
+      const bool done = stop_rule(ns, c, st, strict);
+      const bool room = it + sweeps <= itermax;
+      if (done) st->converged = 1;
+      else if (!room) st->exhausted = 1;
+      status = done ? SOLVE_DONE : (room ? SOLVE_GO_ON : SOLVE_NO_ROOM);
+    }
+  }
+  return status;
+}
+
+// mixed_residual_stop for a 256-thread group with its reduction scratch.
+__device__ __forceinline__ int mixed_residual_stop_g(const double *partials, int nblocks,
+                                                     StepState *st, const Consts &c,
+                                                     unsigned int itermax, int strict,
+                                                     int sweeps, int check, const Thr &t,
+                                                     double *scratch) {
+  const bool mean_free = (strict & STOP_FLUID_NORM) && (strict & STOP_MEAN_FREE);
+  double ns;
+  if (!mean_free) {
+    ns = reduce_partials_g(partials, nblocks, 1, 0, OpAdd(), 0.0, t, scratch) / st->fluid_cells;
+  } else {
+    const double s2 = reduce_partials_g(partials, nblocks, 2, 0, OpAdd(), 0.0, t, scratch);
+    const double s1 = reduce_partials_g(partials, nblocks, 2, 1, OpAdd(), 0.0, t, scratch);
+    ns = (s2 - s1 * (s1 / st->fluid_cells)) / st->fluid_cells;
+  }
+  int status = SOLVE_GO_ON;
+  if (t.tid == 0) {
     st->ns = ns;
     hist_push(st, check ? st->sor_iters + sweeps : 0u, ns);
     if (!check) st->ns_start = ns;
@@ -2290,13 +2598,37 @@ cudaError_t launch_bc(const DevFields &d, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Opts fg_rhs_fast_kernel into its dynamic shared memory (once per device).
+static cudaError_t ff_prepare() {
+  static bool done_on[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  bool &done = done_on[dev & 63];
+  if (done) return cudaSuccess;
+  e = cudaFuncSetAttribute(fg_rhs_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(FastFgSmem));
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+static dim3 ff_grid(const Geom &g) {
+  return dim3((g.ny + FF_T - 1) / FF_T, (g.nx + FF_T - 1) / FF_T);
+}
+
 cudaError_t launch_fg_rhs(const DevFields &d, const RunCfg &r, cudaStream_t s) {
   dim3 grd((r.g.ny + FG_TY - 1) / FG_TY, (r.g.nx + FG_TX - 1) / FG_TX);
-  if (r.precision == 1)
+  if (r.precision == 1) {
     fg_rhs32_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c,
                                                consts32f_of(r.c), d.st);
-  else
+  } else if (r.arith) {
+    cudaError_t e = ff_prepare();
+    if (e != cudaSuccess) return e;
+    fg_rhs_fast_kernel<<<ff_grid(r.g), FF_THREADS, sizeof(FastFgSmem), s>>>(
+        d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c, d.st);
+  } else {
     fg_rhs_kernel<<<grd, FG_THREADS, 0, s>>>(d.u, d.v, d.f, d.g, d.rhs, d.flags, r.g, r.c, d.st);
+  }
   return cudaGetLastError();
 }
 
@@ -2342,9 +2674,9 @@ cudaError_t launch_velocity(const DevFields &d, const RunCfg &r, cudaStream_t s,
   int ty, nt;
   tiles_of(r.g, 0, &ty, &nt);
   int nb = residual_blocks(r.g);
-  velocity_kernel<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, r.g,
-                                           r.c, d.st, d.partials, d.log, ty, nt, update,
-                                           commit_speed, advance);
+  auto k = r.arith ? velocity_kernel<true> : velocity_kernel<false>;
+  k<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, r.g, r.c, d.st,
+                             d.partials, d.log, ty, nt, update, commit_speed, advance);
   return cudaGetLastError();
 }
 
@@ -2582,8 +2914,9 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     }
   }
   prange_kernel<<<nb, kRedBlock, 0, s>>>(d.p, d.flags, g, d.st, d.partials, ty_all, nt_all, 0);
-  velocity_kernel<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, g, c,
-                                           d.st, d.partials, d.log, ty_all, nt_all, 1, 1, 1);
+  auto vk = r.arith ? velocity_kernel<true> : velocity_kernel<false>;
+  vk<<<nb, kRedBlock, 0, s>>>(d.u, d.v, d.f, d.g, d.p, d.ru, d.rv, d.flags, g, c, d.st,
+                              d.partials, d.log, ty_all, nt_all, 1, 1, 1);
   return cudaGetLastError();
 }
 
@@ -2665,14 +2998,21 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                  d.u, d.v, d.ru, d.rv, (const BcEntry *)d.bc, d.bc_val, d.n_bc, d.st, c, r.tau,
                  r.delt, r.itermax, 1);
     dim3 fg_grid((g.ny + FG_TY - 1) / FG_TY, (g.nx + FG_TX - 1) / FG_TX);
-    if (r.precision == 1)
+    if (r.precision == 1) {
       n = b.kernel(b.graph, n, (const void *)fg_rhs32_kernel, fg_grid, dim3(FG_THREADS),
                    (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
                    (const uint8_t *)d.flags, g, c, consts32f_of(c), (const StepState *)d.st);
-    else
+    } else if (r.arith) {
+      if (b.err == cudaSuccess) b.err = ff_prepare();
+      n = b.kernel_smem(b.graph, n, (const void *)fg_rhs_fast_kernel, ff_grid(g),
+                        dim3(FF_THREADS), sizeof(FastFgSmem), (const double *)d.u,
+                        (const double *)d.v, d.f, d.g, d.rhs, (const uint8_t *)d.flags, g, c,
+                        (const StepState *)d.st);
+    } else {
       n = b.kernel(b.graph, n, (const void *)fg_rhs_kernel, fg_grid, dim3(FG_THREADS),
                    (const double *)d.u, (const double *)d.v, d.f, d.g, d.rhs,
                    (const uint8_t *)d.flags, g, c, (const StepState *)d.st);
+    }
   }
   if (part == 1 || part == 3) {
     // the first half of a step ends after the RHS; part 3 is the second
@@ -2862,7 +3202,9 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock,
                  (const double *)d.p, (const uint8_t *)d.flags, g, d.st, d.partials, ty_all,
                  nt_all, 0);
-    n = b.kernel(b.graph, n, (const void *)velocity_kernel, dim3(nb), kRedBlock, d.u, d.v,
+    n = b.kernel(b.graph, n,
+                 r.arith ? (const void *)velocity_kernel<true> : (const void *)velocity_kernel<false>,
+                 dim3(nb), kRedBlock, d.u, d.v,
                  (const double *)d.f, (const double *)d.g, (const double *)d.p,
                  (const double *)d.ru, (const double *)d.rv, (const uint8_t *)d.flags, g, c,
                  d.st, d.partials, d.log, ty_all, nt_all, 1, 1, 1);
@@ -2911,9 +3253,19 @@ struct BatchState {
   unsigned int counter;
   unsigned int active;
   unsigned int body_count;
-  unsigned int overrun;
   unsigned int launches;  // independent count of loop bodies (block 0)
   unsigned int replays;   // members that finish sweep by sweep
+  // persistent solve: grid barrier, the loop decision of each body (by
+  // parity) and of the finishing pass
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  unsigned int go[2];
+  unsigned int open_replay;
+  // the fields above are zeroed before every persistent solve (a solve cut
+  // short by a barrier timeout can leave them anywhere); these two collect
+  // over the steps of one call and are reset by the host before it
+  unsigned int overrun;   // a loop passed its bound
+  unsigned int timeout;   // a CTA of the persistent solve gave up waiting
 };
 
 __device__ __forceinline__ bool inst_stopped(const StepState *st) {
@@ -2927,44 +3279,44 @@ __device__ __forceinline__ bool in_phase(const BInst &b, int fine) {
   return b.solve && (!fine || b.st->replay != 0u);
 }
 
-__global__ void __launch_bounds__(256)
-    batch_refine_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int apply,
-                        int final_b, int fine, int save) {
-  const int2 e = tab[blockIdx.x];
+// The batch kernels' work for one (instance, block) table entry, shared by
+// the graph's kernels (one entry per CTA) and the persistent solve (each CTA
+// walks the table).
+__device__ __forceinline__ void batch_refine_body(const BInst *__restrict__ I, int2 e, int apply,
+                                                  int final_b, int fine, int save,
+                                                  const Thr t = thr_cta()) {
   const BInst &b = I[e.x];
   if (!in_phase(b, fine) || (apply && inst_stopped(b.st))) return;
   refine_cells(b.p, final_b ? b.e32b : b.e32, b.e32, b.flags, b.g, apply, e.y % b.pgx,
-               e.y / b.pgx, (apply && !fine && save) ? b.pw : nullptr);
+               e.y / b.pgx, (apply && !fine && save) ? b.pw : nullptr, t);
 }
 
-template <int H, int TX, int TY>
-__global__ void __launch_bounds__(512)
-    batch_tb_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int n,
-                    int skip_last_copy, int src_b, int finish, int save) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int2 e = tab[blockIdx.x];
+template <int H, int TX, int TY, int WARPS, bool COH>
+__device__ __forceinline__ void batch_tb_body(const BInst *__restrict__ I, int2 e, int n,
+                                              int skip_last_copy, int src_b, int finish,
+                                              int save, unsigned char *smem_raw) {
   const BInst &b = I[e.x];
   if (!b.solve || inst_stopped(b.st)) return;
   // finish: the outer iteration's last launch also refines (as for one
   // simulation, see sweep_plan)
-  sor32_tb_tile<H, TX, TY>(src_b ? b.e32b : b.e32, src_b ? b.e32 : b.e32b, b.r32, b.flags, b.g,
-                           b.k32, e.y, b.tb_tiles_y, n, skip_last_copy, smem_raw,
-                           finish ? b.p : nullptr, (finish && save) ? b.pw : nullptr);
+  sor32_tb_tile<H, TX, TY, WARPS, COH>(src_b ? b.e32b : b.e32, src_b ? b.e32 : b.e32b, b.r32,
+                                  b.flags, b.g, b.k32, e.y, b.tb_tiles_y, n, skip_last_copy,
+                                  smem_raw, finish ? b.p : nullptr,
+                                  (finish && save) ? b.pw : nullptr);
 }
 
-__global__ void __launch_bounds__(256)
-    batch_restore_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int m) {
-  const int2 e = tab[blockIdx.x];
+__device__ __forceinline__ void batch_restore_body(const BInst *__restrict__ I, int2 e, int m,
+                                                   const Thr t = thr_cta()) {
   const BInst &b = I[e.x];
   if (!b.solve) return;
   StepState *st = b.st;
   const unsigned int replay = st->replay;
-  const bool lead = e.y == 0 && threadIdx.x == 0 && threadIdx.y == 0;
+  const bool lead = e.y == 0 && t.tid == 0;
   if (replay == 2u && lead) st->exhausted = 0;
   if (replay != 1u) return;
   const Geom &g = b.g;
-  const int x = (e.y / b.pgx) * blockDim.y + threadIdx.y;
-  const int y0 = 2 * ((e.y % b.pgx) * blockDim.x + threadIdx.x);
+  const int x = (e.y / b.pgx) * t.dy + t.ty;
+  const int y0 = 2 * ((e.y % b.pgx) * t.dx + t.tx);
   if (x < g.nx) {
 #pragma unroll
     for (int q = 0; q < 2; ++q)
@@ -2977,29 +3329,62 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <bool COH>
+__device__ __forceinline__ void batch_color_body(const BInst *__restrict__ I, int2 e, int color,
+                                                 int copy, const Thr t = thr_cta()) {
+  const BInst &b = I[e.x];
+  if (!in_phase(b, 1) || inst_stopped(b.st)) return;
+  sor32_color_cells<COH>(b.e32, b.r32, b.flags, b.g, b.k32, color, copy, e.y % b.pgx,
+                         e.y / b.pgx, t);
+}
+
+template <bool COH, bool GRP = false>
+__device__ __forceinline__ void batch_residual_body(const BInst *__restrict__ I, int2 e,
+                                                    int check, int fine,
+                                                    const Thr t = thr_cta(),
+                                                    double *scratch = nullptr) {
+  const BInst &b = I[e.x];
+  if (!in_phase(b, fine) || (check == 1 && inst_stopped(b.st))) return;
+  // the member's boundary deltas, block-strided over its nb blocks (as
+  // mixed_residual_kernel does for one simulation)
+  const int nt = t.dx * t.dy;
+  for (int k = e.y * nt + t.tid; k < b.npc; k += b.nb * nt)
+    delta_entry<COH>(b.p, b.r32, b.e32, b.pcopy[k], b.g.pitch);
+  mixed_residual_partial<COH, GRP>(b.p, b.rhs, b.flags, b.r32, b.g, b.c, b.partials,
+                                   b.ty_int, b.nt_int, b.strict, e.y, b.nb, t, scratch);
+}
+
+__global__ void __launch_bounds__(256)
+    batch_refine_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int apply,
+                        int final_b, int fine, int save) {
+  batch_refine_body(I, tab[blockIdx.x], apply, final_b, fine, save);
+}
+
+template <int H, int TX, int TY>
+__global__ void __launch_bounds__(512)
+    batch_tb_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int n,
+                    int skip_last_copy, int src_b, int finish, int save) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  batch_tb_body<H, TX, TY, 16, false>(I, tab[blockIdx.x], n, skip_last_copy, src_b, finish,
+                                      save, smem_raw);
+}
+
+__global__ void __launch_bounds__(256)
+    batch_restore_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int m) {
+  batch_restore_body(I, tab[blockIdx.x], m);
+}
+
 // One colour pass of the finishing members
 __global__ void __launch_bounds__(256)
     batch_color_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int color,
                        int copy) {
-  const int2 e = tab[blockIdx.x];
-  const BInst &b = I[e.x];
-  if (!in_phase(b, 1) || inst_stopped(b.st)) return;
-  sor32_color_cells(b.e32, b.r32, b.flags, b.g, b.k32, color, copy, e.y % b.pgx, e.y / b.pgx);
+  batch_color_body<false>(I, tab[blockIdx.x], color, copy);
 }
 
 __global__ void __launch_bounds__(256)
     batch_residual_kernel(const BInst *__restrict__ I, const int2 *__restrict__ tab, int check,
                           int fine) {
-  const int2 e = tab[blockIdx.x];
-  const BInst &b = I[e.x];
-  if (!in_phase(b, fine) || (check == 1 && inst_stopped(b.st))) return;
-  // the member's boundary deltas, block-strided over its nb blocks (as
-  // mixed_residual_kernel does for one simulation)
-  const int nt = blockDim.x * blockDim.y;
-  for (int k = e.y * nt + threadIdx.y * blockDim.x + threadIdx.x; k < b.npc; k += b.nb * nt)
-    delta_entry(b.p, b.r32, b.e32, b.pcopy[k], b.g.pitch);
-  mixed_residual_partial(b.p, b.rhs, b.flags, b.r32, b.g, b.c, b.partials, b.ty_int, b.nt_int,
-                         b.strict, e.y, b.nb);
+  batch_residual_body<false>(I, tab[blockIdx.x], check, fine);
 }
 
 // One block per instance: its norm and stop rule; the last block to finish
@@ -3061,6 +3446,219 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ------------------------------------------------------------------------
+// Persistent batch solve: the whole WHILE loop above (coarse loop, stop
+// tests, the sweep-by-sweep finishing pass) as one cooperative kernel.  Its
+// CTAs (all resident: cooperative launch) walk the same (instance, block)
+// tables phase by phase, calling the graph kernels' bodies, so every member
+// ends bit-identical to the graph loop and to stepping it alone.  Phases are
+// separated by a grid barrier whose wait is bounded: after `limit` polls a
+// CTA sets BatchState::timeout and returns, and every other CTA returns at
+// its next wait; the host then reports STRM_ERR_TIMEOUT.  No CTA spins
+// without a bound and none traps.
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier (generation counter).  Returns false in every thread of
+// a CTA whose wait ran out or that found another CTA's wait run out.
+__device__ __forceinline__ bool grid_barrier(BatchState *bs, unsigned long long limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    int ok = 1;
+    const unsigned int gen = ld_acquire_u32(&bs->bar_gen);
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&bs->bar_count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&bs->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&bs->bar_gen, 1u);
+    } else {
+      unsigned long long polls = 0;
+      while (ld_acquire_u32(&bs->bar_gen) == gen) {
+        if (ld_acquire_u32(&bs->timeout) != 0u || ++polls > limit) {
+          atomicExch(&bs->timeout, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ld_acquire_u32(&bs->timeout) != 0u) ok = 0;
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// batch_finish_kernel's work for member `mi`, the loop decisions written to
+// bs->go[par] (another body) and bs->open_replay instead of graph
+// conditionals.
+__device__ __forceinline__ void batch_finish_body(const BInst *__restrict__ I, int mi, int n,
+                                                  BatchState *bs, int sweeps, int check,
+                                                  unsigned int itermax_all, int fine, int par,
+                                                  const Thr &t, double *scratch) {
+  const BInst &b = I[mi];
+  const bool active = in_phase(b, fine) && !(check && inst_stopped(b.st));
+  if (mi == 0 && t.tid == 0) {
+    if (!check) {
+      if (!fine) bs->launches = 0;
+    } else {
+      const unsigned int l = atomicAdd(&bs->launches, 1u) + 1;
+      if ((unsigned long long)l * sweeps >= itermax_all + 2ull * sweeps) {
+        bs->overrun = 1;
+        atomicExch(&bs->go[par], 0u);
+      }
+    }
+  }
+  gsync(t);
+  int status = SOLVE_GO_ON;
+  if (active)
+    status = mixed_residual_stop_g(b.partials, b.nb, b.st, b.c, b.itermax, b.strict, sweeps,
+                                   check, t, scratch);
+  if (t.tid == 0) {
+    if (active && status == SOLVE_GO_ON) atomicAdd(&bs->active, 1u);
+    if (active && check && status != SOLVE_GO_ON && !fine && sweeps > 1) {
+      const unsigned int rp = replay_of(status, b.st, b.itermax);
+      b.st->replay = rp;
+      if (rp) atomicAdd(&bs->replays, 1u);
+    }
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&bs->counter, 1u);
+    if (ticket == (unsigned int)n - 1) {
+      __threadfence();
+      const unsigned int act = atomicAdd(&bs->active, 0u);
+      if (check) {
+        const unsigned int body = bs->body_count + 1;
+        bs->body_count = body;
+        if (act == 0) {
+          atomicExch(&bs->go[par], 0u);
+          if (!fine && atomicAdd(&bs->replays, 0u) > 0) atomicExch(&bs->open_replay, 1u);
+        } else if ((unsigned long long)body * sweeps >= itermax_all + 2ull * sweeps) {
+          bs->overrun = 1;
+          atomicExch(&bs->go[par], 0u);
+        }
+      } else if (!fine) {
+        bs->body_count = 0;
+        bs->replays = 0;
+      }
+      bs->active = 0;
+      bs->counter = 0;
+    }
+  }
+}
+
+struct PersistArgs {
+  const BInst *inst;
+  const int2 *t_res, *t_ref, *t_tb;
+  int nres, nref, ntb, n;
+  BatchState *bs;
+  int m;             // sweeps per stop test
+  int sweeps;        // sweeps per blocked tile pass
+  int fused;         // the last blocked pass of an outer iteration refines
+  unsigned int itermax_all;
+  unsigned long long limit;  // polls a barrier wait may take
+};
+
+constexpr int kPersistWarps = 16;  // CTA of (32, 16) threads: two (32, 8) groups
+
+template <int H, int TX, int TY>
+__global__ void __launch_bounds__(32 * kPersistWarps, 3)
+    batch_persistent_kernel(PersistArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const BInst *I = a.inst;
+  BatchState *bs = a.bs;
+  // the two 256-thread groups of the CTA: each takes its own table entry in
+  // the (32 x 8)-block phases; their reduction scratch is the start of the
+  // sweep tiles' dynamic shared memory (free between tile phases)
+  Thr t;
+  t.tx = threadIdx.x;
+  t.ty = threadIdx.y & 7;
+  t.dx = 32;
+  t.dy = 8;
+  t.tid = t.tx + 32 * t.ty;
+  t.half = threadIdx.y >> 3;
+  t.bar = 1 + t.half;
+  double *scratch = reinterpret_cast<double *>(smem_raw);
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0;
+  const int gstart = 2 * blockIdx.x + t.half, gstride = 2 * gridDim.x;
+// a phase over the sweep tiles: one entry per CTA at a time
+#define TILE_PHASE(N, BODY)                                      \
+  for (int vb = blockIdx.x; vb < (N); vb += gridDim.x) {         \
+    BODY;                                                        \
+    __syncthreads();                                             \
+  }                                                              \
+  if (!grid_barrier(bs, a.limit)) return;
+// a phase over (32 x 8)-block entries: one entry per group at a time
+#define GROUP_PHASE(N, BODY)                                     \
+  for (int vb = gstart; vb < (N); vb += gstride) {               \
+    BODY;                                                        \
+    gsync(t);                                                    \
+  }                                                              \
+  if (!grid_barrier(bs, a.limit)) return;
+
+  // before the loop: clear the corrections, the starting norms
+  GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 0, 0, 0, 0, t));
+  GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 0, 0, t, scratch)));
+  GROUP_PHASE(a.n, batch_finish_body(I, vb, a.n, bs, a.m, 0, a.itermax_all, 0, 0, t, scratch));
+  // the coarse loop: m sweeps, then the stop test
+  for (unsigned int body = 0;; ++body) {
+    const int par = body & 1;
+    if (lead) atomicExch(&bs->go[par], 1u);
+    int launches = 0;
+    for (int done = 0; done < a.m; done += a.sweeps, ++launches) {
+      const int cnt = a.m - done < a.sweeps ? a.m - done : a.sweeps;
+      const int last = done + cnt >= a.m ? 1 : 0;
+      TILE_PHASE(a.ntb, (batch_tb_body<H, TX, TY, kPersistWarps, true>(
+                            I, a.t_tb[vb], cnt, last, launches & 1, (last && a.fused) ? 1 : 0,
+                            a.m > 1 ? 1 : 0, smem_raw)));
+    }
+    if (!a.fused) {
+      GROUP_PHASE(a.nref,
+                  batch_refine_body(I, a.t_ref[vb], 1, launches & 1, 0, a.m > 1 ? 1 : 0, t));
+    }
+    GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 1, 0, t, scratch)));
+    GROUP_PHASE(a.n,
+                batch_finish_body(I, vb, a.n, bs, a.m, 1, a.itermax_all, 0, par, t, scratch));
+    if (ld_acquire_u32(&bs->go[par]) == 0u) break;
+  }
+  if (a.m <= 1 || ld_acquire_u32(&bs->open_replay) == 0u) return;
+  // members whose coarse loop stopped between checks finish sweep by sweep
+  GROUP_PHASE(a.nref, batch_restore_body(I, a.t_ref[vb], a.m, t));
+  GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 0, 0, 1, 0, t));
+  GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 2, 1, t, scratch)));
+  for (unsigned int body = 0;; ++body) {
+    const int par = body & 1;
+    if (lead) atomicExch(&bs->go[par], 1u);
+    GROUP_PHASE(a.nref, batch_color_body<true>(I, a.t_ref[vb], 0, 1, t));
+    GROUP_PHASE(a.nref, batch_color_body<true>(I, a.t_ref[vb], 1, 0, t));
+    GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 1, 0, 1, 0, t));
+    GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 1, 1, t, scratch)));
+    GROUP_PHASE(a.n,
+                batch_finish_body(I, vb, a.n, bs, 1, 1, a.itermax_all, 1, par, t, scratch));
+    if (ld_acquire_u32(&bs->go[par]) == 0u) break;
+  }
+#undef TILE_PHASE
+#undef GROUP_PHASE
+}
+
+static const void *batch_persistent_fn(int sched) {
+  switch (sched) {
+    case 1: return (const void *)batch_persistent_kernel<4, 56, 120>;
+    case 2: return (const void *)batch_persistent_kernel<8, 48, 112>;
+    case 3: return (const void *)batch_persistent_kernel<16, 32, 96>;
+    case 4: return (const void *)batch_persistent_kernel<8, 80, 112>;
+    case 5: return (const void *)batch_persistent_kernel<8, 112, 112>;
+    case 6: return (const void *)batch_persistent_kernel<16, 64, 96>;
+    default: return nullptr;
+  }
+}
+
 static const void *batch_tb_fn(int sched) {
   switch (sched) {
     case 1: return (const void *)batch_tb_kernel<4, 56, 120>;
@@ -3085,7 +3683,19 @@ void free_batch(BatchPlan *bp) {
   bp->state = nullptr;
 }
 
-cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp) {
+// Dynamic shared memory of the persistent solve: the sweep tiles', which
+// also hold the groups' reduction scratch between tile phases.
+static size_t persist_smem(const TbShape &t) {
+  const size_t scratch = (2 * 512 + 2 * 32) * sizeof(double);
+  const size_t tiles = tb_smem(t);
+  return tiles > scratch ? tiles : scratch;
+}
+
+static_assert(offsetof(BatchState, overrun) == kBatchOverrunOffset, "overrun offset");
+static_assert(offsetof(BatchState, timeout) == kBatchTimeoutOffset, "timeout offset");
+
+cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp,
+                        int persistent, unsigned long long wait_limit) {
   *bp = BatchPlan{};
   const int n = (int)mem.size();
   if (n < 1 || m < 1 || sched < 1 || sched >= kNumSchedules) return cudaErrorInvalidValue;
@@ -3165,6 +3775,25 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
     return e;
   }
 
+  // the persistent solve: as many CTAs as can be resident at once
+  int persist_grid = 0;
+  if (persistent) {
+    const void *fn = batch_persistent_fn(sched);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)persist_smem(shape));
+    int per_sm = 0;
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kPersistWarps,
+                                                        persist_smem(shape));
+    if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+    if (e != cudaSuccess) {
+      free_batch(bp);
+      return e;
+    }
+    persist_grid = per_sm * num_sms();
+    bp->persist_grid = persist_grid;
+  }
+
   // part 0: the whole step; 1: the members' first halves (boundary pass,
   // F/G, RHS); 2: the pressure solves and the second halves
   auto assemble = [&](int part, cudaGraph_t *out) -> cudaError_t {
@@ -3197,9 +3826,43 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
   const int nres = (int)t_res.size(), nref = (int)t_ref.size();
   const int ntb = (int)t_tb.size();
   cudaGraphConditionalHandle h{};
-  if (b.err == cudaSuccess)
+  if (b.err == cudaSuccess && !persistent)
     b.err = cudaGraphConditionalHandleCreate(&h, b.graph, 1, cudaGraphCondAssignDefault);
-  if (nres > 0) {
+  if (nres > 0 && persistent) {
+    // the whole solve as one cooperative kernel: its barrier state zeroed
+    // first, then one CTA per resident slot walking the tables
+    cudaMemsetParams ms{};
+    ms.dst = (char *)d_bs;
+    ms.value = 0;
+    ms.elementSize = 4;
+    ms.width = offsetof(BatchState, overrun) / 4;
+    ms.height = 1;
+    cudaGraphNode_t mnode = nullptr;
+    if (b.err == cudaSuccess)
+      b.err = cudaGraphAddMemsetNode(&mnode, b.graph, nd ? &nd : nullptr, nd ? 1 : 0, &ms);
+    PersistArgs pa{};
+    pa.inst = d_inst;
+    pa.t_res = d_res;
+    pa.t_ref = d_ref;
+    pa.t_tb = d_tb;
+    pa.nres = nres;
+    pa.nref = nref;
+    pa.ntb = ntb;
+    pa.n = n;
+    pa.bs = d_bs;
+    pa.m = m;
+    pa.sweeps = shape.sweeps;
+    pa.fused = ((m + shape.sweeps - 1) / shape.sweeps) % 2 == 0 ? 1 : 0;
+    pa.itermax_all = itermax_all;
+    pa.limit = wait_limit;
+    nd = b.kernel_smem(b.graph, mnode, batch_persistent_fn(sched), dim3(persist_grid),
+                       dim3(32, kPersistWarps), persist_smem(shape), pa);
+    if (b.err == cudaSuccess) {
+      cudaLaunchAttributeValue v{};
+      v.cooperative = 1;
+      b.err = cudaGraphKernelNodeSetAttribute(nd, cudaLaunchAttributeCooperative, &v);
+    }
+  } else if (nres > 0) {
     cudaGraphConditionalHandle h_rep{};
     if (b.err == cudaSuccess)
       b.err = cudaGraphConditionalHandleCreate(&h_rep, b.graph, 0, cudaGraphCondAssignDefault);

@@ -140,15 +140,21 @@ struct BatchState;
 struct BatchPlan {
   void *dev = nullptr;          // device tables (one allocation)
   BatchState *state = nullptr;  // in dev: loop counters and the overrun flag
+  int persist_grid = 0;         // CTAs of the persistent solve (0: graph loop)
   cudaGraph_t graph = nullptr;        // the whole step
   cudaGraph_t graph_pre = nullptr;    // the members' boundary pass, F/G, RHS
   cudaGraph_t graph_solve = nullptr;  // the pressure solves and the second halves
 };
 // sched: internal blocked schedule (1..num_sweep_schedules()-1); m: sweeps
-// per refinement (every member needs max_iterations >= m).
-cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp);
+// per refinement (every member needs max_iterations >= m).  persistent: the
+// pressure solves run as one cooperative kernel whose grid barriers give up
+// after wait_limit polls (otherwise as a WHILE loop of graph kernels).
+cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, BatchPlan *bp,
+                        int persistent = 0, unsigned long long wait_limit = 0);
 void free_batch(BatchPlan *bp);
-// Offset of BatchState::overrun in bytes (the host reads it after steps).
-constexpr size_t kBatchOverrunOffset = 3 * sizeof(unsigned int);
+// Offsets in bytes of BatchState::overrun and ::timeout (the host reads them
+// after steps).
+constexpr size_t kBatchOverrunOffset = 10 * sizeof(unsigned int);
+constexpr size_t kBatchTimeoutOffset = 11 * sizeof(unsigned int);
 
 }  // namespace strm

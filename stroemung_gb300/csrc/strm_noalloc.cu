@@ -1,13 +1,14 @@
 // Allocation-free residual norm (strm_norm_squared_noalloc).
 //
-// For callers that cannot allocate device memory at the moment they need the
-// norm: code running while a CUDA stream is being captured into a graph
-// (cudaMalloc is not permitted there), host frameworks that own the whole
-// device-memory budget through their own pool, and fixed-footprint real-time
-// loops.  They pass their own pressure and RHS fields and an 8-byte device
-// output; the reduction scratch this needs (one partial sum per 8 x 64 tile of
-// the interior, plus a completion ticket) lives in a file-scope __device__
-// array of fixed size that every GPU loading the library keeps until exit.
+// For callers that must not allocate device memory once they are running:
+// host frameworks whose caching allocator already owns the device budget (a
+// cudaMalloc beside that pool can fail or fragment it), and fixed-footprint
+// loops that reserve all of their memory at start-up because cudaMalloc may
+// synchronise the device and has no latency bound.  They pass their own
+// pressure and RHS fields and an 8-byte device output; the reduction scratch
+// this needs (one partial sum per 8 x 64 tile of the interior, plus a
+// completion ticket) lives in a file-scope __device__ array of fixed size
+// that every GPU loading the library keeps until the process exits.
 //
 // Limit: at most STRM_NORM_NOALLOC_MAX_TILES tiles, i.e. interior grids with
 // ceil((nx-2)/8) * ceil((ny-2)/64) <= 16384 (for example 4096 x 2048 interior
@@ -17,6 +18,13 @@
 // calls whose GPU work overlaps (two streams, or two host threads) race on it
 // and give wrong results; serialise them.  Each call clears the fields that
 // must start at zero before its reduction runs.
+//
+// The array's device address is looked up once per device, on the first
+// call made with that device current, and kept for the life of the process;
+// a cudaDeviceReset while the library is in use invalidates it and is not
+// supported.
+#include <float.h>
+
 #include <mutex>
 
 #include "../../include/stroemung_gpu.h"
@@ -68,8 +76,11 @@ __global__ void noalloc_end(const StepState *st, double *out) { *out = st->aux; 
 extern "C" int strm_norm_squared_noalloc(const double *p, const double *rhs, int nx, int ny,
                                          int pitch, double dx, double dy, double fluid_cells,
                                          double *norm_squared, void *stream) {
+  // fluid_cells divides the sum (the reference's BoundaryList::fluid_cells):
+  // zero, negative or non-finite counts are rejected like the other
+  // entry points' bad arguments
   if (!p || !rhs || !norm_squared || nx < 1 || ny < 1 || pitch < ny || !(dx > 0.0) ||
-      !(dy > 0.0))
+      !(dy > 0.0) || !(fluid_cells > 0.0) || !(fluid_cells <= DBL_MAX))
     return STRM_ERR_INVALID;
   Geom g{nx, ny, pitch};
   const int tiles = interior_tiles(g);

@@ -23,13 +23,14 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (ARITH_EXACT, ARITH_FAST, NORM_ALL_INTERIOR, NORM_FLUID,
-                   NORM_FLUID_MEAN_FREE, PREC_FP64,
-                   PREC_MIXED, SOR_LEXICOGRAPHIC, SOR_RED_BLACK, BoundaryTooThinError, NonFiniteError, StroemungError)
+from ._lib import (ARITH_EXACT, ARITH_FAST, EXEC_EAGER, EXEC_GRAPH, NORM_ALL_INTERIOR,
+                   NORM_FLUID, NORM_FLUID_MEAN_FREE, PREC_FP64, PREC_MIXED, SOR_LEXICOGRAPHIC,
+                   SOR_RED_BLACK, BoundaryTooThinError, NonFiniteError, StroemungError)
 
 __all__ = ["Simulation", "BoundaryTooThinError", "NonFiniteError", "StroemungError",
            "SOR_RED_BLACK", "SOR_LEXICOGRAPHIC", "ARITH_EXACT", "ARITH_FAST", "PREC_FP64",
-           "PREC_MIXED", "NORM_ALL_INTERIOR", "NORM_FLUID", "NORM_FLUID_MEAN_FREE"]
+           "PREC_MIXED", "NORM_ALL_INTERIOR", "NORM_FLUID", "NORM_FLUID_MEAN_FREE",
+           "EXEC_GRAPH", "EXEC_EAGER"]
 
 _FIELDS = {"u": _lib.FIELD_U, "v": _lib.FIELD_V, "p": _lib.FIELD_P, "pressure": _lib.FIELD_P,
            "f": _lib.FIELD_F, "g": _lib.FIELD_G, "rhs": _lib.FIELD_RHS}

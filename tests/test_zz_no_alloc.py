@@ -1,13 +1,15 @@
 """The allocation-free residual norm (strm_norm_squared_noalloc).
 
-Callers that cannot allocate device memory at call time — code running inside
-a CUDA stream capture, frameworks whose own pool owns the device budget,
-fixed-footprint real-time loops — get the residual norm from a fixed
-reduction scratch inside the library.  This test calls it through the C ABI on
-a live simulation's own fields and checks it against the ordinary entry point
-(strm_calculate_norm_squared) within the 1e-12 relative tolerance the norm
-parity tests use, on two calls in a row and again after further steps; it
-also checks that a grid beyond the scratch limit is rejected before any GPU
+Callers that must not allocate device memory once they run — host frameworks
+whose caching allocator owns the device budget, fixed-footprint loops that
+reserve all memory at start-up because cudaMalloc may synchronise the device —
+get the residual norm from a fixed reduction scratch inside the library.
+This test calls it through the C ABI on a live simulation's own fields and
+checks it against the ordinary entry point (strm_calculate_norm_squared,
+default norm over every interior cell) within the 1e-12 relative tolerance
+the norm parity tests use, on two calls in a row and again after further
+steps; it also checks that a grid beyond the scratch limit and a
+non-positive or non-finite fluid-cell count are rejected before any GPU
 work.  This file is collected last so that a failure here never hides
 another test.
 """
@@ -61,5 +63,14 @@ def test_noalloc_norm_rejects_grids_beyond_its_scratch():
     dummy = ctypes.cast(ctypes.c_void_p(256), ctypes.POINTER(ctypes.c_double))
     # 20000 x 20000 interior cells need far more than 16384 tiles
     rc = L.strm_norm_squared_noalloc(dummy, dummy, 20002, 20002, 20016, 0.1, 0.1, 1.0,
+                                     dummy, None)
+    assert rc == _lib.STRM_ERR_INVALID
+
+
+@pytest.mark.parametrize("fluid_cells", [0.0, -5.0, float("nan"), float("inf")])
+def test_noalloc_norm_rejects_bad_fluid_cell_counts(fluid_cells):
+    L = _lib.load()
+    dummy = ctypes.cast(ctypes.c_void_p(256), ctypes.POINTER(ctypes.c_double))
+    rc = L.strm_norm_squared_noalloc(dummy, dummy, 66, 66, 80, 0.1, 0.1, fluid_cells,
                                      dummy, None)
     assert rc == _lib.STRM_ERR_INVALID
