@@ -2085,6 +2085,53 @@ __device__ double reduce_partials_g(const double *part, int n, int stride, int i
   return block_reduce_g(v, op, identity, t, scratch);
 }
 
+// mixed_residual_sum for a 256-thread group of the persistent batch solve:
+// p changes within that launch, so it is read through L2; each 8 x 64 tile
+// of p and its one-cell halo is first staged in shared memory (one L2 load
+// per cell instead of five), then every thread takes exactly the cells, in
+// exactly the order, of mixed_residual_sum: the sums are bit-identical.
+// tile: 10 x 66 doubles of the group's shared memory.
+template <bool FLUID, bool MEAN_FREE>
+__device__ __forceinline__ void mixed_residual_sum_staged(
+    const double *__restrict__ p, const double *__restrict__ rhs,
+    const uint8_t *__restrict__ flags, float *__restrict__ s, const Geom &g, const Consts &c,
+    int tiles_y, int ntiles, int bid, int nblocks, double *acc_out, double *acc1_out,
+    const Thr &th, double *tile) {
+  constexpr int TW = RT_Y + 2;
+  double acc = 0.0, acc1 = 0.0;
+  const float mid32 = narrow(c.middle);
+  for (int t = bid; t < ntiles; t += nblocks) {
+    const int x0 = 1 + (t / tiles_y) * RT_X, y0 = 1 + (t % tiles_y) * RT_Y;
+    gsync(th);  // the previous tile's readers are done
+    for (int k = th.tid; k < (RT_X + 2) * TW; k += 256) {
+      const int i = k / TW, j = k % TW;
+      const int x = x0 - 1 + i, y = y0 - 1 + j;
+      tile[k] = (x < g.nx && y < g.ny) ? __ldcg(p + OFF(x, y)) : 0.0;
+    }
+    gsync(th);
+    const int x = x0 + th.ty;
+    if (x > g.nx - 2) continue;
+    const int lx = th.ty + 1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int ly = 2 * th.tx + q + 1, y = y0 + ly - 1;
+      if (y <= g.ny - 2) {
+        const size_t o = OFF(x, y);
+        const double *tc = tile + lx * TW + ly;
+        const double r = residual_of<false>(tc[0], tc[-TW], tc[TW], tc[-1], tc[1], rhs[o], c);
+        const bool fluid = flags[o] == 0;
+        if (fluid || !FLUID) {
+          acc = fma(r, r, acc);
+          if (MEAN_FREE) acc1 += r;
+        }
+        if (fluid) s[o] = narrow(r) * mid32;
+      }
+    }
+  }
+  *acc_out = acc;
+  *acc1_out = acc1;
+}
+
 // FP64 norm of the residual on every interior cell (the reference's norm),
 // the scaled FP32 defect s = middle * r on fluid cells for the next sweeps,
 // and the stop rule every m sweeps.  Block `bid` of `nblocks` sums its tiles
@@ -2100,15 +2147,30 @@ __device__ __forceinline__ void mixed_residual_partial(
   const bool fluid_only = (strict & STOP_FLUID_NORM) != 0;
   const bool mean_free = fluid_only && (strict & STOP_MEAN_FREE) != 0;
   double acc = 0.0, acc1 = 0.0;
-  if (!fluid_only)
-    mixed_residual_sum<false, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
-                                          &acc, &acc1, th);
-  else if (!mean_free)
-    mixed_residual_sum<true, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
-                                         &acc, &acc1, th);
-  else
-    mixed_residual_sum<true, true, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid, nblocks,
-                                        &acc, &acc1, th);
+  if constexpr (GRP) {
+    // the group's p tile follows the reduction scratch (2 x 512 + 2 x 32
+    // doubles) in the persistent kernel's shared memory
+    double *tile = scratch + 2 * 512 + 2 * 32 + th.half * (RT_X + 2) * (RT_Y + 2);
+    if (!fluid_only)
+      mixed_residual_sum_staged<false, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                              nblocks, &acc, &acc1, th, tile);
+    else if (!mean_free)
+      mixed_residual_sum_staged<true, false>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                             nblocks, &acc, &acc1, th, tile);
+    else
+      mixed_residual_sum_staged<true, true>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                            nblocks, &acc, &acc1, th, tile);
+  } else {
+    if (!fluid_only)
+      mixed_residual_sum<false, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                            nblocks, &acc, &acc1, th);
+    else if (!mean_free)
+      mixed_residual_sum<true, false, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                           nblocks, &acc, &acc1, th);
+    else
+      mixed_residual_sum<true, true, COH>(p, rhs, flags, s, g, c, tiles_y, ntiles, bid,
+                                          nblocks, &acc, &acc1, th);
+  }
   if (mean_free) {
     if constexpr (GRP) block_sum_pass_g<true>(acc, acc1, th, scratch);
     else block_sum_pass<true>(acc, acc1);
@@ -3566,6 +3628,10 @@ struct PersistArgs {
 };
 
 constexpr int kPersistWarps = 16;  // CTA of (32, 16) threads: two (32, 8) groups
+// Members whose state bits each CTA keeps in shared memory (larger batches
+// read each member's state from global memory in every phase).
+constexpr int kPersistMaxMembers = 1024;
+enum : uint8_t { ACT_SOLVE = 1, ACT_STOPPED = 2, ACT_REPLAY = 4 };
 
 template <int H, int TX, int TY>
 __global__ void __launch_bounds__(32 * kPersistWarps, 3)
@@ -3587,25 +3653,72 @@ __global__ void __launch_bounds__(32 * kPersistWarps, 3)
   double *scratch = reinterpret_cast<double *>(smem_raw);
   const bool lead = blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0;
   const int gstart = 2 * blockIdx.x + t.half, gstride = 2 * gridDim.x;
+  // every member's state bits, refreshed after each phase that changes them
+  // (the stop tests, the finishing pass's restore), so that entries of
+  // members a phase does not touch are skipped without a global load; the
+  // bodies still apply their own tests to the entries they get
+  __shared__ uint8_t s_act[kPersistMaxMembers];
+  const bool masked = a.n <= kPersistMaxMembers;
+  auto refresh = [&]() {
+    if (masked) {
+      const int tid = threadIdx.y * 32 + threadIdx.x;
+      for (int i = tid; i < a.n; i += 32 * kPersistWarps) {
+        const BInst &b = I[i];
+        uint8_t v = b.solve ? ACT_SOLVE : 0;
+        if (b.solve) {
+          const StepState *st = b.st;
+          if (__ldcg(&st->converged) || __ldcg(&st->exhausted)) v |= ACT_STOPPED;
+          if (__ldcg(&st->replay) != 0u) v |= ACT_REPLAY;
+        }
+        s_act[i] = v;
+      }
+    }
+    __syncthreads();
+  };
+  // skip tests: no solve; stopped or no solve; not finishing; not finishing
+  // or stopped
+  auto no_solve = [&](int mi) { return masked && !(s_act[mi] & ACT_SOLVE); };
+  auto idle = [&](int mi) {
+    return masked && (s_act[mi] & (ACT_SOLVE | ACT_STOPPED)) != ACT_SOLVE;
+  };
+  auto no_fine = [&](int mi) {
+    return masked && (s_act[mi] & (ACT_SOLVE | ACT_REPLAY)) != (ACT_SOLVE | ACT_REPLAY);
+  };
+  auto idle_fine = [&](int mi) {
+    return masked && (s_act[mi] & (ACT_SOLVE | ACT_REPLAY | ACT_STOPPED)) !=
+                         (ACT_SOLVE | ACT_REPLAY);
+  };
+  refresh();
 // a phase over the sweep tiles: one entry per CTA at a time
-#define TILE_PHASE(N, BODY)                                      \
+#define TILE_PHASE(N, TAB, SKIP, BODY)                           \
   for (int vb = blockIdx.x; vb < (N); vb += gridDim.x) {         \
+    if (SKIP((TAB)[vb].x)) continue;                             \
     BODY;                                                        \
     __syncthreads();                                             \
   }                                                              \
   if (!grid_barrier(bs, a.limit)) return;
 // a phase over (32 x 8)-block entries: one entry per group at a time
-#define GROUP_PHASE(N, BODY)                                     \
+#define GROUP_PHASE(N, TAB, SKIP, BODY)                          \
   for (int vb = gstart; vb < (N); vb += gstride) {               \
+    if (SKIP((TAB)[vb].x)) continue;                             \
     BODY;                                                        \
     gsync(t);                                                    \
   }                                                              \
   if (!grid_barrier(bs, a.limit)) return;
+// the stop tests: every member, then the state bits are refreshed
+#define FINISH_PHASE(BODY)                                       \
+  for (int vb = gstart; vb < a.n; vb += gstride) {               \
+    BODY;                                                        \
+    gsync(t);                                                    \
+  }                                                              \
+  if (!grid_barrier(bs, a.limit)) return;                        \
+  refresh();
 
   // before the loop: clear the corrections, the starting norms
-  GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 0, 0, 0, 0, t));
-  GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 0, 0, t, scratch)));
-  GROUP_PHASE(a.n, batch_finish_body(I, vb, a.n, bs, a.m, 0, a.itermax_all, 0, 0, t, scratch));
+  GROUP_PHASE(a.nref, a.t_ref, no_solve, batch_refine_body(I, a.t_ref[vb], 0, 0, 0, 0, t));
+  GROUP_PHASE(a.nres, a.t_res, no_solve,
+              (batch_residual_body<true, true>(I, a.t_res[vb], 0, 0, t, scratch)));
+  FINISH_PHASE(batch_finish_body(I, vb, a.n, bs, a.m, 0, a.itermax_all, 0, 0, t, scratch));
   // the coarse loop: m sweeps, then the stop test
   for (unsigned int body = 0;; ++body) {
     const int par = body & 1;
@@ -3614,37 +3727,44 @@ __global__ void __launch_bounds__(32 * kPersistWarps, 3)
     for (int done = 0; done < a.m; done += a.sweeps, ++launches) {
       const int cnt = a.m - done < a.sweeps ? a.m - done : a.sweeps;
       const int last = done + cnt >= a.m ? 1 : 0;
-      TILE_PHASE(a.ntb, (batch_tb_body<H, TX, TY, kPersistWarps, true>(
-                            I, a.t_tb[vb], cnt, last, launches & 1, (last && a.fused) ? 1 : 0,
-                            a.m > 1 ? 1 : 0, smem_raw)));
+      TILE_PHASE(a.ntb, a.t_tb, idle,
+                 (batch_tb_body<H, TX, TY, kPersistWarps, true>(
+                     I, a.t_tb[vb], cnt, last, launches & 1, (last && a.fused) ? 1 : 0,
+                     a.m > 1 ? 1 : 0, smem_raw)));
     }
     if (!a.fused) {
-      GROUP_PHASE(a.nref,
+      GROUP_PHASE(a.nref, a.t_ref, idle,
                   batch_refine_body(I, a.t_ref[vb], 1, launches & 1, 0, a.m > 1 ? 1 : 0, t));
     }
-    GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 1, 0, t, scratch)));
-    GROUP_PHASE(a.n,
-                batch_finish_body(I, vb, a.n, bs, a.m, 1, a.itermax_all, 0, par, t, scratch));
+    GROUP_PHASE(a.nres, a.t_res, idle,
+                (batch_residual_body<true, true>(I, a.t_res[vb], 1, 0, t, scratch)));
+    FINISH_PHASE(
+        batch_finish_body(I, vb, a.n, bs, a.m, 1, a.itermax_all, 0, par, t, scratch));
     if (ld_acquire_u32(&bs->go[par]) == 0u) break;
   }
   if (a.m <= 1 || ld_acquire_u32(&bs->open_replay) == 0u) return;
   // members whose coarse loop stopped between checks finish sweep by sweep
-  GROUP_PHASE(a.nref, batch_restore_body(I, a.t_ref[vb], a.m, t));
-  GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 0, 0, 1, 0, t));
-  GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 2, 1, t, scratch)));
+  // (the restore re-opens the members that ran out of room)
+  GROUP_PHASE(a.nref, a.t_ref, no_fine, batch_restore_body(I, a.t_ref[vb], a.m, t));
+  refresh();
+  GROUP_PHASE(a.nref, a.t_ref, no_fine, batch_refine_body(I, a.t_ref[vb], 0, 0, 1, 0, t));
+  GROUP_PHASE(a.nres, a.t_res, no_fine,
+              (batch_residual_body<true, true>(I, a.t_res[vb], 2, 1, t, scratch)));
   for (unsigned int body = 0;; ++body) {
     const int par = body & 1;
     if (lead) atomicExch(&bs->go[par], 1u);
-    GROUP_PHASE(a.nref, batch_color_body<true>(I, a.t_ref[vb], 0, 1, t));
-    GROUP_PHASE(a.nref, batch_color_body<true>(I, a.t_ref[vb], 1, 0, t));
-    GROUP_PHASE(a.nref, batch_refine_body(I, a.t_ref[vb], 1, 0, 1, 0, t));
-    GROUP_PHASE(a.nres, (batch_residual_body<true, true>(I, a.t_res[vb], 1, 1, t, scratch)));
-    GROUP_PHASE(a.n,
-                batch_finish_body(I, vb, a.n, bs, 1, 1, a.itermax_all, 1, par, t, scratch));
+    GROUP_PHASE(a.nref, a.t_ref, idle_fine, batch_color_body<true>(I, a.t_ref[vb], 0, 1, t));
+    GROUP_PHASE(a.nref, a.t_ref, idle_fine, batch_color_body<true>(I, a.t_ref[vb], 1, 0, t));
+    GROUP_PHASE(a.nref, a.t_ref, idle_fine, batch_refine_body(I, a.t_ref[vb], 1, 0, 1, 0, t));
+    GROUP_PHASE(a.nres, a.t_res, idle_fine,
+                (batch_residual_body<true, true>(I, a.t_res[vb], 1, 1, t, scratch)));
+    FINISH_PHASE(
+        batch_finish_body(I, vb, a.n, bs, 1, 1, a.itermax_all, 1, par, t, scratch));
     if (ld_acquire_u32(&bs->go[par]) == 0u) break;
   }
 #undef TILE_PHASE
 #undef GROUP_PHASE
+#undef FINISH_PHASE
 }
 
 static const void *batch_persistent_fn(int sched) {
@@ -3684,9 +3804,10 @@ void free_batch(BatchPlan *bp) {
 }
 
 // Dynamic shared memory of the persistent solve: the sweep tiles', which
-// also hold the groups' reduction scratch between tile phases.
+// also hold the groups' reduction scratch and residual tiles between tile
+// phases.
 static size_t persist_smem(const TbShape &t) {
-  const size_t scratch = (2 * 512 + 2 * 32) * sizeof(double);
+  const size_t scratch = (2 * 512 + 2 * 32 + 2 * (RT_X + 2) * (RT_Y + 2)) * sizeof(double);
   const size_t tiles = tb_smem(t);
   return tiles > scratch ? tiles : scratch;
 }
