@@ -39,14 +39,17 @@ def save_bf16(net, path: Path) -> str:
     return hashlib.sha256(arr.tobytes()).hexdigest()
 
 
+def bf16_bits_to_f32(bits: np.ndarray) -> np.ndarray:
+    """BF16 values stored as uint16 bit patterns -> the same values as
+    float32 (exact: BF16 is the top half of an FP32)."""
+    return (np.asarray(bits, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
 def load_weights(net, path) -> str:
     """Loads parameters saved by save_bf16 (uint16 BF16 bits) or FP32
     parameters (float32); returns the SHA-256 of the stored array."""
     arr = np.load(path)
-    if arr.dtype == np.uint16:
-        theta = (arr.astype(np.uint32) << 16).view(np.float32)
-    else:
-        theta = arr.astype(np.float32)
+    theta = bf16_bits_to_f32(arr) if arr.dtype == np.uint16 else arr.astype(np.float32)
     net.load_state_dict({"theta": theta, "step": 1})
     return hashlib.sha256(arr.tobytes()).hexdigest()
 
