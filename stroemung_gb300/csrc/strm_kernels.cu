@@ -3323,6 +3323,7 @@ struct BatchState {
   unsigned int bar_gen;
   unsigned int go[2];
   unsigned int open_replay;
+  unsigned int work[2];   // next table entry of the current phase (by parity)
   // the fields above are zeroed before every persistent solve (a solve cut
   // short by a barrier timeout can leave them anywhere); these two collect
   // over the steps of one call and are reset by the host before it
@@ -3658,6 +3659,9 @@ __global__ void __launch_bounds__(32 * kPersistWarps, 3)
   // members a phase does not touch are skipped without a global load; the
   // bodies still apply their own tests to the entries they get
   __shared__ uint8_t s_act[kPersistMaxMembers];
+  __shared__ int s_next[3];  // next entry: the CTA's, then each group's
+  const int ctid = threadIdx.y * 32 + threadIdx.x;
+  unsigned int phase = 0;    // dynamically scheduled phases so far
   const bool masked = a.n <= kPersistMaxMembers;
   auto refresh = [&]() {
     if (masked) {
@@ -3689,21 +3693,55 @@ __global__ void __launch_bounds__(32 * kPersistWarps, 3)
                          (ACT_SOLVE | ACT_REPLAY);
   };
   refresh();
+// Entries are handed out dynamically: a CTA (or a group) takes the next
+// entry of the phase from an atomic counter, asked for one entry ahead so
+// that the atomic's latency overlaps the work; which CTA does an entry does
+// not change its result.  The counters alternate by phase parity: the one
+// of the previous phase is cleared during this one (every CTA has passed
+// the barrier that ended it).
 // a phase over the sweep tiles: one entry per CTA at a time
-#define TILE_PHASE(N, TAB, SKIP, BODY)                           \
-  for (int vb = blockIdx.x; vb < (N); vb += gridDim.x) {         \
-    if (SKIP((TAB)[vb].x)) continue;                             \
-    BODY;                                                        \
-    __syncthreads();                                             \
-  }                                                              \
+#define TILE_PHASE(N, TAB, SKIP, BODY)                                       \
+  {                                                                          \
+    unsigned int *ctr = &bs->work[phase & 1];                                \
+    if (lead) atomicExch(&bs->work[(phase & 1) ^ 1], 0u);                    \
+    if (ctid == 0) s_next[0] = (int)atomicAdd(ctr, 1u);                      \
+    __syncthreads();                                                         \
+    int vb = s_next[0];                                                      \
+    while (vb < (N)) {                                                       \
+      __syncthreads();                                                       \
+      int nxt = 0;                                                           \
+      if (ctid == 0) nxt = (int)atomicAdd(ctr, 1u);                          \
+      if (!SKIP((TAB)[vb].x)) {                                              \
+        BODY;                                                                \
+      }                                                                      \
+      if (ctid == 0) s_next[0] = nxt;                                        \
+      __syncthreads();                                                       \
+      vb = s_next[0];                                                        \
+    }                                                                        \
+    ++phase;                                                                 \
+  }                                                                          \
   if (!grid_barrier(bs, a.limit)) return;
 // a phase over (32 x 8)-block entries: one entry per group at a time
-#define GROUP_PHASE(N, TAB, SKIP, BODY)                          \
-  for (int vb = gstart; vb < (N); vb += gstride) {               \
-    if (SKIP((TAB)[vb].x)) continue;                             \
-    BODY;                                                        \
-    gsync(t);                                                    \
-  }                                                              \
+#define GROUP_PHASE(N, TAB, SKIP, BODY)                                      \
+  {                                                                          \
+    unsigned int *ctr = &bs->work[phase & 1];                                \
+    if (lead) atomicExch(&bs->work[(phase & 1) ^ 1], 0u);                    \
+    if (t.tid == 0) s_next[1 + t.half] = (int)atomicAdd(ctr, 1u);            \
+    gsync(t);                                                                \
+    int vb = s_next[1 + t.half];                                             \
+    while (vb < (N)) {                                                       \
+      gsync(t);                                                              \
+      int nxt = 0;                                                           \
+      if (t.tid == 0) nxt = (int)atomicAdd(ctr, 1u);                         \
+      if (!SKIP((TAB)[vb].x)) {                                              \
+        BODY;                                                                \
+      }                                                                      \
+      if (t.tid == 0) s_next[1 + t.half] = nxt;                              \
+      gsync(t);                                                              \
+      vb = s_next[1 + t.half];                                               \
+    }                                                                        \
+    ++phase;                                                                 \
+  }                                                                          \
   if (!grid_barrier(bs, a.limit)) return;
 // the stop tests: every member, then the state bits are refreshed
 #define FINISH_PHASE(BODY)                                       \

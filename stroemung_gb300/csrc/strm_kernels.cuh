@@ -154,7 +154,7 @@ cudaError_t build_batch(const std::vector<BatchMember> &mem, int sched, int m, B
 void free_batch(BatchPlan *bp);
 // Offsets in bytes of BatchState::overrun and ::timeout (the host reads them
 // after steps).
-constexpr size_t kBatchOverrunOffset = 10 * sizeof(unsigned int);
-constexpr size_t kBatchTimeoutOffset = 11 * sizeof(unsigned int);
+constexpr size_t kBatchOverrunOffset = 12 * sizeof(unsigned int);
+constexpr size_t kBatchTimeoutOffset = 13 * sizeof(unsigned int);
 
 }  // namespace strm
