@@ -139,25 +139,31 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def oracle_sim(grid):
+def oracle_sim(grid, red_black: bool = False, threads: int = 1):
     """The oracle (the reference's algorithm restated in C: lexicographic SOR
     in its x-major order, FP64, one thread) on `grid` with the workload's
-    parameters."""
+    parameters; red_black / threads select the oracle's red-black order with
+    its sweeps and norm on several threads (a multi-core CPU for comparison,
+    not the reference's own code path)."""
     from oracle import oracle as orc
     orc.build()
     p = PARAMS
-    return orc.OracleSim(kind=grid["kind"], wall_uv=grid["wall_uv"], u=grid["u"], v=grid["v"],
-                         p=grid["p"], dx=p["cell_size"][0], dy=p["cell_size"][1],
-                         delt=p["delt"], gamma=p["gamma"], reynolds=p["reynolds"],
-                         eps=p["sor_absolute_epsilon"], omega=p["omega"],
-                         max_iterations=p["max_iterations"], tau=p["tau"])
+    o = orc.OracleSim(kind=grid["kind"], wall_uv=grid["wall_uv"], u=grid["u"], v=grid["v"],
+                      p=grid["p"], dx=p["cell_size"][0], dy=p["cell_size"][1],
+                      delt=p["delt"], gamma=p["gamma"], reynolds=p["reynolds"],
+                      eps=p["sor_absolute_epsilon"], omega=p["omega"],
+                      max_iterations=p["max_iterations"], tau=p["tau"],
+                      sor_order=orc.RED_BLACK if red_black else orc.LEXICOGRAPHIC)
+    if threads > 1:
+        o.set_threads(threads)
+    return o
 
 
-def cpu_phases(grid, ticks: int, cap: int):
+def cpu_phases(grid, ticks: int, cap: int, red_black: bool = False, threads: int = 1):
     """Times `ticks` oracle ticks of the full workload with the solve capped
     at `cap` iterations: mean seconds before the solve, per solve iteration
     and after it, and the wall time."""
-    o = oracle_sim(grid)
+    o = oracle_sim(grid, red_black, threads)
     pre, it_s, post = [], [], []
     t0 = time.perf_counter()
     for _ in range(ticks):
@@ -234,6 +240,22 @@ def run_reference(args):
                         f"{k} iterations); the model is the sampled steps' pre-solve + "
                         "iterations x per-iteration + post-solve time for the same iteration "
                         "counts"}
+    # beside it, labelled: the same algorithm on every host core (the
+    # oracle's red-black order, its sweeps and norm threaded; the rest of
+    # the tick serial) — what a multi-core CPU does, not the reference's code
+    parallel = None
+    nthreads = os.cpu_count() or 1
+    if args.ref_parallel and nthreads > 1:
+        ph = [cpu_phases(grid, 1, args.ref_cap, red_black=True, threads=nthreads)
+              for _ in range(2)]
+        pt = (statistics.mean(x[0] for x in ph) + k * statistics.mean(x[1] for x in ph) +
+              statistics.mean(x[2] for x in ph))
+        parallel = {"value": CELLS / pt, "unit": "cell-updates/s", "ms_per_step": pt * 1e3,
+                    "threads": nthreads,
+                    "sample": f"2 oracle ticks, red-black order, the SOR sweeps and the norm on "
+                              f"{nthreads} threads (the rest of the tick on one), solve capped "
+                              f"at {args.ref_cap} iterations; step time = pre-solve + {k} x "
+                              f"per-iteration + post-solve"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -248,6 +270,8 @@ def run_reference(args):
     }
     if full is not None:
         line["full_step"] = full
+    if parallel is not None:
+        line["cpu_all_cores_red_black"] = parallel
     print(json.dumps(line))
 
 
@@ -1065,6 +1089,9 @@ def main():
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-cap", type=int, default=10)
+    ap.add_argument("--ref-parallel", type=int, default=1,
+                    help="reference arm: also time the red-black order on every host core "
+                         "(reported beside the single-core value)")
     ap.add_argument("--ref-full-steps", type=int, default=1,
                     help="reference arm: uncapped oracle ticks after the first, timed whole "
                          "beside the samples")

@@ -96,6 +96,7 @@ def lib():
         L.orc_calculate_norm_squared.argtypes = [ctypes.c_void_p]
         L.orc_solve_sor.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), _dp]
         L.orc_tick_timed.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _dp]
+        L.orc_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_render.argtypes = [ctypes.c_void_p, ctypes.c_int, _u8p]
         _lib = L
     return _lib
@@ -266,3 +267,8 @@ class OracleSim:
 
     def adapt_dt(self):
         lib().orc_adapt_dt(self._h)
+
+    def set_threads(self, n: int):
+        """Threads of the red-black sweeps and the norm (timing only; 1 runs
+        the serial loops)."""
+        lib().orc_set_threads(self._h, int(n))

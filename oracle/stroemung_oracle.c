@@ -213,6 +213,7 @@ struct orc_sim {
     restore_t *restore;    /* u_v_restore, src/grid/mod.rs:68 */
     int64_t nrestore;
     double pressure_range[2], speed_range[2];
+    int threads;           /* > 1: red-black sweeps and norm on that many threads */
 };
 
 #define AT(a, x, y) (a)[(size_t)(x) * ny + (y)]
@@ -300,6 +301,18 @@ double orc_calculate_norm_squared(const orc_sim *s) {
     const double dx = s->prm.dx, dy = s->prm.dy;
     const double *p = s->p;
     double acc = 0.0;
+#ifdef _OPENMP
+    if (s->threads > 1) {
+        /* timing only: the threads' partial sums are added in another order */
+#pragma omp parallel for schedule(static) num_threads(s->threads) reduction(+ : acc)
+        for (int x = 1; x < nx - 1; x++)
+            for (int y = 1; y < ny - 1; y++)
+                acc = acc + sq(residual_s(AT(p, x + 1, y), AT(p, x, y), AT(p, x - 1, y),
+                                          AT(p, x, y + 1), AT(p, x, y - 1), dx, dy,
+                                          AT(s->rhs, x, y)));
+        return acc / s->fluid_cells;
+    }
+#endif
     for (int x = 1; x < nx - 1; x++)
         for (int y = 1; y < ny - 1; y++)
             acc = acc + sq(residual_s(AT(p, x + 1, y), AT(p, x, y), AT(p, x - 1, y),
@@ -451,11 +464,17 @@ void orc_solve_sor(orc_sim *s, uint32_t *iters, double *ns_out) {
     for (uint32_t i = 0; i < s->prm.max_iterations; i++) {
         orc_copy_pressure_to_boundaries(s);
         if (s->prm.sor_order == ORC_SOR_RED_BLACK) {
-            for (int color = 0; color < 2; color++)
+            for (int color = 0; color < 2; color++) {
+#ifdef _OPENMP
+                /* the cells of one colour are independent: any thread count
+                   gives the same fields */
+#pragma omp parallel for schedule(static) num_threads(s->threads) if (s->threads > 1)
+#endif
                 for (int x = 1; x < nx - 1; x++)
                     for (int y = 1 + ((x + 1 + color) & 1); y < ny - 1; y += 2)
                         if (AT(s->kind, x, y) == ORC_FLUID)
                             sor_cell(s, x, y, one_minus_w, middle, delx2, dely2);
+            }
         } else {
             for (int x = 1; x < nx - 1; x++)
                 for (int y = 1; y < ny - 1; y++)
@@ -475,6 +494,12 @@ void orc_solve_sor(orc_sim *s, uint32_t *iters, double *ns_out) {
     *iters = s->prm.max_iterations;
     *ns_out = ns;
 }
+
+/* Threads of the red-black sweeps and the norm (1, the default, runs the
+ * reference's serial loops; more is for timing a multi-core CPU: the sweeps
+ * give the same fields, the norm's sum is added in another order).  No
+ * reference counterpart: the crate is single-threaded. */
+void orc_set_threads(orc_sim *s, int threads) { s->threads = threads > 1 ? threads : 1; }
 
 /* src/simulation.rs:287-322 */
 void orc_set_u_and_v(orc_sim *s) {
@@ -514,6 +539,7 @@ orc_sim *orc_create(const orc_params *prm, const uint8_t *kind, const double *wa
     const int nx = prm->nx, ny = prm->ny;
     size_t n = (size_t)nx * ny;
     orc_sim *s = (orc_sim *)calloc(1, sizeof(orc_sim));
+    if (s) s->threads = 1;
     s->prm = *prm;
     s->nx = nx;
     s->ny = ny;

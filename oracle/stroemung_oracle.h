@@ -126,6 +126,8 @@ void orc_calculate_speed_range(orc_sim *s);
 void orc_render(const orc_sim *s, int color_type, uint8_t *rgba);
 /* A tick with its phases timed, for the CPU baseline (see the .c file). */
 void orc_tick_timed(orc_sim *s, uint32_t max_iterations_cap, double *out4);
+/* Threads of the red-black sweeps and the norm (1 = serial, the default). */
+void orc_set_threads(orc_sim *s, int threads);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     monkeypatch.setattr(bench, "CELLS", 256 * 64)
     monkeypatch.delenv("RANK", raising=False)
     args = argparse.Namespace(gpus=1, steps=2, warmup=1, ref_cap=3, ref_full_steps=1,
-                              arith="fast")
+                              ref_parallel=1, arith="fast")
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(args)
@@ -46,6 +46,10 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     assert all(t["sor_iterations"] >= 1 for t in full["ticks"])
     # the extrapolation and the whole-tick measurement describe the same tick
     assert abs(full["model_error"]) < 0.5, full
+    import os
+    if (os.cpu_count() or 1) > 1:
+        par = d["cpu_all_cores_red_black"]
+        assert par["threads"] == os.cpu_count() and par["value"] > 0
 
 
 def test_reference_arm_prints_nothing_on_other_ranks(monkeypatch):
@@ -54,5 +58,6 @@ def test_reference_arm_prints_nothing_on_other_ranks(monkeypatch):
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(argparse.Namespace(gpus=2, steps=1, warmup=1, ref_cap=1,
-                                               ref_full_steps=1, arith="fast"))
+                                               ref_full_steps=1, ref_parallel=1,
+                                               arith="fast"))
     assert out.getvalue() == ""
