@@ -46,6 +46,10 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     assert all(t["sor_iterations"] >= 1 for t in full["ticks"])
     # the extrapolation and the whole-tick measurement describe the same tick
     assert abs(full["model_error"]) < 0.5, full
+    # the whole run: every tick, the model over the same iteration counts
+    assert full["whole_run_sweeps"] == sum(t["sor_iterations"] for t in full["ticks"])
+    assert abs(full["whole_run_s"] - sum(t["ms"] for t in full["ticks"]) / 1e3) < 1e-9
+    assert abs(full["whole_run_model_s"] - full["whole_run_s"]) < 0.5 * full["whole_run_s"]
     import os
     if (os.cpu_count() or 1) > 1:
         par = d["cpu_all_cores_red_black"]
