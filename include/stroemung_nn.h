@@ -27,6 +27,22 @@ enum {
  * returns STRM_NN_ERR_TIMEOUT once any such wait on this device has given
  * up (the flag stays set). */
 int strm_nn_set_sync(int sync);
+/* Staging of the forward convolution's operands (strm_nn_conv3x3): 1 (the
+ * default) stages them with TMA for layers whose input channels are a
+ * multiple of 32 and whose image width is a multiple of 128 (one tensor-map
+ * box per tap and channel slice); 0 gathers every layer's im2col rows with
+ * 16-byte copies.  The results agree within BF16-input / FP32-accumulation
+ * rounding (the K sums are split differently). */
+int strm_nn_set_conv_tma(int use);
+/* Launch shape of the TMA-staged forward: with persistent = 1, ctas_per_sm
+ * CTAs on every SM walk the layer's 128-pixel tiles; with 0 (the default),
+ * one CTA per tile, ctas_per_sm of them sharing an SM's shared memory.
+ * ctas_per_sm 0 (the default) takes as many as hold a two-stage ring each,
+ * at most 8 and what TMEM allows; each CTA has a ring of `stages` operand
+ * stages (0: as many as its share of the SM's shared memory holds; else
+ * 2..32).  Process-wide; results do not depend on it.  STRM_NN_ERR_INVALID
+ * for values out of range. */
+int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int persistent);
 int strm_nn_status(void *stream);
 
 /* d[m x n] (FP32, row-major) = a[m x k] * b[n x k]^T with a, b BF16 row-major

@@ -1,6 +1,8 @@
 // Dense contractions of the learned pressure warm start on the tcgen05 tensor
 // cores: BF16 operands staged in 128B-swizzled shared memory, FP32
 // accumulators in TMEM, one elected thread issuing tcgen05.mma.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -283,6 +285,203 @@ __global__ void __launch_bounds__(160)
 }
 
 // ------------------------------------------------------------------------
+// The same convolution with its operands staged by TMA (layers whose input
+// channels are a multiple of 32 and whose image width is a multiple of 128),
+// as a persistent warp-specialised kernel.  A tile is 128 consecutive
+// pixels of one image row; each CTA walks tiles blockIdx.x, + gridDim.x, ...
+// The K loop of a tile runs over taps and CH-channel slices of each tap
+// (CH = 64: 128-byte swizzled rows; CH = 32: 64-byte swizzled rows).
+//   producer (warp 4, one thread): per K chunk a 4-D TMA load of the input
+//     box {CH channels, 128 pixels at x0 + dx, row y + dy, image b} — the
+//     border falls outside the tensor and is filled with zeros — and a 2-D
+//     TMA load of the weight slice {CH, BN}, into the next stage of an
+//     S-stage ring, across tile boundaries;
+//   MMA issuer (warp 5, one thread): the chunk's CH/16 MMAs into one of
+//     NACC accumulators in TMEM, committed to the stage's "empty" barrier,
+//     and the tile's last commit to its accumulator's "full" barrier;
+//   epilogue (warps 0-3): reads a finished accumulator, adds the bias,
+//     applies the ReLU, stores BF16 (or FP32), and hands the accumulator
+//     back, so that it overlaps the next tile's loads and MMAs.
+// Every wait is bounded; a role whose wait runs out flags the CTA and stops,
+// the producer still waits (bounded) for the copies it issued, and the CTA
+// releases its TMEM.
+// ------------------------------------------------------------------------
+
+constexpr int kTmaMaxStages = 32;
+
+// The ring's stage count is a launch parameter (up to kTmaMaxStages): the
+// launcher fills the shared memory left by the CTAs it places on an SM.
+template <int BN, int CH>
+struct TmaConvPipe {
+  static constexpr int ROWB = CH * 2;              // bytes per operand row
+  static constexpr int A_BYTES = GM * ROWB;
+  static constexpr int B_BYTES = BN * ROWB;
+  static constexpr int STAGE = A_BYTES + B_BYTES;  // multiple of 1024
+  static constexpr int NACC = 2 * BN <= 256 ? 2 : 1;  // accumulators in TMEM
+  static constexpr int TM_COLS = NACC * BN < 32 ? 32 : NACC * BN;
+  static constexpr int TM_ONE = BN < 32 ? 32 : BN;  // one accumulator
+};
+
+template <int BN, int CH>
+__global__ void __launch_bounds__(192)
+    conv3x3_fwd_tma_kernel(const __grid_constant__ CUtensorMap tx,
+                           const __grid_constant__ CUtensorMap tw, const float *__restrict__ bias,
+                           __nv_bfloat16 *__restrict__ y, float *__restrict__ y32, ConvShape s,
+                           int relu, int S, unsigned int *err) {
+  using P = TmaConvPipe<BN, CH>;
+  constexpr int NACC = P::NACC;
+  static_assert(P::STAGE % 1024 == 0, "stage alignment");
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kTmaMaxStages], empty[kTmaMaxStages], tfull[NACC], tempty[NACC];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
+  const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *stage0 = smem_raw + pad;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = (int)((long long)s.batch * s.h * s.w / GM);
+  const int cpt = s.cin_p / CH;  // chunks per tap
+  const int nk = 9 * cpt;
+
+  // a CTA with one tile needs one accumulator
+  const uint32_t tm_cols = (int)gridDim.x >= ntiles ? (uint32_t)P::TM_ONE : (uint32_t)P::TM_COLS;
+  if (warp == 5) tmem_alloc(&tmem_slot, tm_cols);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < NACC; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 4);  // one arrival per epilogue warp
+    }
+    fail = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 4 && lane == 0) {
+    // ---- producer ----
+    // stage st of the ring, its use parity ph, and whether every stage has
+    // been used once (from then on a stage is refilled only after the MMAs
+    // that read it have completed)
+    bool ok = true, wrapped = false;
+    int st = 0;
+    uint32_t ph = 0;
+    int issued = 0;  // chunks issued so far (all tiles)
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const long long q0 = (long long)t * GM;
+      const int x0 = (int)(q0 % s.w);
+      const long long row = q0 / s.w;
+      const int yy = (int)(row % s.h), bb = (int)(row / s.h);
+      for (int kc = 0; kc < nk; ++kc) {
+        if (wrapped) {
+          ok = mbar_wait_bounded(&empty[st], ph ^ 1u, kWaitLimit);
+          if (!ok) break;
+        }
+        const int tap = kc / cpt, j = kc - tap * cpt;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        uint8_t *sA = stage0 + st * P::STAGE;
+        mbar_arrive_expect_tx(&full[st], (uint32_t)P::STAGE);
+        tma_load_4d(smem_u32(sA), &tx, j * CH, x0 + dx, yy + dy, bb, &full[st]);
+        tma_load_2d(smem_u32(sA + P::A_BYTES), &tw, tap * s.cin_p + j * CH, 0, &full[st]);
+        ++issued;
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+          wrapped = true;
+        }
+      }
+    }
+    if (!ok) atomicExch(&fail, 1);
+    // every copy issued has landed before the CTA may leave (bounded): the
+    // last min(issued, S) chunks, one per stage
+    for (int g = issued - S < 0 ? 0 : issued - S; g < issued; ++g)
+      if (!mbar_wait_bounded(&full[g % S], (uint32_t)(g / S) & 1u, kWaitLimit))
+        atomicExch(&fail, 1);
+  } else if (warp == 5 && lane == 0) {
+    // ---- MMA issuer ----
+    const uint32_t idesc = idesc_bf16_f32(GM, BN);
+    bool ok = true;
+    int st = 0;
+    uint32_t ph = 0;
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+      const int acc = it % NACC;
+      if (it >= NACC) {
+        ok = mbar_wait_bounded(&tempty[acc], (uint32_t)((it / NACC) - 1) & 1u, kWaitLimit);
+        if (!ok) break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t)(acc * BN);
+      for (int kc = 0; kc < nk; ++kc) {
+        ok = mbar_wait_bounded(&full[st], ph, kWaitLimit);
+        if (!ok) break;
+        tc_fence_after();
+        uint8_t *sA = stage0 + st * P::STAGE;
+        const uint64_t da = CH == 64 ? desc_kmajor_sw128(smem_u32(sA))
+                                     : desc_kmajor_sw64(smem_u32(sA));
+        const uint64_t db = CH == 64 ? desc_kmajor_sw128(smem_u32(sA + P::A_BYTES))
+                                     : desc_kmajor_sw64(smem_u32(sA + P::A_BYTES));
+#pragma unroll
+        for (int kk = 0; kk < CH / 16; ++kk)
+          umma_bf16(d, da + 2 * kk, db + 2 * kk, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+        umma_commit(&empty[st]);
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+        }
+      }
+      if (ok) umma_commit(&tfull[acc]);
+    }
+    if (!ok) atomicExch(&fail, 1);
+  } else if (warp < 4) {
+    // ---- epilogue ----
+    int it = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+      const int acc = it % NACC;
+      ok = mbar_wait_bounded(&tfull[acc], (uint32_t)(it / NACC) & 1u, kWaitLimit);
+      if (!ok) break;
+      tc_fence_after();
+      const long long q = (long long)t * GM + warp * 32 + lane;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * BN + c), v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          v[i] += bias ? bias[c + i] : 0.0f;
+          if (relu) v[i] = fmaxf(v[i], 0.0f);
+        }
+        if (y32) {
+          float *dst = y32 + q * s.cs_out + c;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dst[i] = v[i];
+        } else {
+          __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
+          uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
+          dst[0] = reinterpret_cast<const uint4 *>(o)[0];
+          dst[1] = reinterpret_cast<const uint4 *>(o)[1];
+        }
+      }
+      // the accumulator may be overwritten once all four warps have read it
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);
+    }
+    if (!ok) atomicExch(&fail, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && fail) atomicExch(err, 1u);
+  if (warp == 5) tmem_dealloc(tmem, tm_cols);
+}
+
+// ------------------------------------------------------------------------
 // Weight gradient of the 3x3 convolution: dW[co][k] += sum over pixels q of
 // g[q][co] * im2col(x)[q][k], with g = dY masked by the ReLU (y > 0) when y
 // is given.  GEMM with M = K rows (128 per CTA), N = Cout, reduction over
@@ -479,6 +678,150 @@ int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, cons
   return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
 }
 
+// 1: layers that qualify use the TMA-fed forward (the default); 0: every
+// layer uses the gathering kernel
+std::atomic<int> g_conv_tma{1};
+// Launch shape of the TMA-fed convolution: CTAs per SM (0: as many as hold a
+// two-stage ring each), ring stages (0: the deepest that fits), and
+// persistent CTAs walking the tiles or one CTA per tile (the default:
+// measured faster at 4096 x 1024 for 32- and 64-channel tiles, where many
+// small independent pipelines per SM hide the TMA latency better than one
+// or two persistent ones).
+std::atomic<int> g_tma_ctas{0}, g_tma_stages{0}, g_tma_persist{0};
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); NULL when the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, []() {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// The TMA path takes layers whose input channels come in slices of 32 or 64
+// and whose image rows hold whole 128-pixel tiles.
+bool tma_conv_applies(int cin_p, int width, int cs_in, const void *x) {
+  return g_conv_tma.load() && cin_p % 32 == 0 && width % GM == 0 && cs_in % 8 == 0 &&
+         (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
+}
+
+template <int BN, int CH>
+int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
+                    const float *bias, void *y, float *y32, int cs_out, int batch, int h,
+                    int width, int relu, cudaStream_t s, unsigned int *err) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return -1;
+  CUtensorMap tx{}, tw{};
+  const CUtensorMapSwizzle sw = CH == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  // input: {channels (cin_p of a pixel's cs_in), x, y, image}, 2-byte elements
+  const cuuint64_t xdim[4] = {(cuuint64_t)cin_p, (cuuint64_t)width, (cuuint64_t)h,
+                              (cuuint64_t)batch};
+  const cuuint64_t xstr[3] = {(cuuint64_t)cs_in * 2, (cuuint64_t)cs_in * 2 * width,
+                              (cuuint64_t)cs_in * 2 * width * h};
+  const cuuint32_t xbox[4] = {(cuuint32_t)CH, (cuuint32_t)GM, 1, 1};
+  const cuuint32_t one[4] = {1, 1, 1, 1};
+  if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(x), xdim, xstr, xbox, one,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return -1;
+  // weights: {K, output channels}
+  const cuuint64_t wdim[2] = {(cuuint64_t)kp, (cuuint64_t)BN};
+  const cuuint64_t wstr[1] = {(cuuint64_t)kp * 2};
+  const cuuint32_t wbox[2] = {(cuuint32_t)CH, (cuuint32_t)BN};
+  if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(w), wdim, wstr, wbox, one,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return -1;
+  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
+  using P = TmaConvPipe<BN, CH>;
+  // device limits, once per instantiation: shared memory per SM, per CTA
+  // (opt-in) and reserved per CTA, the kernel's static shared memory
+  static int nsm = 0, smem_sm = 0, smem_blk = 0, reserved = 0, stat = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+            cudaSuccess ||
+        cudaFuncGetAttributes(&fa, conv3x3_fwd_tma_kernel<BN, CH>) != cudaSuccess)
+      return STRM_NN_ERR_CUDA;
+    stat = (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_blk - stat) != cudaSuccess ||
+        cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return STRM_NN_ERR_CUDA;
+  }
+  // CTAs per SM: the tuned count (TMEM holds 512 columns per SM), and the
+  // ring that fills each CTA's share of the SM's shared memory
+  const bool persist = g_tma_persist.load() != 0;
+  const int tm_cap = 512 / (persist ? P::TM_COLS : P::TM_ONE);
+  int ctas = g_tma_ctas.load();
+  if (ctas < 1) ctas = smem_sm / (2 * P::STAGE + 1024 + reserved + stat);
+  if (ctas > 8) ctas = 8;
+  if (ctas > tm_cap) ctas = tm_cap;
+  if (ctas < 1) ctas = 1;
+  int stages = (smem_sm / ctas - reserved - stat - 1024) / P::STAGE;
+  const int cap_blk = (smem_blk - stat - 1024) / P::STAGE;
+  if (stages > cap_blk) stages = cap_blk;
+  if (stages > kTmaMaxStages) stages = kTmaMaxStages;
+  const int tuned = g_tma_stages.load();
+  if (tuned > 0 && tuned < stages) stages = tuned;
+  if (stages < 2) return -1;
+  const int dyn = stages * P::STAGE + 1024;
+  static int fit_dyn = -1, fit = 0;  // CTAs per SM at the last ring size asked
+  if (dyn != fit_dyn) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH>, 192,
+                                                      dyn) != cudaSuccess ||
+        fit < 1)
+      return STRM_NN_ERR_CUDA;
+    fit_dyn = dyn;
+  }
+  if (fit < ctas) ctas = fit;
+  const long long npix = (long long)batch * h * width;
+  if (npix >= (1LL << 31)) return STRM_NN_ERR_INVALID;
+  const long long ntiles = npix / GM;
+  // persistent: ctas per SM on every SM, at most one per tile; otherwise
+  // one CTA per tile (ctas then only sizes each CTA's ring)
+  const long long want = persist ? (long long)ctas * nsm : ntiles;
+  const unsigned int grid = (unsigned int)(ntiles < want ? ntiles : want);
+  conv3x3_fwd_tma_kernel<BN, CH><<<grid, 192, dyn, s>>>(
+      tx, tw, bias, (__nv_bfloat16 *)y, y32, sh, relu, stages, err);
+  return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
+}
+
+// The TMA-fed forward when it applies (and its tensor maps encode), else the
+// gathering kernel.
+template <int BN>
+int launch_conv_any(const void *x, int cs_in, int cin_p, const void *w, int kp, const float *bias,
+                    void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
+                    cudaStream_t s, unsigned int *err) {
+  if (tma_conv_applies(cin_p, width, cs_in, x)) {
+    const int rc = cin_p % 64 == 0
+                       ? launch_conv_tma<BN, 64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
+                                                 batch, h, width, relu, s, err)
+                       : launch_conv_tma<BN, 32>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
+                                                 batch, h, width, relu, s, err);
+    if (rc >= 0) return rc;
+  }
+  return launch_conv<BN>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s,
+                         err);
+}
+
 template <int BN>
 int launch_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy, int cs_dy,
                  const void *yact, int cs_out, float *dw, int batch, int h, int width,
@@ -519,6 +862,21 @@ bool conv_args_ok(int cs_in, int cin_p, int kp, int cs_out, int cout) {
 
 }  // namespace
 
+extern "C" int strm_nn_set_conv_tma(int use) {
+  g_conv_tma.store(use ? 1 : 0);
+  return STRM_NN_OK;
+}
+
+extern "C" int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int persistent) {
+  if (ctas_per_sm < 0 || ctas_per_sm > 8 || stages < 0 || stages == 1 ||
+      stages > kTmaMaxStages || persistent < 0 || persistent > 1)
+    return STRM_NN_ERR_INVALID;
+  g_tma_ctas.store(ctas_per_sm);
+  g_tma_stages.store(stages);
+  g_tma_persist.store(persistent);
+  return STRM_NN_OK;
+}
+
 extern "C" int strm_nn_set_sync(int sync) {
   g_sync.store(sync ? 1 : 0);
   return STRM_NN_OK;
@@ -541,11 +899,11 @@ extern "C" int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *
   cudaStream_t s = (cudaStream_t)stream;
   int rc;
   switch (cout) {
-    case 16: rc = launch_conv<16>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
-    case 32: rc = launch_conv<32>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
-    case 64: rc = launch_conv<64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
-    case 128: rc = launch_conv<128>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
-    default: rc = launch_conv<256>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 16: rc = launch_conv_any<16>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 32: rc = launch_conv_any<32>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 64: rc = launch_conv_any<64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    case 128: rc = launch_conv_any<128>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+    default: rc = launch_conv_any<256>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
   }
   return finish(err, s, rc);
 }

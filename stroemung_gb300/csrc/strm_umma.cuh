@@ -34,6 +34,20 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t saddr) {
   return d;
 }
 
+// The same descriptor for K-major tiles in the 64-byte swizzle layout: rows
+// of 32 BF16 values (64 bytes), 8-row atoms of 512 bytes (the stride byte
+// offset), swizzle mode 4 in bits [61,64); tiles start on a 512-byte
+// boundary, and the second K = 16 slice of a row is 32 bytes further.
+__device__ __forceinline__ uint64_t desc_kmajor_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)((512u >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)4u << 61;
+  return d;
+}
+
 // Instruction descriptor for kind::f16: D F32 (bits 4-5 = 1), A and B BF16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in
 // bits [17,23), M >> 4 in bits [24,29).
@@ -141,6 +155,35 @@ __device__ __forceinline__ void cp_async_commit() {
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// mbarrier arrival that also announces `bytes` of asynchronous copies the
+// phase waits for (the producer of a TMA-fed stage).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Tiled TMA loads of a box into shared memory, completing on `mbar` (tmap:
+// the generic address of a CUtensorMap kernel parameter).  The innermost
+// coordinate times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *tmap, int c0, int c1,
+                                            uint64_t *mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(smem_u32(mbar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void *tmap, int c0, int c1,
+                                            int c2, int c3, uint64_t *mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+      "r"(smem_u32(mbar))
+      : "memory");
 }
 
 // Byte offset of 16-byte chunk `j` of row `r` in a 128B-swizzled K-major tile.

@@ -52,12 +52,19 @@ def _nhwc(x, cin_p):
     return out.contiguous()
 
 
-# the odd sizes leave partial pixel tiles and image rows
+# the odd sizes leave partial pixel tiles and image rows (the gathering
+# kernel); widths that are multiples of 128 with inputs in slices of 32 or 64
+# channels take the TMA-staged kernel (64-byte rows for 32-channel slices,
+# 128-byte rows for 64)
 @pytest.mark.parametrize("cin,cout,h,w,relu", [(3, 32, 16, 128, 1), (32, 64, 8, 64, 1),
                                                 (96, 32, 16, 32, 0), (128, 256, 4, 64, 1),
                                                 (64, 16, 8, 16, 1), (32, 32, 7, 200, 1),
                                                 (64, 64, 5, 300, 0), (8, 32, 3, 130, 1),
-                                                (48, 32, 9, 140, 1), (96, 32, 4, 256, 1)])
+                                                (48, 32, 9, 140, 1), (96, 32, 4, 256, 1),
+                                                (32, 32, 5, 128, 1), (64, 64, 3, 256, 0),
+                                                (128, 128, 2, 128, 1), (256, 256, 2, 128, 1),
+                                                (192, 64, 2, 128, 1), (64, 16, 3, 128, 1),
+                                                (32, 256, 3, 128, 0), (384, 128, 1, 128, 0)])
 def test_conv3x3_forward_matches_torch(cin, cout, h, w, relu):
     import torch
     import torch.nn.functional as F
@@ -83,7 +90,8 @@ def test_conv3x3_forward_matches_torch(cin, cout, h, w, relu):
     assert err <= 1e-2 * max(1.0, ref.abs().max().item()), err
 
 
-@pytest.mark.parametrize("cin,cout,h,w", [(32, 32, 16, 64), (64, 128, 8, 32), (16, 16, 16, 16)])
+@pytest.mark.parametrize("cin,cout,h,w", [(32, 32, 16, 64), (64, 128, 8, 32), (16, 16, 16, 16),
+                                          (32, 32, 8, 128), (64, 32, 4, 128)])
 def test_conv3x3_weight_and_data_gradients_match_torch(cin, cout, h, w):
     import torch
     import torch.nn.functional as F
@@ -156,3 +164,78 @@ def test_deferred_waits_give_the_same_result():
         L.strm_nn_set_sync(1)
     assert L.strm_nn_status(None) == 0
     assert torch.equal(y1, y2)
+
+
+@pytest.mark.parametrize("use_slice", [False, True], ids=["whole", "channel_slice"])
+def test_tma_staged_forward_matches_the_gathering_kernel(use_slice):
+    """The same convolution with TMA-staged operands and with gathered ones
+    (strm_nn_set_conv_tma 1 / 0): both within BF16 rounding of torch and of
+    each other; with use_slice the input is channels 32..95 of a 96-channel
+    buffer (the decoder's concatenations read such slices)."""
+    import torch
+    import torch.nn.functional as F
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(11)
+    b, cin, cout, h, w = 2, 64, 64, 6, 256
+    x = _bf(torch.randn(b, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.2)
+    bias = torch.randn(cout, device="cuda", generator=g)
+    wp, kp = _pack_weights(wt, cin)
+    if use_slice:
+        buf = torch.zeros(b, h, w, 96, dtype=torch.bfloat16, device="cuda")
+        buf[..., 32:] = x.permute(0, 2, 3, 1)
+        xptr, cs_in = buf.data_ptr() + 32 * 2, 96
+    else:
+        xn = _nhwc(x, cin)
+        xptr, cs_in = xn.data_ptr(), cin
+    outs = []
+    try:
+        for use in (1, 0):
+            assert L.strm_nn_set_conv_tma(use) == 0
+            y = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+            torch.cuda.synchronize()
+            assert L.strm_nn_conv3x3(xptr, cs_in, cin, wp.data_ptr(), kp, bias.data_ptr(),
+                                     y.data_ptr(), None, cout, cout, b, h, w, 1, None) == 0
+            outs.append(y.float())
+    finally:
+        L.strm_nn_set_conv_tma(1)
+    ref = F.conv2d(x.float(), wt.float(), bias, padding=1).clamp_min(0).permute(0, 2, 3, 1)
+    scale = max(1.0, ref.abs().max().item())
+    for y in outs:
+        assert (y - ref).abs().max().item() <= 1e-2 * scale
+    assert (outs[0] - outs[1]).abs().max().item() <= 1e-2 * scale
+
+
+@pytest.mark.parametrize("cin,cout", [(32, 32), (64, 64), (96, 32), (128, 256)])
+def test_tma_forward_is_independent_of_its_launch_shape(cin, cout):
+    """The TMA-fed forward gives the same bits for any launch shape —
+    persistent or one CTA per tile, any number of CTAs per SM and ring depth
+    (each tile's K loop runs in one fixed order) — including rings shallower
+    than a tile's K chunks and more CTAs per SM than TMEM holds."""
+    import torch
+    import torch.nn.functional as F
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    b, h, w = 1, 7, 384
+    x = _bf(torch.randn(b, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.1)
+    bias = torch.randn(cout, device="cuda", generator=g)
+    wp, kp = _pack_weights(wt, cin)
+    xn = _nhwc(x, cin)
+    outs = []
+    try:
+        for ctas, stages, persist in ((0, 0, 0), (0, 0, 1), (1, 2, 1), (1, 32, 1), (2, 3, 1),
+                                      (4, 0, 1), (8, 5, 1), (3, 6, 0), (1, 2, 0), (8, 2, 0)):
+            assert L.strm_nn_tune_conv_tma(ctas, stages, persist) == 0
+            y = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+            assert L.strm_nn_conv3x3(xn.data_ptr(), cin, cin, wp.data_ptr(), kp,
+                                     bias.data_ptr(), y.data_ptr(), None, cout, cout, b, h, w,
+                                     1, None) == 0
+            outs.append(y)
+    finally:
+        L.strm_nn_tune_conv_tma(0, 0, 0)
+    for y in outs[1:]:
+        assert torch.equal(y, outs[0])
+    ref = F.conv2d(x.float(), wt.float(), bias, padding=1).clamp_min(0).permute(0, 2, 3, 1)
+    scale = max(1.0, ref.abs().max().item())
+    assert (outs[0].float() - ref).abs().max().item() <= 1e-2 * scale
