@@ -34,15 +34,20 @@ int strm_nn_set_sync(int sync);
  * 16-byte copies.  The results agree within BF16-input / FP32-accumulation
  * rounding (the K sums are split differently). */
 int strm_nn_set_conv_tma(int use);
-/* Launch shape of the TMA-staged forward: with persistent = 1, ctas_per_sm
- * CTAs on every SM walk the layer's 128-pixel tiles; with 0 (the default),
- * one CTA per tile, ctas_per_sm of them sharing an SM's shared memory.
- * ctas_per_sm 0 (the default) takes as many as hold a two-stage ring each,
- * at most 8 and what TMEM allows; each CTA has a ring of `stages` operand
- * stages (0: as many as its share of the SM's shared memory holds; else
- * 2..32).  Process-wide; results do not depend on it.  STRM_NN_ERR_INVALID
- * for values out of range. */
-int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int persistent);
+/* Launch shape of the TMA-staged forward: tiles_per_cta n >= 1 gives each
+ * CTA n of the layer's 128-pixel tiles, ctas_per_sm of them sharing an SM's
+ * shared memory; 0 (the default) takes four while the layer fills every
+ * CTA slot of the GPU that often, else two, else one.  ctas_per_sm 0 (the
+ * default) takes as many
+ * as hold a two-stage ring each, at most 8 and what TMEM allows; each CTA
+ * has a ring of `stages` operand stages (0: as many as its share of the
+ * SM's shared memory holds; else 2..32).  rows = 1 (the default) loads one
+ * 130-pixel box per kernel row and 32-channel slice and feeds the three
+ * taps of that row from it; 0 loads one 128-pixel box per tap (as 64-channel
+ * slices always do).  Process-wide; for a given `rows` results do not
+ * depend on it (the two `rows` modes add the K terms in different orders).
+ * STRM_NN_ERR_INVALID for values out of range (tiles_per_cta 0..64). */
+int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int tiles_per_cta, int rows);
 int strm_nn_status(void *stream);
 
 /* d[m x n] (FP32, row-major) = a[m x k] * b[n x k]^T with a, b BF16 row-major

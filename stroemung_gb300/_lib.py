@@ -129,7 +129,7 @@ SIGNATURES = {
     # include/stroemung_nn.h
     "strm_nn_set_sync": [_i],
     "strm_nn_set_conv_tma": [_i],
-    "strm_nn_tune_conv_tma": [_i, _i, _i],
+    "strm_nn_tune_conv_tma": [_i, _i, _i, _i],
     "strm_nn_status": [_vp],
     "strm_nn_gemm_bf16": [_vp, _vp, _fp, _i, _i, _i, _vp],
     "strm_nn_conv3x3": [_vp, _i, _i, _vp, _i, _fp, _vp, _fp, _i, _i, _i, _i, _i, _i, _vp],

@@ -311,26 +311,39 @@ constexpr int kTmaMaxStages = 32;
 
 // The ring's stage count is a launch parameter (up to kTmaMaxStages): the
 // launcher fills the shared memory left by the CTAs it places on an SM.
-template <int BN, int CH>
+// ROWS: a chunk is one kernel row dy and channel slice: the input box is the
+// tile's 128 pixels with one more on each side (130 operand rows), and the
+// three taps dx = -1, 0, +1 read it through descriptors that start 0, 1, 2
+// rows in (the swizzle pattern follows the shared-memory address bits, so a
+// start one 64- or 128-byte row into the box reads the rows as the copy
+// swizzled them), against three weight slices.  Otherwise a chunk is one
+// tap and slice (one 128-row box).  Row boxes move a third of the input
+// bytes; the launcher takes them for 32-channel slices only.
+template <int BN, int CH, bool ROWS>
 struct TmaConvPipe {
   static constexpr int ROWB = CH * 2;              // bytes per operand row
-  static constexpr int A_BYTES = GM * ROWB;
-  static constexpr int B_BYTES = BN * ROWB;
+  static constexpr int A_ROWS = ROWS ? GM + 2 : GM;
+  static constexpr int A_BYTES = (A_ROWS * ROWB + 1023) / 1024 * 1024;
+  static constexpr int TAPS = ROWS ? 3 : 1;        // taps per chunk
+  static constexpr int B_TAP = BN * ROWB;
+  static constexpr int B_BYTES = TAPS * B_TAP;
   static constexpr int STAGE = A_BYTES + B_BYTES;  // multiple of 1024
+  static constexpr int TX = A_ROWS * ROWB + B_BYTES;  // bytes the copies write
   static constexpr int NACC = 2 * BN <= 256 ? 2 : 1;  // accumulators in TMEM
   static constexpr int TM_COLS = NACC * BN < 32 ? 32 : NACC * BN;
   static constexpr int TM_ONE = BN < 32 ? 32 : BN;  // one accumulator
 };
 
-template <int BN, int CH>
+template <int BN, int CH, bool ROWS>
 __global__ void __launch_bounds__(192)
     conv3x3_fwd_tma_kernel(const __grid_constant__ CUtensorMap tx,
                            const __grid_constant__ CUtensorMap tw, const float *__restrict__ bias,
                            __nv_bfloat16 *__restrict__ y, float *__restrict__ y32, ConvShape s,
                            int relu, int S, unsigned int *err) {
-  using P = TmaConvPipe<BN, CH>;
+  using P = TmaConvPipe<BN, CH, ROWS>;
   constexpr int NACC = P::NACC;
   static_assert(P::STAGE % 1024 == 0, "stage alignment");
+  static_assert(P::B_TAP % (CH == 64 ? 1024 : 512) == 0, "weight slice alignment");
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[kTmaMaxStages], empty[kTmaMaxStages], tfull[NACC], tempty[NACC];
   __shared__ uint32_t tmem_slot;
@@ -340,7 +353,7 @@ __global__ void __launch_bounds__(192)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntiles = (int)((long long)s.batch * s.h * s.w / GM);
   const int cpt = s.cin_p / CH;  // chunks per tap
-  const int nk = 9 * cpt;
+  const int nk = (ROWS ? 3 : 9) * cpt;
 
   // a CTA with one tile needs one accumulator
   const uint32_t tm_cols = (int)gridDim.x >= ntiles ? (uint32_t)P::TM_ONE : (uint32_t)P::TM_COLS;
@@ -380,12 +393,20 @@ __global__ void __launch_bounds__(192)
           ok = mbar_wait_bounded(&empty[st], ph ^ 1u, kWaitLimit);
           if (!ok) break;
         }
-        const int tap = kc / cpt, j = kc - tap * cpt;
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
         uint8_t *sA = stage0 + st * P::STAGE;
-        mbar_arrive_expect_tx(&full[st], (uint32_t)P::STAGE);
-        tma_load_4d(smem_u32(sA), &tx, j * CH, x0 + dx, yy + dy, bb, &full[st]);
-        tma_load_2d(smem_u32(sA + P::A_BYTES), &tw, tap * s.cin_p + j * CH, 0, &full[st]);
+        mbar_arrive_expect_tx(&full[st], (uint32_t)P::TX);
+        if (ROWS) {
+          const int ky = kc / cpt, j = kc - ky * cpt;
+          tma_load_4d(smem_u32(sA), &tx, j * CH, x0 - 1, yy + ky - 1, bb, &full[st]);
+          for (int kx = 0; kx < 3; ++kx)
+            tma_load_2d(smem_u32(sA + P::A_BYTES + kx * P::B_TAP), &tw,
+                        (ky * 3 + kx) * s.cin_p + j * CH, 0, &full[st]);
+        } else {
+          const int tap = kc / cpt, j = kc - tap * cpt;
+          const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+          tma_load_4d(smem_u32(sA), &tx, j * CH, x0 + dx, yy + dy, bb, &full[st]);
+          tma_load_2d(smem_u32(sA + P::A_BYTES), &tw, tap * s.cin_p + j * CH, 0, &full[st]);
+        }
         ++issued;
         if (++st == S) {
           st = 0;
@@ -420,13 +441,18 @@ __global__ void __launch_bounds__(192)
         if (!ok) break;
         tc_fence_after();
         uint8_t *sA = stage0 + st * P::STAGE;
-        const uint64_t da = CH == 64 ? desc_kmajor_sw128(smem_u32(sA))
-                                     : desc_kmajor_sw64(smem_u32(sA));
-        const uint64_t db = CH == 64 ? desc_kmajor_sw128(smem_u32(sA + P::A_BYTES))
-                                     : desc_kmajor_sw64(smem_u32(sA + P::A_BYTES));
 #pragma unroll
-        for (int kk = 0; kk < CH / 16; ++kk)
-          umma_bf16(d, da + 2 * kk, db + 2 * kk, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+        for (int kx = 0; kx < P::TAPS; ++kx) {
+          // tap dx = kx - 1 of a row box: the 128 rows from row kx
+          const uint32_t a = smem_u32(sA + kx * P::ROWB);
+          const uint32_t b = smem_u32(sA + P::A_BYTES + kx * P::B_TAP);
+          const uint64_t da = CH == 64 ? desc_kmajor_sw128(a) : desc_kmajor_sw64(a);
+          const uint64_t db = CH == 64 ? desc_kmajor_sw128(b) : desc_kmajor_sw64(b);
+#pragma unroll
+          for (int kk = 0; kk < CH / 16; ++kk)
+            umma_bf16(d, da + 2 * kk, db + 2 * kk, idesc,
+                      (kc > 0 || kx > 0 || kk > 0) ? 1u : 0u);
+        }
         umma_commit(&empty[st]);
         if (++st == S) {
           st = 0;
@@ -682,12 +708,13 @@ int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, cons
 // layer uses the gathering kernel
 std::atomic<int> g_conv_tma{1};
 // Launch shape of the TMA-fed convolution: CTAs per SM (0: as many as hold a
-// two-stage ring each), ring stages (0: the deepest that fits), and
-// persistent CTAs walking the tiles or one CTA per tile (the default:
-// measured faster at 4096 x 1024 for 32- and 64-channel tiles, where many
-// small independent pipelines per SM hide the TMA latency better than one
-// or two persistent ones).
-std::atomic<int> g_tma_ctas{0}, g_tma_stages{0}, g_tma_persist{0};
+// two-stage ring each), ring stages (0: the deepest that fits), tiles per
+// CTA (0: four while the layer still fills every CTA slot of the GPU once,
+// else two, else one — measured at 4096 x 1024: many short CTAs per SM hide
+// the TMA latency, and a few tiles per CTA spread its set-up; CTAs walking
+// all tiles persistently were slower on every layer), and row boxes for
+// 32-channel slices.
+std::atomic<int> g_tma_ctas{0}, g_tma_stages{0}, g_tma_tiles{0}, g_tma_rows{1};
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against the driver library); NULL when the driver does not provide it.
@@ -712,10 +739,11 @@ bool tma_conv_applies(int cin_p, int width, int cs_in, const void *x) {
          (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
 }
 
-template <int BN, int CH>
+template <int BN, int CH, bool ROWS>
 int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
                     const float *bias, void *y, float *y32, int cs_out, int batch, int h,
                     int width, int relu, cudaStream_t s, unsigned int *err) {
+  using P = TmaConvPipe<BN, CH, ROWS>;
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return -1;
   CUtensorMap tx{}, tw{};
@@ -725,7 +753,7 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
                               (cuuint64_t)batch};
   const cuuint64_t xstr[3] = {(cuuint64_t)cs_in * 2, (cuuint64_t)cs_in * 2 * width,
                               (cuuint64_t)cs_in * 2 * width * h};
-  const cuuint32_t xbox[4] = {(cuuint32_t)CH, (cuuint32_t)GM, 1, 1};
+  const cuuint32_t xbox[4] = {(cuuint32_t)CH, (cuuint32_t)P::A_ROWS, 1, 1};
   const cuuint32_t one[4] = {1, 1, 1, 1};
   if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(x), xdim, xstr, xbox, one,
           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -740,7 +768,6 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return -1;
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
-  using P = TmaConvPipe<BN, CH>;
   // device limits, once per instantiation: shared memory per SM, per CTA
   // (opt-in) and reserved per CTA, the kernel's static shared memory
   static int nsm = 0, smem_sm = 0, smem_blk = 0, reserved = 0, stat = 0;
@@ -754,13 +781,13 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
             cudaSuccess ||
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
             cudaSuccess ||
-        cudaFuncGetAttributes(&fa, conv3x3_fwd_tma_kernel<BN, CH>) != cudaSuccess)
+        cudaFuncGetAttributes(&fa, conv3x3_fwd_tma_kernel<BN, CH, ROWS>) != cudaSuccess)
       return STRM_NN_ERR_CUDA;
     stat = (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH>,
+    if (cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem_blk - stat) != cudaSuccess ||
-        cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH>,
+        cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
                              cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -768,12 +795,15 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   }
   // CTAs per SM: the tuned count (TMEM holds 512 columns per SM), and the
   // ring that fills each CTA's share of the SM's shared memory
-  const bool persist = g_tma_persist.load() != 0;
-  const int tm_cap = 512 / (persist ? P::TM_COLS : P::TM_ONE);
+  const int tiles = g_tma_tiles.load();  // tiles per CTA, 0: by the layer's size
+  const int tm_cap = 512 / (tiles != 1 ? P::TM_COLS : P::TM_ONE);
   int ctas = g_tma_ctas.load();
   if (ctas < 1) ctas = smem_sm / (2 * P::STAGE + 1024 + reserved + stat);
   if (ctas > 8) ctas = 8;
   if (ctas > tm_cap) ctas = tm_cap;
+  // fewer CTAs until each holds a two-stage ring (the mode a layer takes
+  // does not depend on the launch shape asked for)
+  while (ctas > 1 && (smem_sm / ctas - reserved - stat - 1024) / P::STAGE < 2) --ctas;
   if (ctas < 1) ctas = 1;
   int stages = (smem_sm / ctas - reserved - stat - 1024) / P::STAGE;
   const int cap_blk = (smem_blk - stat - 1024) / P::STAGE;
@@ -785,7 +815,7 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   const int dyn = stages * P::STAGE + 1024;
   static int fit_dyn = -1, fit = 0;  // CTAs per SM at the last ring size asked
   if (dyn != fit_dyn) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH>, 192,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH, ROWS>, 192,
                                                       dyn) != cudaSuccess ||
         fit < 1)
       return STRM_NN_ERR_CUDA;
@@ -795,11 +825,11 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   const long long npix = (long long)batch * h * width;
   if (npix >= (1LL << 31)) return STRM_NN_ERR_INVALID;
   const long long ntiles = npix / GM;
-  // persistent: ctas per SM on every SM, at most one per tile; otherwise
-  // one CTA per tile (ctas then only sizes each CTA's ring)
-  const long long want = persist ? (long long)ctas * nsm : ntiles;
-  const unsigned int grid = (unsigned int)(ntiles < want ? ntiles : want);
-  conv3x3_fwd_tma_kernel<BN, CH><<<grid, 192, dyn, s>>>(
+  // `per` tiles per CTA, CTA b taking tiles b, b + grid, ...
+  const long long slots = (long long)ctas * nsm;
+  const int per = tiles > 0 ? tiles : ntiles >= 4 * slots ? 4 : ntiles >= 2 * slots ? 2 : 1;
+  const unsigned int grid = (unsigned int)((ntiles + per - 1) / per);
+  conv3x3_fwd_tma_kernel<BN, CH, ROWS><<<grid, 192, dyn, s>>>(
       tx, tw, bias, (__nv_bfloat16 *)y, y32, sh, relu, stages, err);
   return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
 }
@@ -811,11 +841,19 @@ int launch_conv_any(const void *x, int cs_in, int cin_p, const void *w, int kp, 
                     void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
                     cudaStream_t s, unsigned int *err) {
   if (tma_conv_applies(cin_p, width, cs_in, x)) {
-    const int rc = cin_p % 64 == 0
-                       ? launch_conv_tma<BN, 64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
-                                                 batch, h, width, relu, s, err)
-                       : launch_conv_tma<BN, 32>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
-                                                 batch, h, width, relu, s, err);
+    const bool c64 = cin_p % 64 == 0;
+    int rc = -1;
+    // row boxes for 32-channel slices; 64-channel slices keep one box per
+    // tap (a row stage with three weight slices of 128-byte rows leaves
+    // half the CTAs per SM, measured slower on every such layer)
+    if (!c64 && g_tma_rows.load())
+      rc = launch_conv_tma<BN, 32, true>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h,
+                                         width, relu, s, err);
+    if (rc < 0)
+      rc = c64 ? launch_conv_tma<BN, 64, false>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
+                                                batch, h, width, relu, s, err)
+               : launch_conv_tma<BN, 32, false>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
+                                                batch, h, width, relu, s, err);
     if (rc >= 0) return rc;
   }
   return launch_conv<BN>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s,
@@ -867,13 +905,15 @@ extern "C" int strm_nn_set_conv_tma(int use) {
   return STRM_NN_OK;
 }
 
-extern "C" int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int persistent) {
+extern "C" int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int tiles_per_cta, int rows) {
   if (ctas_per_sm < 0 || ctas_per_sm > 8 || stages < 0 || stages == 1 ||
-      stages > kTmaMaxStages || persistent < 0 || persistent > 1)
+      stages > kTmaMaxStages || tiles_per_cta < 0 || tiles_per_cta > 64 || rows < 0 ||
+      rows > 1)
     return STRM_NN_ERR_INVALID;
   g_tma_ctas.store(ctas_per_sm);
   g_tma_stages.store(stages);
-  g_tma_persist.store(persistent);
+  g_tma_tiles.store(tiles_per_cta);
+  g_tma_rows.store(rows);
   return STRM_NN_OK;
 }
 

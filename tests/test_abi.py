@@ -57,11 +57,11 @@ def test_create_without_gpu_fails_loudly():
 
 def test_conv_launch_shape_rejects_values_out_of_range():
     """strm_nn_tune_conv_tma only records the launch shape (no device call):
-    CTAs per SM 0..8, stages 0 or 2..32, persistent 0 or 1."""
+    CTAs per SM 0..8, stages 0 or 2..32, tiles per CTA 0..64, rows 0 or 1."""
     L = _lib.load()
-    for bad in ((-1, 0, 1), (9, 0, 1), (0, 1, 1), (0, 33, 1), (0, -2, 1), (0, 0, 2),
-                (0, 0, -1)):
+    for bad in ((-1, 0, 1, 1), (9, 0, 1, 1), (0, 1, 1, 1), (0, 33, 1, 1), (0, -2, 1, 1),
+                (0, 0, 65, 1), (0, 0, -1, 1), (0, 0, 1, 2), (0, 0, 1, -1)):
         assert L.strm_nn_tune_conv_tma(*bad) == 6, bad
-    for good in ((0, 0, 1), (2, 6, 0), (1, 32, 1), (8, 2, 0)):
+    for good in ((0, 0, 0, 0), (2, 6, 1, 1), (1, 32, 0, 1), (8, 2, 64, 0)):
         assert L.strm_nn_tune_conv_tma(*good) == 0, good
-    assert L.strm_nn_tune_conv_tma(0, 0, 0) == 0
+    assert L.strm_nn_tune_conv_tma(0, 0, 0, 1) == 0
