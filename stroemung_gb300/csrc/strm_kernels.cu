@@ -109,17 +109,22 @@ __device__ double block_reduce(double v, Op op, double identity) {
 }
 
 // Returns true in the block that finished last; its reads of the other
-// blocks' partials are then ordered after their writes.
+// blocks' partials are then ordered after their writes.  Every caller has
+// its partials written by thread 0, so thread 0 alone fences: before its
+// ticket (release of this block's partials) and, in the last block, after
+// it (acquire of the others'); the barrier then orders the block's reads.
+// The other threads' stores (field updates) need no fence here: nothing
+// reads them before the kernel ends.
 __device__ __forceinline__ bool last_block_done(unsigned int *counter) {
   __shared__ bool am_last;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    unsigned int t = atomicAdd(counter, 1u);
-    am_last = (t == gridDim.x * gridDim.y - 1);
+    __threadfence();
+    const bool last = atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1;
+    if (last) __threadfence();
+    am_last = last;
   }
   __syncthreads();
-  if (am_last) __threadfence();
   return am_last;
 }
 
