@@ -114,25 +114,41 @@ __device__ __forceinline__ void st8(__nv_bfloat16 *p, const V8 &v) {
   *reinterpret_cast<uint4 *>(p) = v.u;
 }
 
-__global__ void avgpool_fwd8(const __nv_bfloat16 *in, int cs_in, __nv_bfloat16 *out, int cs_out,
-                             int batch, int h, int w, int c) {
-  const int ho = h / 2, wo = w / 2, c8 = c / 8;
-  const long long n = (long long)batch * ho * wo * c8;
-  GRID_STRIDE(i, n) {
-    const int ch = 8 * (int)(i % c8);
-    const long long q = i / c8;
-    const int xo = (int)(q % wo);
-    const long long t = q / wo;
-    const int yo = (int)(t % ho);
-    const long long b = t / ho;
-    const long long q00 = (b * h + 2 * yo) * w + 2 * xo;
+__global__ void avgpool_rows8(const __nv_bfloat16 *__restrict__ in, int cs_in,
+                              __nv_bfloat16 *__restrict__ out, int cs_out, int rows, int h, int w,
+                              int c8) {
+  const int wo = w / 2, ho = h / 2, n = wo * c8;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int xo = k / c8, ch = 8 * (k - xo * c8);
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int b = r / ho, yo = r - b * ho;
+    const long long q00 = ((long long)b * h + 2 * yo) * w + 2 * xo;
     const V8 a = ld8(in + q00 * cs_in + ch), bb = ld8(in + (q00 + 1) * cs_in + ch);
     const V8 cc = ld8(in + (q00 + w) * cs_in + ch), d = ld8(in + (q00 + w + 1) * cs_in + ch);
     V8 o;
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-      o.h[k] = __float2bfloat16_rn(0.25f * (bf(a.h[k]) + bf(bb.h[k]) + bf(cc.h[k]) + bf(d.h[k])));
-    st8(out + q * cs_out + ch, o);
+    for (int j = 0; j < 8; ++j)
+      o.h[j] = __float2bfloat16_rn(0.25f * (bf(a.h[j]) + bf(bb.h[j]) + bf(cc.h[j]) + bf(d.h[j])));
+    st8(out + ((long long)r * wo + xo) * cs_out + ch, o);
+  }
+}
+
+__global__ void upsample_rows8(const __nv_bfloat16 *__restrict__ in, int cs_in,
+                               __nv_bfloat16 *__restrict__ out, int cs_out, int rows, int h, int w,
+                               int c8) {
+  const int wi = w / 2, hi = h / 2, n = wi * c8;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int xi = k / c8, ch = 8 * (k - xi * c8);
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int b = r / hi, yi = r - b * hi;
+    const V8 v = ld8(in + ((long long)r * wi + xi) * cs_in + ch);
+    const long long q00 = ((long long)b * h + 2 * yi) * w + 2 * xi;
+    st8(out + q00 * cs_out + ch, v);
+    st8(out + (q00 + 1) * cs_out + ch, v);
+    st8(out + (q00 + w) * cs_out + ch, v);
+    st8(out + (q00 + w + 1) * cs_out + ch, v);
   }
 }
 
@@ -159,22 +175,6 @@ __global__ void avgpool_bwd8(const __nv_bfloat16 *gout, int cs_out, __nv_bfloat1
       o.h[k] = __float2bfloat16_rn(v);
     }
     st8(gin + q * cs_in + ch, o);
-  }
-}
-
-__global__ void upsample_fwd8(const __nv_bfloat16 *in, int cs_in, __nv_bfloat16 *out, int cs_out,
-                              int batch, int h, int w, int c) {
-  const int c8 = c / 8;
-  const long long n = (long long)batch * h * w * c8;
-  GRID_STRIDE(i, n) {
-    const int ch = 8 * (int)(i % c8);
-    const long long q = i / c8;
-    const int xx = (int)(q % w);
-    const long long t = q / w;
-    const int yy = (int)(t % h);
-    const long long b = t / h;
-    const long long qi = (b * (h / 2) + yy / 2) * (w / 2) + xx / 2;
-    st8(out + q * cs_out + ch, ld8(in + qi * cs_in + ch));
   }
 }
 
@@ -659,8 +659,10 @@ int strm_nn_avgpool(const void *in, int cs_in, void *out, int cs_out, int batch,
                     int c, void *stream) {
   if (!in || !out || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
   if (vec8(in, out, c, cs_in, cs_out)) {
-    avgpool_fwd8<<<grid_for((long long)batch * h * w * c / 32), 256, 0, (cudaStream_t)stream>>>(
-        (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
+    const int rows = batch * (h / 2), n = (w / 2) * (c / 8);
+    const dim3 grid((n + 127) / 128, rows < 65535 ? rows : 65535);
+    avgpool_rows8<<<grid, 128, 0, (cudaStream_t)stream>>>((const bf16 *)in, cs_in, (bf16 *)out,
+                                                          cs_out, rows, h, w, c / 8);
     return done();
   }
   avgpool_fwd<<<grid_for((long long)batch * h * w * c / 4), 256, 0, (cudaStream_t)stream>>>(
@@ -685,8 +687,10 @@ int strm_nn_upsample(const void *in, int cs_in, void *out, int cs_out, int batch
                      int c, void *stream) {
   if (!in || !out || h % 2 || w % 2) return STRM_NN_ERR_INVALID;
   if (vec8(in, out, c, cs_in, cs_out)) {
-    upsample_fwd8<<<grid_for((long long)batch * h * w * c / 8), 256, 0, (cudaStream_t)stream>>>(
-        (const bf16 *)in, cs_in, (bf16 *)out, cs_out, batch, h, w, c);
+    const int rows = batch * (h / 2), n = (w / 2) * (c / 8);
+    const dim3 grid((n + 127) / 128, rows < 65535 ? rows : 65535);
+    upsample_rows8<<<grid, 128, 0, (cudaStream_t)stream>>>((const bf16 *)in, cs_in, (bf16 *)out,
+                                                           cs_out, rows, h, w, c / 8);
     return done();
   }
   upsample_fwd<<<grid_for((long long)batch * h * w * c), 256, 0, (cudaStream_t)stream>>>(

@@ -244,3 +244,37 @@ def test_tma_forward_is_independent_of_its_launch_shape(cin, cout):
             assert (outs[0].float() - ref).abs().max().item() <= 1e-2 * scale, rows
     finally:
         L.strm_nn_tune_conv_tma(0, 0, 0, 1)
+
+
+@pytest.mark.parametrize("b,h,w,c,cs_in,cs_out", [(1, 8, 12, 64, 64, 96), (2, 6, 4, 32, 96, 32),
+                                                  (3, 4, 6, 8, 8, 8), (1, 2, 2, 16, 16, 16),
+                                                  (2, 10, 6, 6, 6, 6)])
+def test_avgpool_and_upsample_match_exact_references(b, h, w, c, cs_in, cs_out):
+    """Average pooling and nearest upsampling on NHWC buffers with pixel
+    strides (channel slices of concatenations): the pooled value is
+    0.25 * (((a + b) + c) + d) in FP32 rounded to BF16, the upsampled one a
+    copy; bit-exact, for the 16-byte row kernels and (c = 6, odd strides)
+    the element kernels."""
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.randn(b, h, w, cs_in, device="cuda", generator=g).to(torch.bfloat16)
+    # pooling: input h x w -> h/2 x w/2
+    out = torch.full((b, h // 2, w // 2, cs_out), 7.0, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_avgpool(x.data_ptr(), cs_in, out.data_ptr(), cs_out, b, h, w, c, None) == 0
+    torch.cuda.synchronize()
+    xf = x[..., :c].float()
+    a, bb = xf[:, 0::2, 0::2], xf[:, 0::2, 1::2]
+    cc, d = xf[:, 1::2, 0::2], xf[:, 1::2, 1::2]
+    ref = (0.25 * (((a + bb) + cc) + d)).to(torch.bfloat16)
+    assert torch.equal(out[..., :c], ref)
+    assert bool((out[..., c:] == 7.0).all())  # channels beyond c untouched
+    # upsampling: input h/2 x w/2 -> h x w
+    lo = x[:, : h // 2, : w // 2].contiguous()
+    up = torch.full((b, h, w, cs_out), 7.0, device="cuda", dtype=torch.bfloat16)
+    assert L.strm_nn_upsample(lo.data_ptr(), cs_in, up.data_ptr(), cs_out, b, h, w, c,
+                              None) == 0
+    torch.cuda.synchronize()
+    ref = lo[..., :c].repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
+    assert torch.equal(up[..., :c], ref)
+    assert bool((up[..., c:] == 7.0).all())
