@@ -319,16 +319,29 @@ constexpr int kTmaMaxStages = 32;
 // swizzled them), against three weight slices.  Otherwise a chunk is one
 // tap and slice (one 128-row box).  Row boxes move a third of the input
 // bytes; the launcher takes them for 32-channel slices only.
+//
+// CH = 8 (layers with 8 input channels, always with row boxes): 16-byte
+// operand rows without swizzle, so that 8 consecutive pixels of a box are
+// one 8 x 16-byte core matrix wherever they start.  A K = 16 MMA pairs two
+// taps of a row: its A descriptor starts at the first tap's pixel row and
+// steps 16 bytes (one pixel) to the second tap's core matrix; the row's
+// third tap pairs with a zero weight block (the box holds 131 pixels so
+// that this pairing reads inside it).  The weights, 12 K blocks of
+// BN x 8 (three rows x [three taps, zeros]), are staged once per CTA.
 template <int BN, int CH, bool ROWS>
 struct TmaConvPipe {
+  static_assert(CH != 8 || ROWS, "8-channel slices take row boxes");
   static constexpr int ROWB = CH * 2;              // bytes per operand row
-  static constexpr int A_ROWS = ROWS ? GM + 2 : GM;
-  static constexpr int A_BYTES = (A_ROWS * ROWB + 1023) / 1024 * 1024;
+  static constexpr int A_ROWS = CH == 8 ? GM + 3 : ROWS ? GM + 2 : GM;
+  static constexpr int ALIGN = CH == 8 ? 128 : 1024;
+  static constexpr int A_BYTES = (A_ROWS * ROWB + ALIGN - 1) / ALIGN * ALIGN;
   static constexpr int TAPS = ROWS ? 3 : 1;        // taps per chunk
-  static constexpr int B_TAP = BN * ROWB;
+  static constexpr int B_TAP = CH == 8 ? 0 : BN * ROWB;
   static constexpr int B_BYTES = TAPS * B_TAP;
-  static constexpr int STAGE = A_BYTES + B_BYTES;  // multiple of 1024
+  static constexpr int STAGE = A_BYTES + B_BYTES;  // multiple of ALIGN
   static constexpr int TX = A_ROWS * ROWB + B_BYTES;  // bytes the copies write
+  static constexpr int B_KBLOCK = BN * 16;           // CH = 8: one K block of the weights
+  static constexpr int B_CONST = CH == 8 ? 12 * B_KBLOCK : 0;  // staged once per CTA
   static constexpr int NACC = 2 * BN <= 256 ? 2 : 1;  // accumulators in TMEM
   static constexpr int TM_COLS = NACC * BN < 32 ? 32 : NACC * BN;
   static constexpr int TM_ONE = BN < 32 ? 32 : BN;  // one accumulator
@@ -339,11 +352,12 @@ __global__ void __launch_bounds__(192)
     conv3x3_fwd_tma_kernel(const __grid_constant__ CUtensorMap tx,
                            const __grid_constant__ CUtensorMap tw, const float *__restrict__ bias,
                            __nv_bfloat16 *__restrict__ y, float *__restrict__ y32, ConvShape s,
-                           int relu, int S, unsigned int *err) {
+                           int relu, int S, const __nv_bfloat16 *__restrict__ w,
+                           unsigned int *err) {
   using P = TmaConvPipe<BN, CH, ROWS>;
   constexpr int NACC = P::NACC;
-  static_assert(P::STAGE % 1024 == 0, "stage alignment");
-  static_assert(P::B_TAP % (CH == 64 ? 1024 : 512) == 0, "weight slice alignment");
+  static_assert(P::STAGE % P::ALIGN == 0, "stage alignment");
+  static_assert(CH == 8 || P::B_TAP % (CH == 64 ? 1024 : 512) == 0, "weight slice alignment");
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[kTmaMaxStages], empty[kTmaMaxStages], tfull[NACC], tempty[NACC];
   __shared__ uint32_t tmem_slot;
@@ -368,6 +382,19 @@ __global__ void __launch_bounds__(192)
       mbar_init(&tempty[i], 4);  // one arrival per epilogue warp
     }
     fail = 0;
+  }
+  // CH = 8: the weights, staged once: K block i = 4 ky + t holds taps
+  // (ky, t) for t < 3 and zeros for t = 3, n-block j's core matrix at
+  // i * B_KBLOCK + 128 j, row n % 8 at +16 (n % 8)
+  uint8_t *sB = stage0 + S * P::STAGE;
+  if (CH == 8) {
+    for (int e = tid; e < 12 * BN; e += blockDim.x) {
+      const int i = e / BN, n = e - i * BN, ky = i >> 2, t3 = i & 3;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (t3 < 3) v = *reinterpret_cast<const uint4 *>(w + (size_t)n * s.kp + (ky * 3 + t3) * 8);
+      *reinterpret_cast<uint4 *>(sB + i * P::B_KBLOCK + (n >> 3) * 128 + (n & 7) * 16) = v;
+    }
+    fence_async_smem();  // visible to the tensor core's reads
   }
   tc_fence_before();
   __syncthreads();
@@ -398,9 +425,10 @@ __global__ void __launch_bounds__(192)
         if (ROWS) {
           const int ky = kc / cpt, j = kc - ky * cpt;
           tma_load_4d(smem_u32(sA), &tx, j * CH, x0 - 1, yy + ky - 1, bb, &full[st]);
-          for (int kx = 0; kx < 3; ++kx)
-            tma_load_2d(smem_u32(sA + P::A_BYTES + kx * P::B_TAP), &tw,
-                        (ky * 3 + kx) * s.cin_p + j * CH, 0, &full[st]);
+          if (CH != 8)
+            for (int kx = 0; kx < 3; ++kx)
+              tma_load_2d(smem_u32(sA + P::A_BYTES + kx * P::B_TAP), &tw,
+                          (ky * 3 + kx) * s.cin_p + j * CH, 0, &full[st]);
         } else {
           const int tap = kc / cpt, j = kc - tap * cpt;
           const int dy = tap / 3 - 1, dx = tap % 3 - 1;
@@ -441,6 +469,16 @@ __global__ void __launch_bounds__(192)
         if (!ok) break;
         tc_fence_after();
         uint8_t *sA = stage0 + st * P::STAGE;
+        if (CH == 8) {
+          // taps (kc, 0) + (kc, 1), then (kc, 2) + the zero block
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const uint64_t da = desc_kmajor_noswz(smem_u32(sA + 32 * half), 16, 128);
+            const uint64_t db = desc_kmajor_noswz(
+                smem_u32(sB + (4 * kc + 2 * half) * P::B_KBLOCK), P::B_KBLOCK, 128);
+            umma_bf16(d, da, db, idesc, (kc > 0 || half > 0) ? 1u : 0u);
+          }
+        } else {
 #pragma unroll
         for (int kx = 0; kx < P::TAPS; ++kx) {
           // tap dx = kx - 1 of a row box: the 128 rows from row kx
@@ -452,6 +490,7 @@ __global__ void __launch_bounds__(192)
           for (int kk = 0; kk < CH / 16; ++kk)
             umma_bf16(d, da + 2 * kk, db + 2 * kk, idesc,
                       (kc > 0 || kx > 0 || kk > 0) ? 1u : 0u);
+        }
         }
         umma_commit(&empty[st]);
         if (++st == S) {
@@ -735,8 +774,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // The TMA path takes layers whose input channels come in slices of 32 or 64
 // and whose image rows hold whole 128-pixel tiles.
 bool tma_conv_applies(int cin_p, int width, int cs_in, const void *x) {
-  return g_conv_tma.load() && cin_p % 32 == 0 && width % GM == 0 && cs_in % 8 == 0 &&
-         (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
+  return g_conv_tma.load() && (cin_p % 32 == 0 || cin_p == 8) && width % GM == 0 &&
+         cs_in % 8 == 0 && (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
 }
 
 template <int BN, int CH, bool ROWS>
@@ -747,7 +786,9 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return -1;
   CUtensorMap tx{}, tw{};
-  const CUtensorMapSwizzle sw = CH == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  const CUtensorMapSwizzle sw = CH == 64   ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : CH == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                           : CU_TENSOR_MAP_SWIZZLE_NONE;
   // input: {channels (cin_p of a pixel's cs_in), x, y, image}, 2-byte elements
   const cuuint64_t xdim[4] = {(cuuint64_t)cin_p, (cuuint64_t)width, (cuuint64_t)h,
                               (cuuint64_t)batch};
@@ -759,14 +800,16 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return -1;
-  // weights: {K, output channels}
+  // weights: {K, output channels} (CH = 8 stages them without TMA)
   const cuuint64_t wdim[2] = {(cuuint64_t)kp, (cuuint64_t)BN};
   const cuuint64_t wstr[1] = {(cuuint64_t)kp * 2};
   const cuuint32_t wbox[2] = {(cuuint32_t)CH, (cuuint32_t)BN};
-  if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(w), wdim, wstr, wbox, one,
+  if (CH != 8 &&
+      enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(w), wdim, wstr, wbox, one,
           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return -1;
+  if (CH == 8 && (reinterpret_cast<uintptr_t>(w) & 15u) != 0) return -1;
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
   // device limits, once per instantiation: shared memory per SM, per CTA
   // (opt-in) and reserved per CTA, the kernel's static shared memory
@@ -798,21 +841,22 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   const int tiles = g_tma_tiles.load();  // tiles per CTA, 0: by the layer's size
   const int tm_cap = 512 / (tiles != 1 ? P::TM_COLS : P::TM_ONE);
   int ctas = g_tma_ctas.load();
-  if (ctas < 1) ctas = smem_sm / (2 * P::STAGE + 1024 + reserved + stat);
+  if (ctas < 1) ctas = smem_sm / (2 * P::STAGE + P::B_CONST + 1024 + reserved + stat);
   if (ctas > 8) ctas = 8;
   if (ctas > tm_cap) ctas = tm_cap;
   // fewer CTAs until each holds a two-stage ring (the mode a layer takes
   // does not depend on the launch shape asked for)
-  while (ctas > 1 && (smem_sm / ctas - reserved - stat - 1024) / P::STAGE < 2) --ctas;
+  const int fixed = reserved + stat + 1024 + P::B_CONST;  // per CTA, besides the ring
+  while (ctas > 1 && (smem_sm / ctas - fixed) / P::STAGE < 2) --ctas;
   if (ctas < 1) ctas = 1;
-  int stages = (smem_sm / ctas - reserved - stat - 1024) / P::STAGE;
-  const int cap_blk = (smem_blk - stat - 1024) / P::STAGE;
+  int stages = (smem_sm / ctas - fixed) / P::STAGE;
+  const int cap_blk = (smem_blk - stat - 1024 - P::B_CONST) / P::STAGE;
   if (stages > cap_blk) stages = cap_blk;
   if (stages > kTmaMaxStages) stages = kTmaMaxStages;
   const int tuned = g_tma_stages.load();
   if (tuned > 0 && tuned < stages) stages = tuned;
   if (stages < 2) return -1;
-  const int dyn = stages * P::STAGE + 1024;
+  const int dyn = stages * P::STAGE + P::B_CONST + 1024;
   static int fit_dyn = -1, fit = 0;  // CTAs per SM at the last ring size asked
   if (dyn != fit_dyn) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH, ROWS>, 192,
@@ -830,7 +874,7 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   const int per = tiles > 0 ? tiles : ntiles >= 4 * slots ? 4 : ntiles >= 2 * slots ? 2 : 1;
   const unsigned int grid = (unsigned int)((ntiles + per - 1) / per);
   conv3x3_fwd_tma_kernel<BN, CH, ROWS><<<grid, 192, dyn, s>>>(
-      tx, tw, bias, (__nv_bfloat16 *)y, y32, sh, relu, stages, err);
+      tx, tw, bias, (__nv_bfloat16 *)y, y32, sh, relu, stages, (const __nv_bfloat16 *)w, err);
   return cudaGetLastError() == cudaSuccess ? STRM_NN_OK : STRM_NN_ERR_CUDA;
 }
 
@@ -843,6 +887,15 @@ int launch_conv_any(const void *x, int cs_in, int cin_p, const void *w, int kp, 
   if (tma_conv_applies(cin_p, width, cs_in, x)) {
     const bool c64 = cin_p % 64 == 0;
     int rc = -1;
+    if (cin_p == 8) {
+      // 8-channel input (the first layer): row boxes of 16-byte pixels
+      if (g_tma_rows.load())
+        rc = launch_conv_tma<BN, 8, true>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h,
+                                          width, relu, s, err);
+      if (rc >= 0) return rc;
+      return launch_conv<BN>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width,
+                             relu, s, err);
+    }
     // row boxes for 32-channel slices; 64-channel slices keep one box per
     // tap (a row stage with three weight slices of 128-byte rows leaves
     // half the CTAs per SM, measured slower on every such layer)

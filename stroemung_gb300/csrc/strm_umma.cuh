@@ -48,6 +48,20 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw64(uint32_t saddr) {
   return d;
 }
 
+// Descriptor for a K-major tile without swizzle: 8-row x 16-byte core
+// matrices, each 128 contiguous bytes (row r at +16 r); `lbo` bytes between
+// core matrices adjacent in K, `sbo` between those adjacent in M (or N).
+// The start needs 16-byte alignment only.
+__device__ __forceinline__ uint64_t desc_kmajor_noswz(uint32_t saddr, uint32_t lbo,
+                                                      uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  return d;
+}
+
 // Instruction descriptor for kind::f16: D F32 (bits 4-5 = 1), A and B BF16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in
 // bits [17,23), M >> 4 in bits [24,29).

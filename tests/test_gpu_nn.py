@@ -54,8 +54,9 @@ def _nhwc(x, cin_p):
 
 # the odd sizes leave partial pixel tiles and image rows (the gathering
 # kernel); widths that are multiples of 128 with inputs in slices of 32 or 64
-# channels take the TMA-staged kernel (64-byte rows for 32-channel slices,
-# 128-byte rows for 64)
+# channels, or of 8 (inputs of up to 8 channels), take the TMA-staged kernel
+# (64-byte swizzled rows for 32-channel slices, 128-byte for 64, unswizzled
+# 16-byte pixels for 8)
 @pytest.mark.parametrize("cin,cout,h,w,relu", [(3, 32, 16, 128, 1), (32, 64, 8, 64, 1),
                                                 (96, 32, 16, 32, 0), (128, 256, 4, 64, 1),
                                                 (64, 16, 8, 16, 1), (32, 32, 7, 200, 1),
@@ -64,7 +65,10 @@ def _nhwc(x, cin_p):
                                                 (32, 32, 5, 128, 1), (64, 64, 3, 256, 0),
                                                 (128, 128, 2, 128, 1), (256, 256, 2, 128, 1),
                                                 (192, 64, 2, 128, 1), (64, 16, 3, 128, 1),
-                                                (32, 256, 3, 128, 0), (384, 128, 1, 128, 0)])
+                                                (32, 256, 3, 128, 0), (384, 128, 1, 128, 0),
+                                                (8, 32, 4, 256, 1), (8, 64, 3, 128, 0),
+                                                (5, 16, 2, 384, 1), (8, 256, 2, 128, 1),
+                                                (8, 128, 3, 256, 1)])
 def test_conv3x3_forward_matches_torch(cin, cout, h, w, relu):
     import torch
     import torch.nn.functional as F
@@ -206,7 +210,8 @@ def test_tma_staged_forward_matches_the_gathering_kernel(use_slice):
     assert (outs[0] - outs[1]).abs().max().item() <= 1e-2 * scale
 
 
-@pytest.mark.parametrize("cin,cout", [(32, 32), (64, 64), (96, 32), (128, 128), (128, 256)])
+@pytest.mark.parametrize("cin,cout", [(32, 32), (64, 64), (96, 32), (128, 128), (128, 256),
+                                      (8, 32)])
 def test_tma_forward_is_independent_of_its_launch_shape(cin, cout):
     """The TMA-fed forward gives the same bits for any launch shape — one,
     several or all tiles per CTA, any number of CTAs per SM and ring depth
