@@ -38,15 +38,16 @@ int strm_nn_set_conv_tma(int use);
  * CTA n of the layer's 128-pixel tiles, ctas_per_sm of them sharing an SM's
  * shared memory; 0 (the default) takes four while the layer fills every
  * CTA slot of the GPU that often, else two, else one.  ctas_per_sm 0 (the
- * default) takes as many
- * as hold a two-stage ring each, at most 8 and what TMEM allows; each CTA
- * has a ring of `stages` operand stages (0: as many as its share of the
- * SM's shared memory holds; else 2..32).  rows = 1 (the default) loads one
- * 130-pixel box per kernel row and 32-channel slice and feeds the three
- * taps of that row from it; 0 loads one 128-pixel box per tap (as 64-channel
- * slices always do).  Process-wide; for a given `rows` results do not
- * depend on it (the two `rows` modes add the K terms in different orders).
- * STRM_NN_ERR_INVALID for values out of range (tiles_per_cta 0..64). */
+ * default) takes as many as hold a two-stage ring each, at most 8 and what
+ * TMEM allows; each CTA has a ring of `stages` operand stages (0: as many
+ * as its share of the SM's shared memory holds; else 2..32).  rows = 1 (the
+ * default) loads, for up to 128 output channels, one 130-pixel box per
+ * kernel row and 32-channel slice and feeds the three taps of that row from
+ * it; 0 loads one 128-pixel box per tap and 32- or 64-channel slice (as
+ * 256-channel tiles always do).  Process-wide; for a given `rows` results
+ * do not depend on it (the two `rows` modes add the K terms in different
+ * orders).  STRM_NN_ERR_INVALID for values out of range (tiles_per_cta
+ * 0..64). */
 int strm_nn_tune_conv_tma(int ctas_per_sm, int stages, int tiles_per_cta, int rows);
 int strm_nn_status(void *stream);
 
@@ -78,6 +79,14 @@ int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *w, int kp,
  * forward ReLU output yact (y > 0) when yact is not NULL (yact uses the
  * forward pixel stride cs_out).  Waits for the kernel unless
  * strm_nn_set_sync(0). */
+/* strm_nn_conv3x3 with ReLU (relu = 1) and BF16 output, followed by the 1x1
+ * FP32 head of strm_nn_head in the same kernel: q[p] = bh[0] + sum_c wh[c] *
+ * y[p][c] over the BF16 outputs, in channel order — the same bits as the two
+ * calls.  y may be NULL: the activations are then not stored (cs_out is
+ * ignored), as a prediction that no backward follows needs. */
+int strm_nn_conv3x3_head(const void *x, int cs_in, int cin_p, const void *w, int kp,
+                         const float *bias, void *y, int cs_out, int cout, int batch, int h,
+                         int width, const float *wh, const float *bh, float *q, void *stream);
 int strm_nn_conv3x3_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy,
                           int cs_dy, const void *yact, int cs_out, float *dw, int cout,
                           int batch, int h, int width, void *stream);

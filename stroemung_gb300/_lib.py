@@ -133,6 +133,8 @@ SIGNATURES = {
     "strm_nn_status": [_vp],
     "strm_nn_gemm_bf16": [_vp, _vp, _fp, _i, _i, _i, _vp],
     "strm_nn_conv3x3": [_vp, _i, _i, _vp, _i, _fp, _vp, _fp, _i, _i, _i, _i, _i, _i, _vp],
+    "strm_nn_conv3x3_head": [_vp, _i, _i, _vp, _i, _fp, _vp, _i, _i, _i, _i, _i, _fp, _fp, _fp,
+                             _vp],
     "strm_nn_conv3x3_wgrad": [_vp, _i, _i, _i, _vp, _i, _vp, _i, _fp, _i, _i, _i, _i, _vp],
     "strm_nn_avgpool": [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp],
     "strm_nn_avgpool_bwd": [_vp, _i, _vp, _i, _i, _i, _i, _i, _i, _vp],

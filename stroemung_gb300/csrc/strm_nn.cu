@@ -101,6 +101,15 @@ __global__ void __launch_bounds__(128)
 // image.  Epilogue: + bias, optional ReLU, BF16 NHWC store.
 // ------------------------------------------------------------------------
 
+// The 1x1 FP32 head fused into a convolution's epilogue (q != nullptr):
+// q[p] = bh + sum_c wh[c] * y[p][c] over the BF16-rounded outputs, with the
+// operations of head_fwd in its order; y may then be left unstored.
+struct Head {
+  const float *wh = nullptr;
+  const float *bh = nullptr;
+  float *q = nullptr;
+};
+
 struct ConvShape {
   int batch, h, w;
   int cin_p;      // padded input channels (multiple of 8)
@@ -108,7 +117,45 @@ struct ConvShape {
   int cout;       // output channels (multiple of 16, <= 256)
   int cs_out;     // output pixel stride (elements)
   int kp;         // padded K = roundup(9*cin_p, 64)
+  Head hd{};
 };
+
+// Epilogue of one 16-channel group of a pixel: bias, ReLU, the store (FP32,
+// BF16 or none) and the fused head's share.
+__device__ __forceinline__ void conv_epilogue16(float *v, int c, const float *bias, int relu,
+                                                __nv_bfloat16 *y, float *y32, long long q,
+                                                const ConvShape &s, float &hs) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    v[i] += bias ? bias[c + i] : 0.0f;
+    if (relu) v[i] = fmaxf(v[i], 0.0f);
+  }
+  if (y32) {
+    float *dst = y32 + q * s.cs_out + c;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) dst[i] = v[i];
+    return;
+  }
+  // BF16 bits of the 16 outputs, two per word (channel 2i in the low half)
+  uint32_t pk[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    pk[i] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * i])) |
+            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * i + 1])) << 16);
+  if (y) {
+    uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
+    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  }
+  if (s.hd.q) {
+    // the BF16 value as FP32: its bits in the high half
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      hs = fmaf(s.hd.wh[c + 2 * i], __uint_as_float(pk[i] << 16), hs);
+      hs = fmaf(s.hd.wh[c + 2 * i + 1], __uint_as_float(pk[i] & 0xFFFF0000u), hs);
+    }
+  }
+}
 
 // Pipelined and warp-specialised: warps 0-3 gather the im2col rows (A) and
 // the weights (B) of each 64-wide K chunk into a ring of S shared-memory
@@ -250,30 +297,14 @@ __global__ void __launch_bounds__(160)
     tc_fence_after();
     const long long q = q0 + warp * 32 + lane;
     if (ok) {
+      float hs = s.hd.q ? *s.hd.bh : 0.0f;
 #pragma unroll 1
       for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-        if (q < npix) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            v[i] += bias ? bias[c + i] : 0.0f;
-            if (relu) v[i] = fmaxf(v[i], 0.0f);
-          }
-          if (y32) {
-            float *dst = y32 + q * s.cs_out + c;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) dst[i] = v[i];
-          } else {
-            __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
-            uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
-            dst[0] = reinterpret_cast<const uint4 *>(o)[0];
-            dst[1] = reinterpret_cast<const uint4 *>(o)[1];
-          }
-        }
+        if (q < npix) conv_epilogue16(v, c, bias, relu, y, y32, q, s, hs);
       }
+      if (s.hd.q && q < npix) s.hd.q[q] = hs;
     } else {
       atomicExch(&fail, 1);
     }
@@ -318,7 +349,8 @@ constexpr int kTmaMaxStages = 32;
 // start one 64- or 128-byte row into the box reads the rows as the copy
 // swizzled them), against three weight slices.  Otherwise a chunk is one
 // tap and slice (one 128-row box).  Row boxes move a third of the input
-// bytes; the launcher takes them for 32-channel slices only.
+// bytes; the launcher takes them (with 32-channel slices) for tiles of up to
+// 128 output channels.
 //
 // CH = 8 (layers with 8 input channels, always with row boxes): 16-byte
 // operand rows without swizzle, so that 8 consecutive pixels of a box are
@@ -511,28 +543,14 @@ __global__ void __launch_bounds__(192)
       if (!ok) break;
       tc_fence_after();
       const long long q = (long long)t * GM + warp * 32 + lane;
+      float hs = s.hd.q ? *s.hd.bh : 0.0f;
 #pragma unroll 1
       for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * BN + c), v);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          v[i] += bias ? bias[c + i] : 0.0f;
-          if (relu) v[i] = fmaxf(v[i], 0.0f);
-        }
-        if (y32) {
-          float *dst = y32 + q * s.cs_out + c;
-#pragma unroll
-          for (int i = 0; i < 16; ++i) dst[i] = v[i];
-        } else {
-          __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) o[i] = __float2bfloat16_rn(v[i]);
-          uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
-          dst[0] = reinterpret_cast<const uint4 *>(o)[0];
-          dst[1] = reinterpret_cast<const uint4 *>(o)[1];
-        }
+        conv_epilogue16(v, c, bias, relu, y, y32, q, s, hs);
       }
+      if (s.hd.q) s.hd.q[q] = hs;
       // the accumulator may be overwritten once all four warps have read it
       tc_fence_before();
       __syncwarp();
@@ -724,8 +742,8 @@ namespace {
 template <int BN>
 int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, const float *bias,
                 void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
-                cudaStream_t s, unsigned int *err) {
-  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
+                cudaStream_t s, unsigned int *err, Head hd = Head{}) {
+  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp, hd};
   const int smem = ConvPipe<BN>::SMEM;
   static bool configured = false;
   if (!configured) {
@@ -781,7 +799,7 @@ bool tma_conv_applies(int cin_p, int width, int cs_in, const void *x) {
 template <int BN, int CH, bool ROWS>
 int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
                     const float *bias, void *y, float *y32, int cs_out, int batch, int h,
-                    int width, int relu, cudaStream_t s, unsigned int *err) {
+                    int width, int relu, cudaStream_t s, unsigned int *err, Head hd) {
   using P = TmaConvPipe<BN, CH, ROWS>;
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return -1;
@@ -810,7 +828,7 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return -1;
   if (CH == 8 && (reinterpret_cast<uintptr_t>(w) & 15u) != 0) return -1;
-  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
+  ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp, hd};
   // device limits, once per instantiation: shared memory per SM, per CTA
   // (opt-in) and reserved per CTA, the kernel's static shared memory
   static int nsm = 0, smem_sm = 0, smem_blk = 0, reserved = 0, stat = 0;
@@ -883,7 +901,7 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
 template <int BN>
 int launch_conv_any(const void *x, int cs_in, int cin_p, const void *w, int kp, const float *bias,
                     void *y, float *y32, int cs_out, int batch, int h, int width, int relu,
-                    cudaStream_t s, unsigned int *err) {
+                    cudaStream_t s, unsigned int *err, Head hd = Head{}) {
   if (tma_conv_applies(cin_p, width, cs_in, x)) {
     const bool c64 = cin_p % 64 == 0;
     int rc = -1;
@@ -891,26 +909,28 @@ int launch_conv_any(const void *x, int cs_in, int cin_p, const void *w, int kp, 
       // 8-channel input (the first layer): row boxes of 16-byte pixels
       if (g_tma_rows.load())
         rc = launch_conv_tma<BN, 8, true>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h,
-                                          width, relu, s, err);
+                                          width, relu, s, err, hd);
       if (rc >= 0) return rc;
       return launch_conv<BN>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width,
-                             relu, s, err);
+                             relu, s, err, hd);
     }
-    // row boxes for 32-channel slices; 64-channel slices keep one box per
-    // tap (a row stage with three weight slices of 128-byte rows leaves
-    // half the CTAs per SM, measured slower on every such layer)
-    if (!c64 && g_tma_rows.load())
+    // row boxes of 32-channel slices (also for channel counts that are
+    // multiples of 64) up to 128 output channels; 256-channel tiles keep one
+    // box of 64-channel slices per tap (their row stages, with three weight
+    // slices, leave too few CTAs per SM: measured slower), and so do
+    // 64-channel slices in row boxes of 128-byte rows
+    if (g_tma_rows.load() && BN <= 128)
       rc = launch_conv_tma<BN, 32, true>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h,
-                                         width, relu, s, err);
+                                         width, relu, s, err, hd);
     if (rc < 0)
       rc = c64 ? launch_conv_tma<BN, 64, false>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
-                                                batch, h, width, relu, s, err)
+                                                batch, h, width, relu, s, err, hd)
                : launch_conv_tma<BN, 32, false>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out,
-                                                batch, h, width, relu, s, err);
+                                                batch, h, width, relu, s, err, hd);
     if (rc >= 0) return rc;
   }
   return launch_conv<BN>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s,
-                         err);
+                         err, hd);
 }
 
 template <int BN>
@@ -997,6 +1017,31 @@ extern "C" int strm_nn_conv3x3(const void *x, int cs_in, int cin_p, const void *
     case 64: rc = launch_conv_any<64>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
     case 128: rc = launch_conv_any<128>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
     default: rc = launch_conv_any<256>(x, cs_in, cin_p, w, kp, bias, y, y32, cs_out, batch, h, width, relu, s, err); break;
+  }
+  return finish(err, s, rc);
+}
+
+extern "C" int strm_nn_conv3x3_head(const void *x, int cs_in, int cin_p, const void *w, int kp,
+                                    const float *bias, void *y, int cs_out, int cout, int batch,
+                                    int h, int width, const float *wh, const float *bh, float *q,
+                                    void *stream) {
+  if (!x || !w || !wh || !bh || !q || batch < 1 || h < 1 || width < 1 ||
+      !conv_args_ok(cs_in, cin_p, kp, y ? cs_out : cout, cout))
+    return STRM_NN_ERR_INVALID;
+  unsigned int *err = nullptr;
+  if (error_flag(&err) != cudaSuccess) return STRM_NN_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  Head hd;
+  hd.wh = wh;
+  hd.bh = bh;
+  hd.q = q;
+  int rc;
+  switch (cout) {
+    case 16: rc = launch_conv_any<16>(x, cs_in, cin_p, w, kp, bias, y, nullptr, cs_out, batch, h, width, 1, s, err, hd); break;
+    case 32: rc = launch_conv_any<32>(x, cs_in, cin_p, w, kp, bias, y, nullptr, cs_out, batch, h, width, 1, s, err, hd); break;
+    case 64: rc = launch_conv_any<64>(x, cs_in, cin_p, w, kp, bias, y, nullptr, cs_out, batch, h, width, 1, s, err, hd); break;
+    case 128: rc = launch_conv_any<128>(x, cs_in, cin_p, w, kp, bias, y, nullptr, cs_out, batch, h, width, 1, s, err, hd); break;
+    default: rc = launch_conv_any<256>(x, cs_in, cin_p, w, kp, bias, y, nullptr, cs_out, batch, h, width, 1, s, err, hd); break;
   }
   return finish(err, s, rc);
 }

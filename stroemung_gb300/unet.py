@@ -208,7 +208,7 @@ class UNet:
                 ("b1", h // 8, w // 8, c3), ("b2", h // 8, w // 8, c3),
                 ("d2a", h // 4, w // 4, c2), ("d2", h // 4, w // 4, c2),
                 ("d1a", h // 2, w // 2, c1), ("d1", h // 2, w // 2, c1),
-                ("d0a", h, w, c0), ("d0", h, w, c0)]
+                ("d0a", h, w, c0)]  # the last activations are not stored (fused head)
         offs, total = [], 0
         for _, hh, ww, c in spec:
             offs.append(total)
@@ -316,9 +316,12 @@ class UNet:
         self._check(L.strm_nn_upsample(ptr("d1"), c1, ptr("cat0"), c1 + c0, b, h, w, c1, self._stream),
                     "up")
         self._conv(d0a, ptr("cat0"), c1 + c0, ptr("d0a"), c0, b, h, w)
-        self._conv(d0b, ptr("d0a"), c0, ptr("d0"), c0, b, h, w)
-        self._check(L.strm_nn_head(ptr("d0"), c0, c0, self._ptr(self.wh), self._ptr(self.bh),
-                                   ptr("q"), b * h * w, self._stream), "head")
+        # the last convolution with the 1x1 head in its epilogue; its
+        # activations are stored only for a backward
+        self._check(L.strm_nn_conv3x3_head(
+            ptr("d0a"), c0, d0b.cin_p, self._wbf(d0b), d0b.kp, self._ptr(d0b.b),
+            ptr("d0") if keep else None, c0, d0b.cout, b, h, w, self._ptr(self.wh),
+            self._ptr(self.bh), ptr("q"), self._stream), "conv3x3 + head")
         return B["q"]
 
     # ---- backward ----------------------------------------------------------------

@@ -283,3 +283,41 @@ def test_avgpool_and_upsample_match_exact_references(b, h, w, c, cs_in, cs_out):
     ref = lo[..., :c].repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
     assert torch.equal(up[..., :c], ref)
     assert bool((up[..., c:] == 7.0).all())
+
+
+@pytest.mark.parametrize("cin,cout,h,w", [(32, 32, 3, 256), (64, 64, 2, 128), (8, 32, 3, 128),
+                                          (32, 32, 5, 200), (96, 32, 2, 384)])
+def test_conv_with_fused_head_equals_conv_then_head(cin, cout, h, w):
+    """strm_nn_conv3x3_head gives the activations and the head output of
+    strm_nn_conv3x3 (ReLU) followed by strm_nn_head bit for bit, on the
+    TMA-fed kernel (widths of whole 128-pixel tiles) and on the gathering
+    one (w = 200), with and without storing the activations."""
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(cin + 3 * cout + w)
+    b = 2
+    x = _bf(torch.randn(b, cin, h, w, device="cuda", generator=g))
+    wt = _bf(torch.randn(cout, cin, 3, 3, device="cuda", generator=g) * 0.2)
+    bias = torch.randn(cout, device="cuda", generator=g)
+    wh = torch.randn(cout, device="cuda", generator=g)
+    bh = torch.randn(1, device="cuda", generator=g)
+    wp, kp = _pack_weights(wt, cin)
+    xn = _nhwc(x, cin)
+    y1 = torch.empty(b, h, w, cout, device="cuda", dtype=torch.bfloat16)
+    q1 = torch.empty(b, h, w, device="cuda")
+    assert L.strm_nn_conv3x3(xn.data_ptr(), cin, cin, wp.data_ptr(), kp, bias.data_ptr(),
+                             y1.data_ptr(), None, cout, cout, b, h, w, 1, None) == 0
+    assert L.strm_nn_head(y1.data_ptr(), cout, cout, wh.data_ptr(), bh.data_ptr(), q1.data_ptr(),
+                          b * h * w, None) == 0
+    y2 = torch.empty_like(y1)
+    q2 = torch.empty_like(q1)
+    q3 = torch.empty_like(q1)
+    assert L.strm_nn_conv3x3_head(xn.data_ptr(), cin, cin, wp.data_ptr(), kp, bias.data_ptr(),
+                                  y2.data_ptr(), cout, cout, b, h, w, wh.data_ptr(),
+                                  bh.data_ptr(), q2.data_ptr(), None) == 0
+    assert L.strm_nn_conv3x3_head(xn.data_ptr(), cin, cin, wp.data_ptr(), kp, bias.data_ptr(),
+                                  None, cout, cout, b, h, w, wh.data_ptr(), bh.data_ptr(),
+                                  q3.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(y2, y1)
+    assert torch.equal(q2, q1) and torch.equal(q3, q1)
