@@ -317,11 +317,12 @@ __global__ void __launch_bounds__(160)
 
 // ------------------------------------------------------------------------
 // The same convolution with its operands staged by TMA (layers whose input
-// channels are a multiple of 32 and whose image width is a multiple of 128),
-// as a persistent warp-specialised kernel.  A tile is 128 consecutive
-// pixels of one image row; each CTA walks tiles blockIdx.x, + gridDim.x, ...
-// The K loop of a tile runs over taps and CH-channel slices of each tap
-// (CH = 64: 128-byte swizzled rows; CH = 32: 64-byte swizzled rows).
+// channels are a multiple of 32, or 8, and whose image width is a multiple
+// of 128), warp-specialised.  A tile is 128 consecutive pixels of one image
+// row; CTA b takes tiles b, b + gridDim.x, ... (the launcher picks how many
+// per CTA).  The K loop of a tile runs over taps (or kernel rows, below) and
+// CH-channel slices (CH = 64: 128-byte swizzled rows; CH = 32: 64-byte
+// swizzled rows; CH = 8: unswizzled 16-byte rows).
 //   producer (warp 4, one thread): per K chunk a 4-D TMA load of the input
 //     box {CH channels, 128 pixels at x0 + dx, row y + dy, image b} — the
 //     border falls outside the tensor and is filled with zeros — and a 2-D
