@@ -30,6 +30,7 @@
 #include <stddef.h>
 
 #include <algorithm>
+#include <atomic>
 #include <initializer_list>
 
 #include "strm_kernels.cuh"
@@ -2616,12 +2617,12 @@ static std::vector<SweepLaunch> sweep_plan(const DevFields &d, const Geom &g, in
 
 // Opts the blocked kernels into their shared-memory size, once per device.
 static cudaError_t tb_prepare() {
-  static bool done_on[64] = {};
+  static std::atomic<bool> done_on[64] = {};
   int dev = 0;
   cudaError_t e0 = cudaGetDevice(&dev);
   if (e0 != cudaSuccess) return e0;
-  bool &done = done_on[dev & 63];
-  if (done) return cudaSuccess;
+  std::atomic<bool> &done = done_on[dev & 63];
+  if (done.load()) return cudaSuccess;
   for (int i = 1; i < kNumSchedules; ++i) {
     cudaError_t e = cudaFuncSetAttribute(kTbShapes[i].fn,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2667,12 +2668,12 @@ cudaError_t launch_bc(const DevFields &d, cudaStream_t s) {
 
 // Opts fg_rhs_fast_kernel into its dynamic shared memory (once per device).
 static cudaError_t ff_prepare() {
-  static bool done_on[64] = {};
+  static std::atomic<bool> done_on[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  bool &done = done_on[dev & 63];
-  if (done) return cudaSuccess;
+  std::atomic<bool> &done = done_on[dev & 63];
+  if (done.load()) return cudaSuccess;
   e = cudaFuncSetAttribute(fg_rhs_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sizeof(FastFgSmem));
   if (e == cudaSuccess) done = true;

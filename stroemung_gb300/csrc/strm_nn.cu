@@ -746,13 +746,11 @@ int launch_conv(const void *x, int cs_in, int cin_p, const void *w, int kp, cons
                 cudaStream_t s, unsigned int *err, Head hd = Head{}) {
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp, hd};
   const int smem = ConvPipe<BN>::SMEM;
-  static bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(conv3x3_fwd_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
-      return STRM_NN_ERR_CUDA;
-    configured = true;
-  }
+  // once per instantiation (thread-safe static initialisation)
+  static const bool configured =
+      cudaFuncSetAttribute(conv3x3_fwd_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) == cudaSuccess;
+  if (!configured) return STRM_NN_ERR_CUDA;
   const long long npix = (long long)batch * h * width;
   if (npix + GM >= (1LL << 31)) return STRM_NN_ERR_INVALID;
   const unsigned int grid = (unsigned int)((npix + GM - 1) / GM);
@@ -797,6 +795,44 @@ bool tma_conv_applies(int cin_p, int width, int cs_in, const void *x) {
          cs_in % 8 == 0 && (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
 }
 
+// Device limits of a TMA-fed instantiation, queried once (thread-safe
+// static initialisation; the kernel's shared-memory attributes are set
+// there too): SMs, shared memory per SM, per CTA (opt-in) and reserved per
+// CTA, the kernel's static shared memory.
+struct TmaLimits {
+  int ok, nsm, smem_sm, smem_blk, reserved, stat;
+};
+
+template <int BN, int CH, bool ROWS>
+TmaLimits tma_limits() {
+  static const TmaLimits lim = [] {
+    TmaLimits l{0, 0, 0, 0, 0, 0};
+    int dev = 0;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&l.smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&l.smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&l.reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&l.nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, conv3x3_fwd_tma_kernel<BN, CH, ROWS>) != cudaSuccess)
+      return l;
+    l.stat = (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             l.smem_blk - l.stat) != cudaSuccess ||
+        cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+      return l;
+    l.ok = 1;
+    return l;
+  }();
+  return lim;
+}
+
 template <int BN, int CH, bool ROWS>
 int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
                     const float *bias, void *y, float *y32, int cs_out, int batch, int h,
@@ -830,31 +866,10 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
     return -1;
   if (CH == 8 && (reinterpret_cast<uintptr_t>(w) & 15u) != 0) return -1;
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp, hd};
-  // device limits, once per instantiation: shared memory per SM, per CTA
-  // (opt-in) and reserved per CTA, the kernel's static shared memory
-  static int nsm = 0, smem_sm = 0, smem_blk = 0, reserved = 0, stat = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaFuncAttributes fa{};
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
-            cudaSuccess ||
-        cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
-            cudaSuccess ||
-        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
-            cudaSuccess ||
-        cudaFuncGetAttributes(&fa, conv3x3_fwd_tma_kernel<BN, CH, ROWS>) != cudaSuccess)
-      return STRM_NN_ERR_CUDA;
-    stat = (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem_blk - stat) != cudaSuccess ||
-        cudaFuncSetAttribute(conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
-                             cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      return STRM_NN_ERR_CUDA;
-  }
+  const TmaLimits lim = tma_limits<BN, CH, ROWS>();
+  if (!lim.ok) return STRM_NN_ERR_CUDA;
+  const int nsm = lim.nsm, smem_sm = lim.smem_sm, smem_blk = lim.smem_blk,
+            reserved = lim.reserved, stat = lim.stat;
   // CTAs per SM: the tuned count (TMEM holds 512 columns per SM), and the
   // ring that fills each CTA's share of the SM's shared memory
   const int tiles = g_tma_tiles.load();  // tiles per CTA, 0: by the layer's size
@@ -876,13 +891,18 @@ int launch_conv_tma(const void *x, int cs_in, int cin_p, const void *w, int kp,
   if (tuned > 0 && tuned < stages) stages = tuned;
   if (stages < 2) return -1;
   const int dyn = stages * P::STAGE + P::B_CONST + 1024;
-  static int fit_dyn = -1, fit = 0;  // CTAs per SM at the last ring size asked
-  if (dyn != fit_dyn) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH, ROWS>, 192,
-                                                      dyn) != cudaSuccess ||
+  // CTAs per SM at the last ring size asked: (dyn << 32) | fit, one atomic
+  // word (concurrent callers store the same value for the same size)
+  static std::atomic<unsigned long long> fit_cache{0};
+  unsigned long long fc = fit_cache.load(std::memory_order_relaxed);
+  int fit = (int)(fc & 0xFFFFFFFFu);
+  if ((int)(fc >> 32) != dyn || fit < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, conv3x3_fwd_tma_kernel<BN, CH, ROWS>,
+                                                      192, dyn) != cudaSuccess ||
         fit < 1)
       return STRM_NN_ERR_CUDA;
-    fit_dyn = dyn;
+    fit_cache.store(((unsigned long long)dyn << 32) | (unsigned int)fit,
+                    std::memory_order_relaxed);
   }
   if (fit < ctas) ctas = fit;
   const long long npix = (long long)batch * h * width;
@@ -940,13 +960,10 @@ int launch_wgrad(const void *x, int cs_in, int cin_p, int kp, const void *dy, in
                  cudaStream_t s, unsigned int *err) {
   ConvShape sh{batch, h, width, cin_p, cs_in, BN, cs_out, kp};
   const int smem = GM * 128 + BN * 128 + 1024;
-  static bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(conv3x3_wgrad_kernel<BN>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-      return STRM_NN_ERR_CUDA;
-    configured = true;
-  }
+  static const bool configured =
+      cudaFuncSetAttribute(conv3x3_wgrad_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) == cudaSuccess;
+  if (!configured) return STRM_NN_ERR_CUDA;
   const long long npix = (long long)batch * h * width;
   // split the pixel reduction so that the grid fills the GPU
   const int mtiles = (kp + GM - 1) / GM;
