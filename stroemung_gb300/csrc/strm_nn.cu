@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <climits>
 #include <mutex>
 
 #include "../../include/stroemung_nn.h"
@@ -122,18 +123,27 @@ struct ConvShape {
 
 // Epilogue of one 16-channel group of a pixel: bias, ReLU, the store (FP32,
 // BF16 or none) and the fused head's share.
+// Called by all 32 lanes of a warp together, lane l holding pixel q = (a
+// multiple of 32) + l; pixels q >= npix are computed but not stored.
+// PAIRED: BF16 stores of whole 32-byte sectors by lane pairs (below);
+// otherwise each lane stores its own pixel's two 16-byte halves (fewer
+// registers: the 8-channel layer, whose short CTAs gain more from
+// occupancy, measured faster that way).
+template <bool PAIRED = true>
 __device__ __forceinline__ void conv_epilogue16(float *v, int c, const float *bias, int relu,
                                                 __nv_bfloat16 *y, float *y32, long long q,
-                                                const ConvShape &s, float &hs) {
+                                                long long npix, const ConvShape &s, float &hs) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     v[i] += bias ? bias[c + i] : 0.0f;
     if (relu) v[i] = fmaxf(v[i], 0.0f);
   }
   if (y32) {
-    float *dst = y32 + q * s.cs_out + c;
+    if (q < npix) {
+      float *dst = y32 + q * s.cs_out + c;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) dst[i] = v[i];
+      for (int i = 0; i < 16; ++i) dst[i] = v[i];
+    }
     return;
   }
   // BF16 bits of the 16 outputs, two per word (channel 2i in the low half)
@@ -142,10 +152,30 @@ __device__ __forceinline__ void conv_epilogue16(float *v, int c, const float *bi
   for (int i = 0; i < 8; ++i)
     pk[i] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * i])) |
             ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * i + 1])) << 16);
-  if (y) {
-    uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
-    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  if (y && !PAIRED) {
+    if (q < npix) {
+      uint4 *dst = reinterpret_cast<uint4 *>(y + q * s.cs_out + c);
+      dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+  } else if (y) {
+    // The two lanes of a pair store one pixel's 32 bytes (16 channels) with
+    // one instruction, whole 32-byte sectors: first the even pixel (its
+    // low half from the even lane, its high half handed to the odd lane),
+    // then the odd pixel (its low half handed to the even lane).
+    const uint4 lo = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    const uint4 hi = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    const bool odd = (threadIdx.x & 1) != 0;
+    const uint4 snd = odd ? lo : hi;
+    uint4 got;
+    got.x = __shfl_xor_sync(0xffffffffu, snd.x, 1);
+    got.y = __shfl_xor_sync(0xffffffffu, snd.y, 1);
+    got.z = __shfl_xor_sync(0xffffffffu, snd.z, 1);
+    got.w = __shfl_xor_sync(0xffffffffu, snd.w, 1);
+    const long long pe = odd ? q - 1 : q, po = pe + 1;
+    const int half = odd ? 8 : 0;  // elements
+    if (pe < npix) *reinterpret_cast<uint4 *>(y + pe * s.cs_out + c + half) = odd ? got : lo;
+    if (po < npix) *reinterpret_cast<uint4 *>(y + po * s.cs_out + c + half) = odd ? hi : got;
   }
   if (s.hd.q) {
     // the BF16 value as FP32: its bits in the high half
@@ -302,7 +332,7 @@ __global__ void __launch_bounds__(160)
       for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-        if (q < npix) conv_epilogue16(v, c, bias, relu, y, y32, q, s, hs);
+        conv_epilogue16(v, c, bias, relu, y, y32, q, npix, s, hs);
       }
       if (s.hd.q && q < npix) s.hd.q[q] = hs;
     } else {
@@ -549,7 +579,7 @@ __global__ void __launch_bounds__(192)
       for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * BN + c), v);
-        conv_epilogue16(v, c, bias, relu, y, y32, q, s, hs);
+        conv_epilogue16<CH != 8>(v, c, bias, relu, y, y32, q, LLONG_MAX, s, hs);
       }
       if (s.hd.q) s.hd.q[q] = hs;
       // the accumulator may be overwritten once all four warps have read it
