@@ -362,8 +362,10 @@ __global__ void __launch_bounds__(160)
 //     NACC accumulators in TMEM, committed to the stage's "empty" barrier,
 //     and the tile's last commit to its accumulator's "full" barrier;
 //   epilogue (warps 0-3): reads a finished accumulator, adds the bias,
-//     applies the ReLU, stores BF16 (or FP32), and hands the accumulator
-//     back, so that it overlaps the next tile's loads and MMAs.
+//     applies the ReLU, stores BF16 (lane pairs writing whole 32-byte
+//     sectors; or FP32) and, for the last layer, the 1x1 head, and hands
+//     the accumulator back, so that it overlaps the next tile's loads and
+//     MMAs.
 // Every wait is bounded; a role whose wait runs out flags the CTA and stops,
 // the producer still waits (bounded) for the copies it issued, and the CTA
 // releases its TMEM.
@@ -798,8 +800,8 @@ std::atomic<int> g_conv_tma{1};
 // CTA (0: four while the layer still fills every CTA slot of the GPU once,
 // else two, else one — measured at 4096 x 1024: many short CTAs per SM hide
 // the TMA latency, and a few tiles per CTA spread its set-up; CTAs walking
-// all tiles persistently were slower on every layer), and row boxes for
-// 32-channel slices.
+// all tiles persistently were slower on every layer), and row boxes of
+// 32-channel slices for tiles of up to 128 output channels.
 std::atomic<int> g_tma_ctas{0}, g_tma_stages{0}, g_tma_tiles{0}, g_tma_rows{1};
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
