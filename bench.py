@@ -568,6 +568,17 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
     f1.record()
     torch.cuda.synchronize()
     fwd_ms = f0.elapsed_time(f1) / 3
+    # the prediction's forward as the warm start runs it (recorded once as a
+    # CUDA graph and replayed: no activation kept for a backward, the last
+    # layer's outputs not stored, no host work between the launches)
+    net.forward_graphed(x, 1, IMAX, JMAX)
+    torch.cuda.synchronize()
+    f0.record()
+    for _ in range(3):
+        net.forward_graphed(x, 1, IMAX, JMAX)
+    f1.record()
+    torch.cuda.synchronize()
+    pred_fwd_ms = f0.elapsed_time(f1) / 3
     flops = 0.0
     pixel_scale = [1, 1, 4, 4, 16, 16, 64, 64, 16, 16, 4, 4, 1, 1]  # pixels per layer: 1/scale
     for l, sc in zip(net.layers(), pixel_scale):
@@ -635,7 +646,14 @@ def learned_block(args, grid, fp64_ms_step, mixed_ms_step):
                                          "sweeps_to_plain_norm")} for r in rows],
         "cnn": {"forward_ms_at_workload": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9,
                 "tensor_frac_of_measured_bf16": (flops / fwd_ms / 1e9) / BF16_PEAK,
-                "params": net.parameter_count()},
+                "prediction_forward_ms": pred_fwd_ms,
+                "prediction_tensor_frac_of_measured_bf16": (flops / pred_fwd_ms / 1e9) /
+                BF16_PEAK,
+                "params": net.parameter_count(),
+                "note": "forward_ms_at_workload: forward() keeping every activation for a "
+                        "backward, host calls between the launches; prediction_forward_ms: the "
+                        "warm start's recorded forward graph, storing no activation it does not "
+                        "read"},
         "training": train_info,
         "judge_sweeps": args.ws_judge_sweeps,
         "note": "the reference stop rule runs 2000 sweeps in every step of this workload, so no "
