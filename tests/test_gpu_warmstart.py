@@ -313,6 +313,26 @@ def test_recorded_forward_equals_forward():
     assert torch.equal(net.forward_graphed(x, 1, 64, 48).clone(), want)
 
 
+def test_prediction_forward_equals_training_forward_on_tma_layers():
+    """At a size whose full-resolution layers take the TMA-fed convolutions
+    (rows of whole 128-pixel tiles), the prediction's forward (no
+    activations kept; the last layer's outputs not stored, the head fused
+    into its epilogue) gives the bits of the training forward, which stores
+    every activation, and its recorded graph the same again."""
+    import torch
+    net, _ = _net_with_random_head(seed=5)
+    g = torch.Generator(device="cuda").manual_seed(8)
+    x = torch.randn(2, 64, 256, 8, device="cuda", generator=g).to(torch.bfloat16)
+    keep = net.forward(x, 2, 64, 256, keep=True).clone()
+    pred = net.forward(x, 2, 64, 256, keep=False).clone()
+    assert torch.isfinite(keep).all()
+    assert torch.equal(pred, keep)
+    x1 = x[:1].contiguous()
+    want = net.forward(x1, 1, 64, 256, keep=True).clone()
+    assert torch.equal(net.forward_graphed(x1, 1, 64, 256).clone(), want)
+    assert torch.equal(want, keep[:1])
+
+
 @pytest.mark.parametrize("sweeps", [0, 4])
 def test_judge_matches_the_phase_entry_points(sweeps):
     """strm_judge_correction, its launches recorded as one CUDA graph, gives
