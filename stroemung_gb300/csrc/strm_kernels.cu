@@ -16,7 +16,8 @@
 //     sor_red_res_kernel    red pass of the next iteration + this one's
 //                           residual of the red cells, norm, stop test;
 //                           copies the red-coloured boundary cells
-//   sor_rollback_kernel  undoes the next iteration's copy and red pass
+//   sor_unred_kernel, sor_rollback_kernel  undo the next iteration's red
+//                        pass and copy
 //   mixed precision: FP32 sweeps with FP64 refinement (see the mixed solve)
 //   prange_kernel    pressure range when the solve ran out of iterations
 //   velocity_kernel  velocity update + restore + max|u|,|v| + speed range + time
@@ -1175,9 +1176,11 @@ __global__ void __launch_bounds__(256)
 // them, and the red pass reads the copied cells in the stencils of the red
 // fluid cells next to them (class 1) and of the red-coloured non-fluid
 // interior cells from pw.  The stop itself: when iteration k stops the
-// solve, the red pass and the copy of k+1 have run; both saved what they
-// overwrote (in pw), and sor_rollback_kernel puts it back, so the solve
-// ends on iteration k's pressure, boundary values included.  Iteration
+// solve, the red pass and the copy of k+1 have run; the copy saved what it
+// overwrote (in pw), and so did the red pass when omega is near 1; for
+// other omega sor_unred_kernel inverts the red pass instead, and
+// sor_rollback_kernel puts the saved values back, so the solve ends on
+// iteration k's pressure, boundary values included.  Iteration
 // k+1's red pass and copy run only when k < itermax.
 // Per iteration: black pass (+ its residual, the save and half the copy)
 // and red pass (+ the other half, the red residual and the stop test),
@@ -1288,7 +1291,10 @@ __device__ __forceinline__ void solve_iteration_done_snap(StepState *st, const S
 // red-coloured cell, and the residuals here read copied cells from pw).  The
 // last block adds the black pass's sums and applies the stop test of
 // iteration k.
-template <bool IN_GRAPH, bool MEAN_FREE, bool ALL>
+// SAVE: the red cells' values before the update go to pw for the rollback;
+// without it the rollback inverts the update instead (sor_unred_kernel),
+// saving the pass 8 bytes of writes per red cell.
+template <bool IN_GRAPH, bool MEAN_FREE, bool ALL, bool SAVE = true>
 __global__ void __launch_bounds__(256, 4)
     sor_red_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                        const double *__restrict__ rhs, const uint8_t *__restrict__ cls, Geom g,
@@ -1355,7 +1361,7 @@ __global__ void __launch_bounds__(256, 4)
         if (MEAN_FREE) acc1 += rk;
       }
       if (write) {
-        if (sum) pw[cells.o[u]] = pc[u];
+        if (sum && SAVE) pw[cells.o[u]] = pc[u];
         p[cells.o[u]] = fma(c.middle, r, pc[u]);
       }
     }
@@ -1379,9 +1385,10 @@ __global__ void __launch_bounds__(256, 4)
 __global__ void __launch_bounds__(256)
     sor_rollback_kernel(double *__restrict__ p, const double *__restrict__ pw,
                         const uint8_t *__restrict__ cls, const PCopy *__restrict__ pc, int npc,
-                        Geom g, const StepState *st, unsigned int itermax, int gx, int nvb) {
+                        Geom g, const StepState *st, unsigned int itermax, int gx, int nvb,
+                        int red_saved) {
   if (!(st->converged && st->sor_iters < itermax)) return;
-  for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+  for (int vb = blockIdx.x; red_saved && vb < nvb; vb += gridDim.x) {
     const int x = 1 + (vb / gx) * blockDim.y + threadIdx.y;
     const int y = 2 * ((vb % gx) * blockDim.x + threadIdx.x) + (x & 1);
     if (x > g.nx - 2 || y < 1 || y > g.ny - 2) continue;
@@ -1392,6 +1399,36 @@ __global__ void __launch_bounds__(256)
   for (int k = blockIdx.x * nt + threadIdx.x + threadIdx.y * blockDim.x; k < npc;
        k += gridDim.x * nt)
     p[pc[k].off] = pw[pc[k].off];
+}
+
+// The rollback of a red pass that did not save (sor_red_res_kernel, SAVE
+// false): every red cell it updated (classes 0 and 1) gets its old value
+// back from the update itself.  The pass computed
+//   t = (pe + pw)/dx^2 + (ps + pn)/dy^2 - rhs,  r = t - 2(1/dx^2+1/dy^2) p,
+//   p' = p + omega / (2(1/dx^2+1/dy^2)) r = (1 - omega) p + middle t,
+// from black neighbours (and copied cells) that nothing has changed since,
+// so t is recomputed bit for bit and p = (p' - middle t) / (1 - omega),
+// within a few units in the last place of p' and middle t, amplified by at
+// most 1 / |1 - omega| (the graph builder keeps the saving pass for
+// |1 - omega| < 0.5).  It runs before the copied cells are restored (their
+// restored values are not the ones the red pass read).
+__global__ void __launch_bounds__(256)
+    sor_unred_kernel(double *__restrict__ p, const double *__restrict__ rhs,
+                     const uint8_t *__restrict__ cls, Geom g, Consts c, const StepState *st,
+                     unsigned int itermax, int gx, int nvb) {
+  if (!(st->converged && st->sor_iters < itermax)) return;
+  const double inv = 1.0 / c.one_minus_w;
+  for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
+    const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 0, g);
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      const size_t o = cells.o[u];
+      if (!cells.ok[u] || (cls[o] & 3u) >= CLS_OTHER) continue;
+      const double t = fma(p[o + g.pitch] + p[o - g.pitch], c.r_dx2,
+                           fma(p[o + 1] + p[o - 1], c.r_dy2, -rhs[o]));
+      p[o] = fma(-c.middle, t, p[o]) * inv;
+    }
+  }
 }
 
 // Lexicographic Gauss-Seidel SOR in one CTA, bit-identical to the reference
@@ -2499,28 +2536,40 @@ int black_pass_blocks(const Geom &g) {
   return n < 1 ? 1 : (int)n;
 }
 
-// Kernel choices of the FAST red-black solve for a stop-rule setting.
+// Kernel choices of the FAST red-black solve for a stop-rule setting and
+// relaxation factor: the red pass saves the values it overwrites only when
+// omega is near 1 (|1 - omega| < 0.5); otherwise the rollback inverts it.
 struct FastSolveKernels {
   const void *red_graph, *red_eager, *black;
+  bool save;
 };
 
-static FastSolveKernels fast_solve_kernels(int strict) {
+template <bool SAVE>
+static void fast_red_kernels(FastSolveKernels &k, bool mf, bool fluid) {
+  if (mf) {
+    k.red_graph = (const void *)sor_red_res_kernel<true, true, false, SAVE>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, true, false, SAVE>;
+  } else if (fluid) {
+    k.red_graph = (const void *)sor_red_res_kernel<true, false, false, SAVE>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, false, false, SAVE>;
+  } else {
+    k.red_graph = (const void *)sor_red_res_kernel<true, false, true, SAVE>;
+    k.red_eager = (const void *)sor_red_res_kernel<false, false, true, SAVE>;
+  }
+}
+
+static FastSolveKernels fast_solve_kernels(int strict, double one_minus_w) {
   const bool fluid = (strict & STOP_FLUID_NORM) != 0;
   const bool mf = fluid && (strict & STOP_MEAN_FREE) != 0;
   FastSolveKernels k;
-  if (mf) {
-    k.black = (const void *)sor_black_res_kernel<true, false>;
-    k.red_graph = (const void *)sor_red_res_kernel<true, true, false>;
-    k.red_eager = (const void *)sor_red_res_kernel<false, true, false>;
-  } else if (fluid) {
-    k.black = (const void *)sor_black_res_kernel<false, false>;
-    k.red_graph = (const void *)sor_red_res_kernel<true, false, false>;
-    k.red_eager = (const void *)sor_red_res_kernel<false, false, false>;
-  } else {
-    k.black = (const void *)sor_black_res_kernel<false, true>;
-    k.red_graph = (const void *)sor_red_res_kernel<true, false, true>;
-    k.red_eager = (const void *)sor_red_res_kernel<false, false, true>;
-  }
+  k.black = mf      ? (const void *)sor_black_res_kernel<true, false>
+            : fluid ? (const void *)sor_black_res_kernel<false, false>
+                    : (const void *)sor_black_res_kernel<false, true>;
+  k.save = fabs(one_minus_w) < 0.5;
+  if (k.save)
+    fast_red_kernels<true>(k, mf, fluid);
+  else
+    fast_red_kernels<false>(k, mf, fluid);
   return k;
 }
 
@@ -2933,7 +2982,7 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
     if (r.arith) {
       // fast arithmetic: the red pass of iteration k+1 finishes iteration k's
       // norm (see sor_red_res_kernel); the same launches as the graph
-      const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
+      const FastSolveKernels fk = fast_solve_kernels(r.strict_eps, c.one_minus_w);
       const int bb = black_pass_blocks(g);
       int gx = (int)sgrid.x;
       unsigned int itermax = r.itermax;
@@ -2966,8 +3015,11 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
           return e;
         if ((e = poll_done(d, s, h, &done)) != cudaSuccess) return e;
       }
+      if (!fk.save)
+        sor_unred_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.rhs, d.cls, g, c, d.st, r.itermax, gx,
+                                                  nbb);
       sor_rollback_kernel<<<bb, kRedBlock, 0, s>>>(d.p, d.pw, d.cls, d.pcopy, d.n_pcopy, g, d.st,
-                                                   r.itermax, gx, nbb);
+                                                   r.itermax, gx, nbb, fk.save ? 1 : 0);
     }
     while (!done) {
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
@@ -3213,7 +3265,7 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                (g.nx - 2 + kRedBlock.y - 1) / kRedBlock.y);
     const int nbb = (int)(sgrid.x * sgrid.y);
     const int bb = black_pass_blocks(g);
-    const FastSolveKernels fk = fast_solve_kernels(r.strict_eps);
+    const FastSolveKernels fk = fast_solve_kernels(r.strict_eps, c.one_minus_w);
     if (r.arith) {
       // fast arithmetic: first copy and red pass outside the loop; the red
       // pass of iteration k+1 finishes iteration k's norm (sor_red_res_kernel)
@@ -3261,10 +3313,15 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       }
     }
     n = wnode;
+    if (r.arith && !fk.save)
+      n = b.kernel(b.graph, n, (const void *)sor_unred_kernel, dim3(bb), kRedBlock, d.p,
+                   (const double *)d.rhs, (const uint8_t *)d.cls, g, c, (const StepState *)d.st,
+                   r.itermax, (int)sgrid.x, nbb);
     if (r.arith)
       n = b.kernel(b.graph, n, (const void *)sor_rollback_kernel, dim3(bb), kRedBlock, d.p,
                    (const double *)d.pw, (const uint8_t *)d.cls, (const PCopy *)d.pcopy,
-                   d.n_pcopy, g, (const StepState *)d.st, r.itermax, (int)sgrid.x, nbb);
+                   d.n_pcopy, g, (const StepState *)d.st, r.itermax, (int)sgrid.x, nbb,
+                   fk.save ? 1 : 0);
   }
   if (part != 1) {
     n = b.kernel(b.graph, n, (const void *)prange_kernel, dim3(nb), kRedBlock,

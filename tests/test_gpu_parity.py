@@ -208,10 +208,11 @@ def test_random_layouts_all_boundary_kinds(seed):
     assert_fields_equal(o2, s2, "red-black after 5 steps")
 
 
+@pytest.mark.parametrize("omega", [1.6, 1.2])
 @pytest.mark.parametrize("seed", range(6))
 @pytest.mark.parametrize("strict,eps", [(False, 1e-3), (True, 1e-3), (True, 100.0)],
                          ids=["reference_rule", "to_itermax", "strict_eps_100"])
-def test_random_layouts_fast_red_black(seed, strict, eps):
+def test_random_layouts_fast_red_black(seed, strict, eps, omega):
     """The FAST red-black solve on random layouts with every boundary kind:
     its boundary copy is split by the colour of the copied cell between the
     black and the red passes, the residuals next to boundary cells read the
@@ -221,7 +222,9 @@ def test_random_layouts_fast_red_black(seed, strict, eps):
     or two iterations (a rollback each step), strict eps 1e-3 runs every
     solve to max_iterations, strict eps 100 stops some solves in between.
     Against the oracle's red-black order: the same iteration counts, norms
-    and fields within 1e-9; eager launches bit-identical to the graph."""
+    and fields within 1e-9; eager launches bit-identical to the graph.
+    omega 1.6 rolls the red pass back by inverting it, omega 1.2 (near 1,
+    where the inverse would amplify rounding) from the values it saved."""
     from stroemung_gb300.simulation import ARITH_FAST
     from tests.test_host_boundary import random_layout
     rng = np.random.default_rng(200 + seed)
@@ -239,7 +242,7 @@ def test_random_layouts_fast_red_black(seed, strict, eps):
     g["v"] = rng.normal(size=(nx, ny))
     g["p"] = rng.normal(size=(nx, ny))
     prm = dict(cell_size=(0.1, 0.07), delt=0.002, gamma=0.8, reynolds=50.0, eps=eps,
-               max_iterations=60, omega=1.6)
+               max_iterations=60, omega=omega)
     mode = {"sor_order": 0, "arithmetic": ARITH_FAST}
     o, s = make_pair(g, orc_order=orc.RED_BLACK, gpu_mode=mode, strict_eps=strict, **prm)
     _, e = make_pair(g, orc_order=orc.RED_BLACK, gpu_mode=dict(mode, execution=1),
