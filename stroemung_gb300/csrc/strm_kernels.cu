@@ -818,8 +818,10 @@ __global__ void __launch_bounds__(256)
 // a time and issues every load of those cells (class byte, the five
 // pressures, rhs) before it uses one: the pressure loads do not wait for the
 // class byte, and several cells' loads are in flight.  The FP64 pipe is the
-// bound; memory latency is what keeps it idle.
-constexpr int kPassUnroll = 2;
+// bound; memory latency is what keeps it idle.  Three cells per batch
+// measured 0.8 % faster per step than two (a few dozen bytes of the red
+// pass spill at its 64-register bound), four 11 % slower.
+constexpr int kPassUnroll = 3;
 
 struct PassCells {
   size_t o[kPassUnroll];
