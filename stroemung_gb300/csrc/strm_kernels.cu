@@ -916,6 +916,8 @@ __global__ void __launch_bounds__(256)
                          Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
                          const BCell *__restrict__ bl, int nbl_b, int nbl, const StepState *st,
                          unsigned int itermax) {
+  // a later iteration of a WHILE body whose solve has stopped: nothing to do
+  if (st->converged | st->exhausted) return;
   double accl = 0.0;  // residuals of the listed cells (ALL only, never MEAN_FREE)
   {
     const int nt = blockDim.x * blockDim.y;
@@ -1304,6 +1306,8 @@ __global__ void __launch_bounds__(256, 4)
                        const double *partials_b, int nbb, const BCell *__restrict__ bl,
                        int nbl_b, int nbl, int gx, int nvb, unsigned int itermax, int strict,
                        int mode, cudaGraphConditionalHandle h) {
+  // a later iteration of a WHILE body whose solve has stopped: nothing to do
+  if (mode == 1 && (st->converged | st->exhausted)) return;
   const bool sum = mode == 1;
   const bool write = !sum || st->sor_iters + 1 < itermax;
   __shared__ SolveSnap sn;  // written and read by thread 0 only
@@ -2538,6 +2542,13 @@ int black_pass_blocks(const Geom &g) {
   return n < 1 ? 1 : (int)n;
 }
 
+// Iterations of the FAST red-black solve per body of its WHILE node: each
+// evaluation of the condition costs a few microseconds between the body's
+// kernels (measured per step at 2000 iterations: 2 per body -1.5 %, 4
+// -3.8 %, 8 -4.6 %); a body that stops early runs the remaining passes as
+// launches that return at once.
+constexpr int kFastBodyIters = 8;
+
 // Kernel choices of the FAST red-black solve for a stop-rule setting and
 // relaxation factor: the red pass saves the values it overwrites only when
 // omega is near 1 (|1 - omega| < 0.5); otherwise the rollback inverts it.
@@ -3291,14 +3302,19 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       cudaGraphNode_t bn = nullptr;
       if (r.arith) {
-        bn = b.kernel(body, nullptr, fk.black, dim3(bb), kRedBlock, d.p, d.pw,
-                      (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
-                      (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
-                      (const StepState *)d.st, r.itermax);
-        bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
-                      (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st, d.partials_r,
-                      (const double *)d.partials_b, bb, (const BCell *)d.blist, d.n_blist_b,
-                      d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
+        // kFastBodyIters iterations per evaluation of the WHILE condition;
+        // the passes after the one that stopped the solve return at once
+        for (int i = 0; i < kFastBodyIters; ++i) {
+          bn = b.kernel(body, bn, fk.black, dim3(bb), kRedBlock, d.p, d.pw,
+                        (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
+                        (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
+                        (const StepState *)d.st, r.itermax);
+          bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
+                        (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st,
+                        d.partials_r, (const double *)d.partials_b, bb, (const BCell *)d.blist,
+                        d.n_blist_b, d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1,
+                        h);
+        }
       } else {
         if (d.n_pcopy > 0)
           bn = b.kernel(body, nullptr, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
