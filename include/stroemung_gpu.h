@@ -343,6 +343,13 @@ int strm_residual_history(strm_sim *sim, double *out, int cap, int *n);
  * not depend on the schedule.  No reference counterpart. */
 int strm_autotune_sweeps(strm_sim *sim, int reps, int *best, double *ms_per_sweep);
 
+/* Process-wide: whether the step graphs built from now on chain the colour
+ * passes of the FAST red-black loop body by programmatic dependent launch
+ * (on = 1, the default) or by plain graph edges (0); a graph that a driver
+ * refuses to build with them is built without them.  Results do not depend
+ * on it.  Returns the previous setting.  No reference counterpart. */
+int strm_set_programmatic_launch(int on);
+
 /* Residual norm that allocates nothing.  No counterpart in the reference.
  * For callers that must not allocate device memory once they are running:
  * host frameworks whose caching allocator owns the device budget (a

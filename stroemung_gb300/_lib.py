@@ -105,6 +105,7 @@ SIGNATURES = {
     "strm_tick_solve": [_vp, ctypes.POINTER(ctypes.c_uint32), _dp],
     "strm_export_planes": [_vp, _vp, _vp, _vp],
     "strm_autotune_sweeps": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
+    "strm_set_programmatic_launch": [ctypes.c_int],
     "strm_residual_history": [_vp, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "strm_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                           ctypes.POINTER(ctypes.c_void_p)],

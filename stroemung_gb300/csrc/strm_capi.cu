@@ -157,15 +157,31 @@ void destroy_graphs(strm_sim *s) {
   }
 }
 
+static cudaError_t build_graphs(strm_sim *s) {
+  cudaGraphExec_t *ex[3] = {&s->exec, &s->exec_pre, &s->exec_post};
+  cudaGraph_t *gr[3] = {&s->graph, &s->graph_pre, &s->graph_post};
+  for (int part = 0; part < 3; ++part) {
+    cudaError_t e = build_step_graph(s->d, s->cfg, gr[part], part);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(ex[part], *gr[part], 0);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 int rebuild_graph(strm_sim *s) {
   destroy_graphs(s);
   update_cfg(s);
-  CK(build_step_graph(s->d, s->cfg, &s->graph, 0));
-  CK(cudaGraphInstantiate(&s->exec, s->graph, 0));
-  CK(build_step_graph(s->d, s->cfg, &s->graph_pre, 1));
-  CK(cudaGraphInstantiate(&s->exec_pre, s->graph_pre, 0));
-  CK(build_step_graph(s->d, s->cfg, &s->graph_post, 2));
-  CK(cudaGraphInstantiate(&s->exec_post, s->graph_post, 0));
+  cudaError_t e = build_graphs(s);
+  if (e != cudaSuccess && fast_pdl()) {
+    // a driver that refuses programmatic edges inside the solve's loop body:
+    // build without them, and keep them off if that is what made it work
+    destroy_graphs(s);
+    (void)cudaGetLastError();
+    set_fast_pdl(0);
+    e = build_graphs(s);
+    if (e != cudaSuccess) set_fast_pdl(1);
+  }
+  CK(e);
   return STRM_OK;
 }
 
@@ -1117,6 +1133,8 @@ int strm_residual_history(strm_sim *s, double *out, int cap, int *n) {
   }
   return STRM_OK;
 }
+
+int strm_set_programmatic_launch(int on) { return set_fast_pdl(on); }
 
 int strm_autotune_sweeps(strm_sim *s, int reps, int *best, double *ms_per_sweep) {
   if (!s || reps < 1) return fail(STRM_ERR_INVALID, "invalid arguments");

@@ -49,6 +49,18 @@ constexpr int RT_Y = 64;
 
 __device__ __forceinline__ double sqd(double x) { return x * x; }
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later).  A
+// colour pass of the FAST solve's loop body starts with both: the trigger
+// lets the next pass's blocks be placed on the SMs as this pass's blocks
+// finish, instead of after the whole grid has completed and the next launch
+// has been processed; the wait holds each block until the previous pass has
+// completed and its writes are visible.  Launched without a programmatic
+// edge (eager launches, graphs built without them) both do nothing.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Load of a buffer that other CTAs of the same launch may have written
 // earlier (the persistent batch solve): COH reads it at L2 (ld.global.cg),
 // never through the read-only path; otherwise a plain load.
@@ -117,6 +129,26 @@ __device__ double block_reduce(double v, Op op, double identity) {
 // it (acquire of the others'); the barrier then orders the block's reads.
 // The other threads' stores (field updates) need no fence here: nothing
 // reads them before the kernel ends.
+// The same with one acquire-release atomic in place of the two full fences
+// around a relaxed one: the ticket releases the partial that thread 0 stored
+// before it, and the last block's thread 0 acquires every other block's
+// (its threads then read them at L2 after the barrier).  Only for blocks
+// whose thread 0 stored everything the last block reads.
+__device__ __forceinline__ bool last_block_done_t0(unsigned int *counter) {
+  __shared__ bool am_last;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "l"(counter)
+                 : "memory");
+    am_last = old == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  return am_last;
+}
+
 __device__ __forceinline__ bool last_block_done(unsigned int *counter) {
   __shared__ bool am_last;
   __syncthreads();
@@ -916,6 +948,8 @@ __global__ void __launch_bounds__(256)
                          Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
                          const BCell *__restrict__ bl, int nbl_b, int nbl, const StepState *st,
                          unsigned int itermax) {
+  pdl_trigger();
+  pdl_wait();
   // a later iteration of a WHILE body whose solve has stopped: nothing to do
   if (st->converged | st->exhausted) return;
   double accl = 0.0;  // residuals of the listed cells (ALL only, never MEAN_FREE)
@@ -1191,50 +1225,56 @@ __global__ void __launch_bounds__(256)
 // instead of copy, red, black, residual.
 // ------------------------------------------------------------------------
 
-
+// The sum of the red pass's partials (each already holding the black
+// pass's partial of the same block index), on the critical path of every
+// iteration: the grid waits for this one block.  Each thread loads up to
+// four entries at once and adds them as a tree, then a tree over the block
+// (one shared-memory level, then one warp's additions and shuffles); with
+// partials of both passes and running sums this block took 2.6 us per
+// iteration, 1.3 us as trees.  Fixed order (deterministic); blocks of 256
+// threads; entries past 768 (grids above 3 blocks per thread) are added to
+// the first slot.  s2 = sum r^2, s1 = sum r (when MEAN_FREE); valid in
+// thread 0.
 template <bool MEAN_FREE>
-__device__ __forceinline__ void store_sums(double acc, double acc1, double *partials) {
-  block_sum_pass<MEAN_FREE>(acc, acc1);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    if (MEAN_FREE) {
-      partials[2 * blockIdx.x] = acc;
-      partials[2 * blockIdx.x + 1] = acc1;
-    } else {
-      partials[blockIdx.x] = acc;
-    }
-  }
-}
-
-// The sums of the black pass's and the red pass's partials: each thread
-// adds its entries of the two arrays in that order, then one block sum —
-// one chain of loads and one barrier pair on the critical path of the
-// iteration.  s2 = sum r^2, s1 = sum r (when mean_free); valid in thread 0.
-__device__ __forceinline__ void sum_partials_passes(const double *pa, int na, const double *pb,
-                                                    int nb, bool mean_free, double &s2,
+__device__ __forceinline__ void sum_partials_passes(const double *pr, int n, double &s2,
                                                     double &s1) {
+  constexpr int kNt = 256;
+  constexpr int W = MEAN_FREE ? 2 : 1;
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  const int nt = blockDim.x * blockDim.y;
+  double v[3], w[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const int k = tid + j * kNt;
+    v[j] = k < n ? __ldcg(pr + W * k) : 0.0;
+    if (MEAN_FREE) w[j] = k < n ? __ldcg(pr + W * k + 1) : 0.0;
+  }
+  for (int k = tid + 3 * kNt; k < n; k += kNt) {
+    v[0] += __ldcg(pr + W * k);
+    if (MEAN_FREE) w[0] += __ldcg(pr + W * k + 1);
+  }
+  __shared__ double sa[kNt];
+  __shared__ double sb[MEAN_FREE ? kNt : 1];
+  sa[tid] = (v[0] + v[1]) + v[2];
+  if (MEAN_FREE) sb[tid] = (w[0] + w[1]) + w[2];
+  __syncthreads();
+  if (tid < 128) {
+    sa[tid] += sa[tid + 128];
+    if (MEAN_FREE) sb[tid] += sb[tid + 128];
+  }
+  __syncthreads();
   s2 = 0.0;
   s1 = 0.0;
-  if (!mean_free) {
-#pragma unroll 4
-    for (int k = tid; k < na; k += nt) s2 += __ldcg(pa + k);
-#pragma unroll 4
-    for (int k = tid; k < nb; k += nt) s2 += __ldcg(pb + k);
-    block_sum_pass<false>(s2, s1);
-    return;
+  if (tid < 32) {
+    double x = (sa[tid] + sa[tid + 64]) + (sa[tid + 32] + sa[tid + 96]);
+    double y = MEAN_FREE ? (sb[tid] + sb[tid + 64]) + (sb[tid + 32] + sb[tid + 96]) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (MEAN_FREE) y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    s2 = x;
+    s1 = y;
   }
-#pragma unroll 4
-  for (int k = tid; k < na; k += nt) {
-    s2 += __ldcg(pa + 2 * k);
-    s1 += __ldcg(pa + 2 * k + 1);
-  }
-#pragma unroll 4
-  for (int k = tid; k < nb; k += nt) {
-    s2 += __ldcg(pb + 2 * k);
-    s1 += __ldcg(pb + 2 * k + 1);
-  }
-  block_sum_pass<true>(s2, s1);
 }
 
 // What the red pass's stop test needs of the step state, loaded by each
@@ -1306,6 +1346,8 @@ __global__ void __launch_bounds__(256, 4)
                        const double *partials_b, int nbb, const BCell *__restrict__ bl,
                        int nbl_b, int nbl, int gx, int nvb, unsigned int itermax, int strict,
                        int mode, cudaGraphConditionalHandle h) {
+  pdl_trigger();
+  pdl_wait();
   // a later iteration of a WHILE body whose solve has stopped: nothing to do
   if (mode == 1 && (st->converged | st->exhausted)) return;
   const bool sum = mode == 1;
@@ -1373,11 +1415,31 @@ __global__ void __launch_bounds__(256, 4)
     }
   }
   if (!sum) return;
-  store_sums<MEAN_FREE>(acc, acc1, partials_r);
+  // the black pass has completed: its partial of this block index joins
+  // this block's, so that the last block sums one array (the two grids are
+  // the same size; a larger black grid's rest would go to the blocks of the
+  // same index modulo this grid).  Thread 0 loads it before the block sum,
+  // which hides the load.
+  double pb2 = 0.0, pb1 = 0.0;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int k = blockIdx.x; k < nbb; k += gridDim.x) {
+      pb2 += __ldcg(partials_b + (MEAN_FREE ? 2 : 1) * k);
+      if (MEAN_FREE) pb1 += __ldcg(partials_b + 2 * k + 1);
+    }
+  }
+  block_sum_pass<MEAN_FREE>(acc, acc1);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (MEAN_FREE) {
+      partials_r[2 * blockIdx.x] = acc + pb2;
+      partials_r[2 * blockIdx.x + 1] = acc1 + pb1;
+    } else {
+      partials_r[blockIdx.x] = acc + pb2;
+    }
+  }
   loop_guard<IN_GRAPH>(st, itermax, h);
-  if (!last_block_done(&st->counter)) return;
+  if (!last_block_done_t0(&st->counter)) return;
   double s2, s1;
-  sum_partials_passes(partials_b, nbb, partials_r, gridDim.x, MEAN_FREE, s2, s1);
+  sum_partials_passes<MEAN_FREE>(partials_r, gridDim.x, s2, s1);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     const double n = sn.fluid_cells;
     const double ns = MEAN_FREE ? (s2 - s1 * (s1 / n)) / n : s2 / n;
@@ -3103,6 +3165,22 @@ struct GraphBuilder {
     return node;
   }
 
+  // the same as kernel(), the edge from dep programmatic: the node's blocks
+  // may start once every block of dep has triggered (pdl_trigger) or ended,
+  // and wait (pdl_wait) for dep's completion themselves
+  template <typename... Args>
+  cudaGraphNode_t kernel_pdl(cudaGraph_t gr, cudaGraphNode_t dep, const void *fn, dim3 grid,
+                             dim3 block, Args... args) {
+    if (!dep) return kernel(gr, dep, fn, grid, block, args...);
+    cudaGraphNode_t node = kernel(gr, nullptr, fn, grid, block, args...);
+    if (err != cudaSuccess) return nullptr;
+    cudaGraphEdgeData ed{};
+    ed.from_port = cudaGraphKernelNodePortProgrammatic;
+    ed.type = cudaGraphDependencyTypeProgrammatic;
+    err = cudaGraphAddDependencies(gr, &dep, &node, &ed, 1);
+    return node;
+  }
+
   template <typename T>
   void *keep(const T &v) {
     store.emplace_back(sizeof(T));
@@ -3111,7 +3189,12 @@ struct GraphBuilder {
   }
 };
 
+std::atomic<int> g_fast_pdl{1};
+
 }  // namespace
+
+int set_fast_pdl(int on) { return g_fast_pdl.exchange(on ? 1 : 0); }
+int fast_pdl() { return g_fast_pdl.load(); }
 
 cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out, int part) {
   GraphBuilder b;
@@ -3303,17 +3386,21 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
       cudaGraphNode_t bn = nullptr;
       if (r.arith) {
         // kFastBodyIters iterations per evaluation of the WHILE condition;
-        // the passes after the one that stopped the solve return at once
+        // the passes after the one that stopped the solve return at once.
+        // Within the body each pass follows the previous one by a
+        // programmatic edge unless switched off (set_fast_pdl)
+        const bool pdl = g_fast_pdl.load() != 0;
+        auto pass = [&](const void *fn, auto... args) {
+          bn = pdl ? b.kernel_pdl(body, bn, fn, dim3(bb), kRedBlock, args...)
+                   : b.kernel(body, bn, fn, dim3(bb), kRedBlock, args...);
+        };
         for (int i = 0; i < kFastBodyIters; ++i) {
-          bn = b.kernel(body, bn, fk.black, dim3(bb), kRedBlock, d.p, d.pw,
-                        (const double *)d.rhs, (const uint8_t *)d.flags, g, c, d.partials_b,
-                        (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
-                        (const StepState *)d.st, r.itermax);
-          bn = b.kernel(body, bn, fk.red_graph, dim3(bb), kRedBlock, d.p, d.pw,
-                        (const double *)d.rhs, (const uint8_t *)d.cls, g, c, d.st,
-                        d.partials_r, (const double *)d.partials_b, bb, (const BCell *)d.blist,
-                        d.n_blist_b, d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1,
-                        h);
+          pass(fk.black, d.p, d.pw, (const double *)d.rhs, (const uint8_t *)d.flags, g, c,
+               d.partials_b, (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
+               (const StepState *)d.st, r.itermax);
+          pass(fk.red_graph, d.p, d.pw, (const double *)d.rhs, (const uint8_t *)d.cls, g, c,
+               d.st, d.partials_r, (const double *)d.partials_b, bb, (const BCell *)d.blist,
+               d.n_blist_b, d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
         }
       } else {
         if (d.n_pcopy > 0)

@@ -106,6 +106,10 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
 // conditional WHILE node for the red-black solve).
 // part 0: the whole step; 1: up to the RHS; 2: from the pressure solve on.
 cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *out, int part);
+// programmatic edges between the FAST loop body's colour passes in the
+// graphs built from now on; returns the previous setting
+int set_fast_pdl(int on);
+int fast_pdl();
 
 // Dense FP32 copies ([nx][ny]) of RHS and pressure and the flag bytes (any
 // output may be NULL); p += scale*q on fluid interior cells, q [nx-2][ny-2]

@@ -258,6 +258,42 @@ def test_random_layouts_fast_red_black(seed, strict, eps, omega):
     for n in ("u", "v", "p"):
         assert rel_l2(s.download(n), o.field(n)) < 1e-9, n
         assert_bits_equal(e.download(n), s.download(n), n)
+
+
+@pytest.mark.parametrize("strict", [False, True], ids=["reference_rule", "to_itermax_123"])
+def test_fast_solve_programmatic_launch_is_bitwise_neutral(strict):
+    """The FAST loop body chains its colour passes by programmatic dependent
+    launch (each pass triggers its successor's launch at once and waits for
+    its predecessor's completion itself).  Graphs built with and without
+    those edges give bit-identical iteration counts, norms and fields, both
+    when solves stop inside a body of eight iterations (the reference rule
+    on random fields: 1-3 iterations) and when they run to a max_iterations
+    that is no multiple of eight (strict eps 1e-3: 123)."""
+    from stroemung_gb300 import _lib
+    from stroemung_gb300.simulation import ARITH_FAST
+    L = _lib.load()
+    g = presets.channel(192, 48, presets.random_rectangles(192, 48, 6, seed=3))
+    rng = np.random.default_rng(5)
+    for k in ("u", "v", "p"):
+        g[k] = rng.normal(size=g[k].shape)
+    prm = dict(cell_size=(0.05, 0.05), delt=0.002, gamma=0.9, reynolds=200.0, eps=1e-3,
+               max_iterations=123, omega=1.7)
+    mode = {"sor_order": 0, "arithmetic": ARITH_FAST}
+    prev = L.strm_set_programmatic_launch(0)
+    try:
+        _, off = make_pair(g, gpu_mode=mode, strict_eps=strict, **prm)
+        assert L.strm_set_programmatic_launch(1) == 0
+        _, on = make_pair(g, gpu_mode=mode, strict_eps=strict, **prm)
+    finally:
+        L.strm_set_programmatic_launch(prev)
+    iters = []
+    for step in range(8):
+        a, b = off.run_simulation_tick(), on.run_simulation_tick()
+        assert a == b, step
+        iters.append(a[0])
+    assert all(i % 8 for i in iters) if strict else max(iters) < 8, iters
+    for n in ("u", "v", "p"):
+        assert_bits_equal(on.download(n), off.download(n), n)
     if not strict:
         assert max(iters) < prm["max_iterations"], iters
 
