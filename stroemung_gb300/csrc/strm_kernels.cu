@@ -1281,7 +1281,7 @@ __device__ __forceinline__ void sum_partials_passes(const double *pr, int n, dou
 // block's thread 0 when the pass starts (nothing changes it during the
 // pass but the last block), so that the test waits for no load of its own.
 struct SolveSnap {
-  double ns0, ns_start, fluid_cells;
+  double ns0, ns_start, inv_cells;  // inv_cells = 1 / fluid_cells
   double *hist;
   unsigned int sor_iters, hist_n, hist_cap;
 };
@@ -1290,7 +1290,10 @@ __device__ __forceinline__ SolveSnap solve_snap(const StepState *st) {
   SolveSnap sn;
   sn.ns0 = st->ns0;
   sn.ns_start = st->ns_start;
-  sn.fluid_cells = st->fluid_cells;
+  // the division happens here, when the pass starts, not in the last
+  // block's stop test: the norm is the sums times the reciprocal (within an
+  // ulp of the quotient)
+  sn.inv_cells = 1.0 / st->fluid_cells;
   sn.hist = st->hist;
   sn.sor_iters = st->sor_iters;
   sn.hist_n = st->hist_n;
@@ -1441,8 +1444,8 @@ __global__ void __launch_bounds__(256, 4)
   double s2, s1;
   sum_partials_passes<MEAN_FREE>(partials_r, gridDim.x, s2, s1);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    const double n = sn.fluid_cells;
-    const double ns = MEAN_FREE ? (s2 - s1 * (s1 / n)) / n : s2 / n;
+    const double q = sn.inv_cells;
+    const double ns = MEAN_FREE ? (s2 - s1 * (s1 * q)) * q : s2 * q;
     st->counter = 0;
     solve_iteration_done_snap<IN_GRAPH>(st, sn, ns, c, strict, itermax, h);
   }
