@@ -850,10 +850,14 @@ __global__ void __launch_bounds__(256)
 // a time and issues every load of those cells (class byte, the five
 // pressures, rhs) before it uses one: the pressure loads do not wait for the
 // class byte, and several cells' loads are in flight.  The FP64 pipe is the
-// bound; memory latency is what keeps it idle.  Three cells per batch
-// measured 0.8 % faster per step than two (a few dozen bytes of the red
-// pass spill at its 64-register bound), four 11 % slower.
-constexpr int kPassUnroll = 3;
+// bound; memory latency is what keeps it idle.  The passes run two blocks
+// of 256 threads per SM (kPassBlocksPerSm; up to 128 registers a thread)
+// with five cells per batch.  Measured per 2000-iteration step against
+// that: four blocks per SM (64 registers) with three cells 1.7 % slower and
+// with four 11 % slower (spilling), three blocks with four cells even,
+// three with five 3.6 % slower, two with six 0.9 % slower.
+constexpr int kPassUnroll = 5;
+constexpr int kPassBlocksPerSm = 2;
 
 struct PassCells {
   size_t o[kPassUnroll];
@@ -942,7 +946,7 @@ __device__ __forceinline__ void pcopy_cell(double *p, size_t o, int edge, int pi
 //     same thread.
 // The sums of the black fluid cells and of the list go to partials_b.
 template <bool MEAN_FREE, bool ALL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, kPassBlocksPerSm)
     sor_black_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                          const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
                          Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
@@ -1342,7 +1346,7 @@ __device__ __forceinline__ void solve_iteration_done_snap(StepState *st, const S
 // without it the rollback inverts the update instead (sor_unred_kernel),
 // saving the pass 8 bytes of writes per red cell.
 template <bool IN_GRAPH, bool MEAN_FREE, bool ALL, bool SAVE = true>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, kPassBlocksPerSm)
     sor_red_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                        const double *__restrict__ rhs, const uint8_t *__restrict__ cls, Geom g,
                        Consts c, StepState *st, double *__restrict__ partials_r,
@@ -2602,7 +2606,7 @@ int black_pass_blocks(const Geom &g) {
   const long long gx = (g.ny / 2 + 1 + (int)kRedBlock.x - 1) / (int)kRedBlock.x;
   const long long gy = (g.nx - 2 + (int)kRedBlock.y - 1) / (int)kRedBlock.y;
   long long n = gx * (gy > 0 ? gy : 0);
-  const long long cap = 4LL * num_sms();  // measured: more blocks ran slower
+  const long long cap = (long long)kPassBlocksPerSm * num_sms();  // one wave
   if (n > cap) n = cap;
   return n < 1 ? 1 : (int)n;
 }
