@@ -284,9 +284,10 @@ def run_reference(args):
 METRIC = "cell-updates/s (4096x1024 channel timestep, FP64 red-black SOR)"
 
 # DRAM traffic from the committed ncu captures of this workload (bytes):
-# one FP64 iteration (red pass 89.0 + 20.0 MB, black pass 72.5 + 1.1 MB)
-# and one FP32 sweep (a 4-sweep blocked launch: 38.4 + 49.9 MB).
-SOR_ITERATION_TRAFFIC = (89.0 + 20.0 + 72.5 + 1.1) * 1e6
+# one FP64 iteration (red pass 73.2 + 0.9 MB, black pass 72.5 + 0.2 MB: the
+# updated pressures stay in L2, written back later) and one FP32 sweep (a
+# 4-sweep blocked launch: 38.4 + 49.9 MB).
+SOR_ITERATION_TRAFFIC = (73.2 + 0.9 + 72.5 + 0.2) * 1e6
 SWEEP_TRAFFIC = (38.4 + 49.9) * 1e6 / 4
 
 
@@ -1322,8 +1323,10 @@ def main():
                      # passes) in one ncu capture of this workload, cold cache
                      "traffic": SOR_ITERATION_TRAFFIC,
                      "traffic_note": "ncu dram__bytes read+write of one iteration's kernels, "
-                                     "cold cache; each colour pass touches the whole of p and "
-                                     "rhs (the colours interleave within cache lines)",
+                                     "cold cache; each colour pass reads the whole of p and "
+                                     "rhs (the colours interleave within cache lines); the "
+                                     "updated pressures stay in the 129 MB L2 and are "
+                                     "written back after the pass",
                      # the pipe that binds the FP64 iteration: its FP64
                      # operations per second against the FP64 instruction
                      # rate of a DGEMM measured here (2 FLOP per FMA)
