@@ -65,3 +65,17 @@ def test_conv_launch_shape_rejects_values_out_of_range():
     for good in ((0, 0, 0, 0), (2, 6, 1, 1), (1, 32, 0, 1), (8, 2, 64, 0)):
         assert L.strm_nn_tune_conv_tma(*good) == 0, good
     assert L.strm_nn_tune_conv_tma(0, 0, 0, 1) == 0
+
+
+def test_programmatic_launch_switch_returns_the_previous_setting():
+    """strm_set_programmatic_launch only records a process-wide setting for
+    graphs built afterwards (no device call): on by default, any nonzero
+    value means on, and each call returns the setting it replaced."""
+    L = _lib.load()
+    prev = L.strm_set_programmatic_launch(0)
+    try:
+        assert prev in (0, 1)
+        assert L.strm_set_programmatic_launch(7) == 0
+        assert L.strm_set_programmatic_launch(1) == 1
+    finally:
+        L.strm_set_programmatic_launch(prev)
