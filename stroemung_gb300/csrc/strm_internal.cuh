@@ -74,6 +74,11 @@ struct StepState {
   // residual history of the current step's solve: (sweeps, norm) pairs
   double *hist;
   unsigned int hist_n, hist_cap;
+  // FAST red-black solve, written by the red pass for the next black pass:
+  // 1 / fluid_cells (from the solve's first red pass) and the iteration
+  // whose norm the black pass decides (0: none)
+  double pass_inv_cells;
+  unsigned int pass_iter;
 };
 
 // Appends (sweeps, norm) to the solve's residual history (one thread).

@@ -10,11 +10,13 @@
 //     residual_kernel  residual norm, stop test, sets the WHILE condition
 //   fast arithmetic: pcopy_kernel, sor_red_res_kernel (first red pass), then
 //   WHILE(solve not done):
-//     sor_black_res_kernel  black pass + the residual of the black cells;
-//                           saves the boundary values, copies the
+//     sor_black_res_kernel  the previous iteration's norm and stop test
+//                           (every block, from the red pass's partials),
+//                           then the black pass + the residual of the black
+//                           cells; saves the boundary values, copies the
 //                           black-coloured ones for the next iteration
 //     sor_red_res_kernel    red pass of the next iteration + this one's
-//                           residual of the red cells, norm, stop test;
+//                           residual of the red cells (partial sums);
 //                           copies the red-coloured boundary cells
 //   sor_unred_kernel, sor_rollback_kernel  undo the next iteration's red
 //                        pass and copy
@@ -129,26 +131,6 @@ __device__ double block_reduce(double v, Op op, double identity) {
 // it (acquire of the others'); the barrier then orders the block's reads.
 // The other threads' stores (field updates) need no fence here: nothing
 // reads them before the kernel ends.
-// The same with one acquire-release atomic in place of the two full fences
-// around a relaxed one: the ticket releases the partial that thread 0 stored
-// before it, and the last block's thread 0 acquires every other block's
-// (its threads then read them at L2 after the barrier).  Only for blocks
-// whose thread 0 stored everything the last block reads.
-__device__ __forceinline__ bool last_block_done_t0(unsigned int *counter) {
-  __shared__ bool am_last;
-  __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    unsigned int old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
-                 : "=r"(old)
-                 : "l"(counter)
-                 : "memory");
-    am_last = old == gridDim.x * gridDim.y - 1;
-  }
-  __syncthreads();
-  return am_last;
-}
-
 __device__ __forceinline__ bool last_block_done(unsigned int *counter) {
   __shared__ bool am_last;
   __syncthreads();
@@ -945,23 +927,67 @@ __device__ __forceinline__ void pcopy_cell(double *p, size_t o, int edge, int pi
 //     writes.  The cell's own residual is read before the copy, by the
 //     same thread.
 // The sums of the black fluid cells and of the list go to partials_b.
-template <bool MEAN_FREE, bool ALL>
+//
+// The stop test of iteration k happens here, at the start of the black pass
+// of iteration k+1, not in a last block of the red pass that the whole grid
+// would wait for: the red pass of iteration k+1 (which summed iteration k's
+// red residuals, the black pass's partials folded into its own) has
+// completed, so every block adds its nred partials in the same order, gets
+// the same norm and the same decision, and returns at once when the solve
+// stops; block 0 records the iteration (sor_iters, ns, the history, the
+// stop flags, the WHILE condition).  it = st->pass_iter (written by the red
+// pass, 0 before the solve's first black pass: nothing to decide).
+template <bool MEAN_FREE>
+__device__ __forceinline__ void sum_partials_passes(const double *pr, int n, double &s2,
+                                                    double &s1);
+__device__ __forceinline__ bool stop_rule_of(double ns, const Consts &c, double ns0,
+                                             double ns_start, int strict);
+
+template <bool IN_GRAPH, bool MEAN_FREE, bool ALL>
 __global__ void __launch_bounds__(256, kPassBlocksPerSm)
     sor_black_res_kernel(double *__restrict__ p, double *__restrict__ pw,
                          const double *__restrict__ rhs, const uint8_t *__restrict__ flags,
                          Geom g, Consts c, double *__restrict__ partials_b, int gx, int nvb,
-                         const BCell *__restrict__ bl, int nbl_b, int nbl, const StepState *st,
-                         unsigned int itermax) {
+                         const BCell *__restrict__ bl, int nbl_b, int nbl, StepState *st,
+                         unsigned int itermax, const double *partials_r, int nred, int strict,
+                         cudaGraphConditionalHandle h) {
   pdl_trigger();
   pdl_wait();
   // a later iteration of a WHILE body whose solve has stopped: nothing to do
+  // (block 0 of this pass may set the flags while another block reads them:
+  // either way that block ends as its own decision below would end it)
   if (st->converged | st->exhausted) return;
+  const unsigned int it = st->pass_iter;
+  if (it > 0) {
+    double s2, s1;
+    sum_partials_passes<MEAN_FREE>(partials_r, nred, s2, s1);
+    __shared__ int stop;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      const double q = st->pass_inv_cells;
+      const double ns = MEAN_FREE ? (s2 - s1 * (s1 * q)) * q : s2 * q;
+      const bool done = stop_rule_of(ns, c, st->ns0, st->ns_start, strict);
+      stop = done || it >= itermax;
+      if (blockIdx.x == 0) {
+        st->sor_iters = it;
+        st->ns = ns;
+        hist_push(st, it, ns);
+        st->nonfinite = !isfinite(ns);
+        if (done) st->converged = 1;
+        else if (it >= itermax) st->exhausted = 1;
+        if (IN_GRAPH && stop) cudaGraphSetConditional(h, 0);
+      }
+    }
+    __syncthreads();
+    if (stop) return;
+  }
   double accl = 0.0;  // residuals of the listed cells (ALL only, never MEAN_FREE)
   {
     const int nt = blockDim.x * blockDim.y;
     int i = blockIdx.x * nt + threadIdx.y * blockDim.x + threadIdx.x;
     if (i < nbl) {
-      const bool copy = st->sor_iters + 1 < itermax;
+      // this pass is iteration it+1; the copy of iteration it+2 runs only
+      // when there is one
+      const bool copy = it + 1 < itermax;
       for (; i < nbl; i += gridDim.x * nt) {
         const BCell e = bl[i];
         const size_t o = e.off;
@@ -1230,15 +1256,14 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------------------
 
 // The sum of the red pass's partials (each already holding the black
-// pass's partial of the same block index), on the critical path of every
-// iteration: the grid waits for this one block.  Each thread loads up to
-// four entries at once and adds them as a tree, then a tree over the block
-// (one shared-memory level, then one warp's additions and shuffles); with
-// partials of both passes and running sums this block took 2.6 us per
-// iteration, 1.3 us as trees.  Fixed order (deterministic); blocks of 256
-// threads; entries past 768 (grids above 3 blocks per thread) are added to
-// the first slot.  s2 = sum r^2, s1 = sum r (when MEAN_FREE); valid in
-// thread 0.
+// pass's partial of the same block index), taken by every block of the
+// next black pass before its cells: on the critical path of every
+// iteration.  Each thread loads up to three entries at once and adds them
+// as a tree, then a tree over the block (one shared-memory level, then one
+// warp's additions and shuffles): 8 dependent additions.  Fixed order, so
+// every block gets the same bits; blocks of 256 threads; entries past 768
+// (grids above 3 blocks per thread) are added to the first slot.  s2 = sum
+// r^2, s1 = sum r (when MEAN_FREE); valid in thread 0.
 template <bool MEAN_FREE>
 __device__ __forceinline__ void sum_partials_passes(const double *pr, int n, double &s2,
                                                     double &s1) {
@@ -1281,51 +1306,6 @@ __device__ __forceinline__ void sum_partials_passes(const double *pr, int n, dou
   }
 }
 
-// What the red pass's stop test needs of the step state, loaded by each
-// block's thread 0 when the pass starts (nothing changes it during the
-// pass but the last block), so that the test waits for no load of its own.
-struct SolveSnap {
-  double ns0, ns_start, inv_cells;  // inv_cells = 1 / fluid_cells
-  double *hist;
-  unsigned int sor_iters, hist_n, hist_cap;
-};
-
-__device__ __forceinline__ SolveSnap solve_snap(const StepState *st) {
-  SolveSnap sn;
-  sn.ns0 = st->ns0;
-  sn.ns_start = st->ns_start;
-  // the division happens here, when the pass starts, not in the last
-  // block's stop test: the norm is the sums times the reciprocal (within an
-  // ulp of the quotient)
-  sn.inv_cells = 1.0 / st->fluid_cells;
-  sn.hist = st->hist;
-  sn.sor_iters = st->sor_iters;
-  sn.hist_n = st->hist_n;
-  sn.hist_cap = st->hist_cap;
-  return sn;
-}
-
-// solve_iteration_done from a snapshot of the state (one thread).
-template <bool IN_GRAPH>
-__device__ __forceinline__ void solve_iteration_done_snap(StepState *st, const SolveSnap &sn,
-                                                          double ns, const Consts &c,
-                                                          int strict, unsigned int itermax,
-                                                          cudaGraphConditionalHandle h) {
-  const unsigned int it = sn.sor_iters + 1;
-  st->sor_iters = it;
-  st->ns = ns;
-  if (sn.hist && sn.hist_n < sn.hist_cap) {
-    sn.hist[2 * (size_t)sn.hist_n] = (double)it;
-    sn.hist[2 * (size_t)sn.hist_n + 1] = ns;
-    st->hist_n = sn.hist_n + 1;
-  }
-  st->nonfinite = !isfinite(ns);
-  const bool done = stop_rule_of(ns, c, sn.ns0, sn.ns_start, strict);
-  if (done) st->converged = 1;
-  else if (it >= itermax) st->exhausted = 1;
-  if (IN_GRAPH && (done || it >= itermax)) cudaGraphSetConditional(h, 0);
-}
-
 // Red pass.  mode 0: update only (the first red pass of a solve, and the
 // phase entry points).  mode 1 (the solve's loop): the red pass of iteration
 // k+1, which updates (saving the old value into pw) only when k < itermax
@@ -1339,9 +1319,11 @@ __device__ __forceinline__ void solve_iteration_done_snap(StepState *st, const S
 //     reading the copied cells of their stencil (BCell::mask) from pw;
 // and writes the boundary copy of iteration k+1 of the red-coloured listed
 // cells (their sources are black cells, final; red cells' stencils hold no
-// red-coloured cell, and the residuals here read copied cells from pw).  The
-// last block adds the black pass's sums and applies the stop test of
-// iteration k.
+// red-coloured cell, and the residuals here read copied cells from pw).  Each
+// block stores its sum with the black pass's partial of its index added;
+// the next black pass adds them up and applies the stop test of iteration k
+// (sor_black_res_kernel).  Block 0 sets st->pass_iter to k (0 in mode 0)
+// and, in mode 0, st->pass_inv_cells.
 // SAVE: the red cells' values before the update go to pw for the rollback;
 // without it the rollback inverts the update instead (sor_unred_kernel),
 // saving the pass 8 bytes of writes per red cell.
@@ -1358,9 +1340,14 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
   // a later iteration of a WHILE body whose solve has stopped: nothing to do
   if (mode == 1 && (st->converged | st->exhausted)) return;
   const bool sum = mode == 1;
-  const bool write = !sum || st->sor_iters + 1 < itermax;
-  __shared__ SolveSnap sn;  // written and read by thread 0 only
-  if (sum && threadIdx.x == 0 && threadIdx.y == 0) sn = solve_snap(st);
+  const unsigned int done_iters = st->sor_iters;  // k - 1: iteration k is not decided yet
+  const bool write = !sum || done_iters + 1 < itermax;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    st->pass_iter = sum ? done_iters + 1 : 0;
+    // the decisions' norms are the sums times this reciprocal (within an
+    // ulp of the quotient); the division runs once per solve
+    if (!sum) st->pass_inv_cells = 1.0 / st->fluid_cells;
+  }
   double acc = 0.0, acc1 = 0.0;
   if (sum) {
     const int nt = blockDim.x * blockDim.y;
@@ -1423,10 +1410,10 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
   }
   if (!sum) return;
   // the black pass has completed: its partial of this block index joins
-  // this block's, so that the last block sums one array (the two grids are
-  // the same size; a larger black grid's rest would go to the blocks of the
-  // same index modulo this grid).  Thread 0 loads it before the block sum,
-  // which hides the load.
+  // this block's, so that the next black pass sums one array (the two grids
+  // are the same size; a larger black grid's rest would go to the blocks of
+  // the same index modulo this grid).  Thread 0 loads it before the block
+  // sum, which hides the load.
   double pb2 = 0.0, pb1 = 0.0;
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     for (int k = blockIdx.x; k < nbb; k += gridDim.x) {
@@ -1444,15 +1431,7 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
     }
   }
   loop_guard<IN_GRAPH>(st, itermax, h);
-  if (!last_block_done_t0(&st->counter)) return;
-  double s2, s1;
-  sum_partials_passes<MEAN_FREE>(partials_r, gridDim.x, s2, s1);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    const double q = sn.inv_cells;
-    const double ns = MEAN_FREE ? (s2 - s1 * (s1 * q)) * q : s2 * q;
-    st->counter = 0;
-    solve_iteration_done_snap<IN_GRAPH>(st, sn, ns, c, strict, itermax, h);
-  }
+  (void)strict;
 }
 
 // After the solve: when it stopped at iteration k < itermax, undo the red
@@ -2622,7 +2601,7 @@ constexpr int kFastBodyIters = 8;
 // relaxation factor: the red pass saves the values it overwrites only when
 // omega is near 1 (|1 - omega| < 0.5); otherwise the rollback inverts it.
 struct FastSolveKernels {
-  const void *red_graph, *red_eager, *black;
+  const void *red_graph, *red_eager, *black_graph, *black_eager;
   bool save;
 };
 
@@ -2644,9 +2623,12 @@ static FastSolveKernels fast_solve_kernels(int strict, double one_minus_w) {
   const bool fluid = (strict & STOP_FLUID_NORM) != 0;
   const bool mf = fluid && (strict & STOP_MEAN_FREE) != 0;
   FastSolveKernels k;
-  k.black = mf      ? (const void *)sor_black_res_kernel<true, false>
-            : fluid ? (const void *)sor_black_res_kernel<false, false>
-                    : (const void *)sor_black_res_kernel<false, true>;
+  k.black_graph = mf      ? (const void *)sor_black_res_kernel<true, true, false>
+                  : fluid ? (const void *)sor_black_res_kernel<true, false, false>
+                          : (const void *)sor_black_res_kernel<true, false, true>;
+  k.black_eager = mf      ? (const void *)sor_black_res_kernel<false, true, false>
+                  : fluid ? (const void *)sor_black_res_kernel<false, false, false>
+                          : (const void *)sor_black_res_kernel<false, false, true>;
   k.save = fabs(one_minus_w) < 0.5;
   if (k.save)
     fast_red_kernels<true>(k, mf, fluid);
@@ -2929,14 +2911,15 @@ cudaError_t launch_sor_iteration(const DevFields &d, const RunCfg &r, cudaStream
         d.p, d.pw, d.rhs, d.cls, r.g, r.c, d.st, d.partials_r, d.partials_b, bb, nullptr, 0, 0,
         (int)sgrid.x, nvb, r.itermax, r.strict_eps, 0, 0);
     // (an empty boundary-cell list: the pass makes no boundary copy here)
+    // (the red pass in mode 0 leaves no iteration for the black pass to decide)
     if (mean_free)
-      sor_black_res_kernel<true, false><<<bb, kRedBlock, 0, s>>>(
+      sor_black_res_kernel<false, true, false><<<bb, kRedBlock, 0, s>>>(
           d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
-          d.st, r.itermax);
+          d.st, r.itermax, d.partials_r, bb, r.strict_eps, 0);
     else
-      sor_black_res_kernel<false, false><<<bb, kRedBlock, 0, s>>>(
+      sor_black_res_kernel<false, false, false><<<bb, kRedBlock, 0, s>>>(
           d.p, d.pw, d.rhs, d.flags, r.g, r.c, d.partials_b, (int)sgrid.x, nvb, nullptr, 0, 0,
-          d.st, r.itermax);
+          d.st, r.itermax, d.partials_r, bb, r.strict_eps, 0);
     if (norm)
       residual_kernel<false, false><<<nb, kRedBlock, 0, s>>>(
           d.p, d.rhs, d.flags, r.g, r.c, d.st, d.partials, ty, nt, 0, r.itermax, r.strict_eps,
@@ -3075,21 +3058,23 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
       const uint8_t *cls = d.cls, *flags = d.flags;
       const BCell *bl = d.blist;
       StepState *st = d.st;
-      const StepState *cst = d.st;
       Geom gg = g;
       Consts cc = c;
       int nbb_b = bb, nvb = nbb, nbl_b = d.n_blist_b, nbl = d.n_blist;
       void *red_args[] = {&p,   &pw,  &rhs,   &cls, &gg,      &cc,     &st,   &prt_r, &prt_b, &nbb_b,
                           &bl, &nbl_b, &nbl, &gx,  &nvb, &itermax, &strict, &mode, &h0};
-      void *black_args[] = {&p,  &pw,  &rhs,   &flags, &gg,  &cc,      &prt_bw, &gx,
-                            &nvb, &bl, &nbl_b, &nbl,   &cst, &itermax};
+      const double *prt_rc = d.partials_r;
+      int nred = bb;
+      void *black_args[] = {&p,   &pw,  &rhs,   &flags, &gg, &cc,      &prt_bw,
+                            &gx,  &nvb, &bl,    &nbl_b, &nbl, &st,     &itermax,
+                            &prt_rc, &nred, &strict, &h0};
       if ((e = launch_pcopy(d, g, s)) != cudaSuccess) return e;
       if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
           cudaSuccess)
         return e;
       mode = 1;
       while (!done) {
-        if ((e = cudaLaunchKernel(fk.black, dim3(bb), kRedBlock, black_args, 0, s)) !=
+        if ((e = cudaLaunchKernel(fk.black_eager, dim3(bb), kRedBlock, black_args, 0, s)) !=
             cudaSuccess)
           return e;
         if ((e = cudaLaunchKernel(fk.red_eager, dim3(bb), kRedBlock, red_args, 0, s)) !=
@@ -3402,9 +3387,9 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
                    : b.kernel(body, bn, fn, dim3(bb), kRedBlock, args...);
         };
         for (int i = 0; i < kFastBodyIters; ++i) {
-          pass(fk.black, d.p, d.pw, (const double *)d.rhs, (const uint8_t *)d.flags, g, c,
-               d.partials_b, (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b, d.n_blist,
-               (const StepState *)d.st, r.itermax);
+          pass(fk.black_graph, d.p, d.pw, (const double *)d.rhs, (const uint8_t *)d.flags, g,
+               c, d.partials_b, (int)sgrid.x, nbb, (const BCell *)d.blist, d.n_blist_b,
+               d.n_blist, d.st, r.itermax, (const double *)d.partials_r, bb, r.strict_eps, h);
           pass(fk.red_graph, d.p, d.pw, (const double *)d.rhs, (const uint8_t *)d.cls, g, c,
                d.st, d.partials_r, (const double *)d.partials_b, bb, (const BCell *)d.blist,
                d.n_blist_b, d.n_blist, (int)sgrid.x, nbb, r.itermax, r.strict_eps, 1, h);
