@@ -958,6 +958,31 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
   // either way that block ends as its own decision below would end it)
   if (st->converged | st->exhausted) return;
   const unsigned int it = st->pass_iter;
+  // The first batch's loads go out before the stop test and the boundary
+  // list, so that their latency overlaps the test's sums: they depend on
+  // neither (the list's copy writes black-coloured boundary cells, and no
+  // black fluid cell's stencil holds one).
+  const int stride = kPassUnroll * gridDim.x;
+  int vb0 = blockIdx.x;
+  PassCells cells;
+  unsigned int f[kPassUnroll];
+  double pc[kPassUnroll], pe[kPassUnroll], pwv[kPassUnroll], pn[kPassUnroll],
+      ps[kPassUnroll], rh[kPassUnroll];
+  auto load_batch = [&]() {
+    cells = pass_cells(vb0, gridDim.x, nvb, gx, 1, g);
+#pragma unroll
+    for (int u = 0; u < kPassUnroll; ++u) {
+      const size_t o = cells.o[u];
+      f[u] = flags[o];
+      pc[u] = p[o];
+      pe[u] = p[o + g.pitch];
+      pwv[u] = p[o - g.pitch];
+      ps[u] = p[o + 1];
+      pn[u] = p[o - 1];
+      rh[u] = rhs[o];
+    }
+  };
+  load_batch();
   if (it > 0) {
     double s2, s1;
     sum_partials_passes<MEAN_FREE>(partials_r, nred, s2, s1);
@@ -1008,31 +1033,19 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
     }
   }
   double acc = 0.0, acc1 = 0.0;
-  for (int vb0 = blockIdx.x; vb0 < nvb; vb0 += kPassUnroll * gridDim.x) {
-    const PassCells cells = pass_cells(vb0, gridDim.x, nvb, gx, 1, g);
-    unsigned int f[kPassUnroll];
-    double pc[kPassUnroll], pe[kPassUnroll], pw[kPassUnroll], pn[kPassUnroll], ps[kPassUnroll],
-        rh[kPassUnroll];
-#pragma unroll
-    for (int u = 0; u < kPassUnroll; ++u) {
-      const size_t o = cells.o[u];
-      f[u] = flags[o];
-      pc[u] = p[o];
-      pe[u] = p[o + g.pitch];
-      pw[u] = p[o - g.pitch];
-      ps[u] = p[o + 1];
-      pn[u] = p[o - 1];
-      rh[u] = rhs[o];
-    }
+  for (;;) {
 #pragma unroll
     for (int u = 0; u < kPassUnroll; ++u) {
       if (!cells.ok[u] || f[u] != 0) continue;
-      const double t = fma(pe[u] + pw[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
+      const double t = fma(pe[u] + pwv[u], c.r_dx2, fma(ps[u] + pn[u], c.r_dy2, -rh[u]));
       const double r0 = fma(-c.two_r_sum, pc[u], t);
       p[cells.o[u]] = fma(c.middle, r0, pc[u]);
       acc = fma(r0, r0, acc);
       if (MEAN_FREE) acc1 += r0;
     }
+    vb0 += stride;
+    if (vb0 >= nvb) break;
+    load_batch();
   }
   const double q = c.one_minus_w;
   double a = fma(acc, q * q, accl), a1 = acc1 * q;
