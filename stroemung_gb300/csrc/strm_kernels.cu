@@ -1346,7 +1346,8 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
                        const double *__restrict__ rhs, const uint8_t *__restrict__ cls, Geom g,
                        Consts c, StepState *st, double *__restrict__ partials_r,
                        const double *partials_b, int nbb, const BCell *__restrict__ bl,
-                       int nbl_b, int nbl, int gx, int nvb, unsigned int itermax, int strict,
+                       int nbl_b, int nbl, int gx, int nvb, unsigned int itermax,
+                       int /* stop rule: applied by the next black pass */,
                        int mode, cudaGraphConditionalHandle h) {
   pdl_trigger();
   pdl_wait();
@@ -1444,7 +1445,6 @@ __global__ void __launch_bounds__(256, kPassBlocksPerSm)
     }
   }
   loop_guard<IN_GRAPH>(st, itermax, h);
-  (void)strict;
 }
 
 // After the solve: when it stopped at iteration k < itermax, undo the red
