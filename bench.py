@@ -54,6 +54,9 @@ PARAMS = dict(cell_size=(0.01, 0.01), delt=0.005, gamma=0.9, reynolds=400.0,
               sor_absolute_epsilon=1e-3, max_iterations=2000, omega=1.7, tau=0.5)
 # delt is the adaptive rule's value at t = 0 (u = 1): 0.5 * min(Re/2/(2/dx^2), dx/1)
 CELLS = IMAX * JMAX
+# iterations per WHILE body of the FAST solve's step graph (the library's
+# kFastBodyIters)
+FAST_BODY_ITERS = 8
 L2_BYTES = 129e6
 # the warm-start network's parameters, trained at 512 x 128 outside the
 # benchmark (python -m stroemung_gb300.train_warmstart)
@@ -1224,10 +1227,16 @@ def main():
     value = replica_value(CELLS, args.steps, world, ms / 1e3)
     iters = [s[0] for s in stats]
     if arith == ARITH_FAST:
-        # boundary pass, F/G+RHS; copy + first red pass; per iteration black
-        # pass (+ half the next copy) and red pass (+ the other half);
-        # rollback; pressure range, velocity
-        launches = sum(2 + 2 + 2 * k + 1 + 2 for k in iters)
+        # boundary pass, F/G+RHS; copy + first red pass; the WHILE body of
+        # FAST_BODY_ITERS black and red passes, run ceil((k + 1) /
+        # FAST_BODY_ITERS) times for a solve that ends at iteration k (the
+        # black pass of iteration k+1 applies k's stop test; the passes after
+        # it return at once, but they are launched); the inverse of the last
+        # red pass (omega away from 1) and the rollback; pressure range,
+        # velocity
+        unred = 1 if abs(1.0 - PARAMS["omega"]) >= 0.5 else 0
+        launches = sum(2 + 2 + 2 * FAST_BODY_ITERS * -(-(k + 1) // FAST_BODY_ITERS)
+                       + unred + 1 + 2 for k in iters)
     else:
         # per iteration copy, red, black, residual
         launches = sum(2 + 4 * k + 2 for k in iters)

@@ -65,3 +65,16 @@ def test_reference_arm_prints_nothing_on_other_ranks(monkeypatch):
                                                ref_full_steps=1, ref_parallel=1,
                                                arith="fast"))
     assert out.getvalue() == ""
+
+
+def test_launch_count_follows_the_solve_graph():
+    """bench.py counts the kernels the FAST step graph launches from the
+    length of the solve's WHILE body, which must be the library's
+    kFastBodyIters."""
+    import re
+    from pathlib import Path
+    import bench
+    src = (Path(__file__).resolve().parent.parent / "stroemung_gb300" / "csrc" /
+           "strm_kernels.cu").read_text()
+    m = re.search(r"constexpr int kFastBodyIters = (\d+);", src)
+    assert m and int(m.group(1)) == bench.FAST_BODY_ITERS
