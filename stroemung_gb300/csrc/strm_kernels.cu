@@ -3058,8 +3058,9 @@ cudaError_t run_step_eager(const DevFields &d, const RunCfg &r, cudaStream_t s, 
                                                               nullptr, 0);
     }
     if (r.arith) {
-      // fast arithmetic: the red pass of iteration k+1 finishes iteration k's
-      // norm (see sor_red_res_kernel); the same launches as the graph
+      // fast arithmetic: the red pass of iteration k+1 sums iteration k's
+      // red residuals and the black pass of k+1 applies k's stop test (see
+      // sor_black_res_kernel); the same launches as the graph
       const FastSolveKernels fk = fast_solve_kernels(r.strict_eps, c.one_minus_w);
       const int bb = black_pass_blocks(g);
       int gx = (int)sgrid.x;
@@ -3369,7 +3370,8 @@ cudaError_t build_step_graph(const DevFields &d, const RunCfg &r, cudaGraph_t *o
     const FastSolveKernels fk = fast_solve_kernels(r.strict_eps, c.one_minus_w);
     if (r.arith) {
       // fast arithmetic: first copy and red pass outside the loop; the red
-      // pass of iteration k+1 finishes iteration k's norm (sor_red_res_kernel)
+      // pass of iteration k+1 sums iteration k's red residuals, the black
+      // pass of k+1 applies k's stop test (sor_black_res_kernel)
       if (d.n_pcopy > 0)
         n = b.kernel(b.graph, n, (const void *)pcopy_kernel, dim3((d.n_pcopy + 255) / 256),
                      dim3(256), d.p, (const PCopy *)d.pcopy, d.n_pcopy, g.pitch);
